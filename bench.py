@@ -1,0 +1,375 @@
+"""Benchmark of the sync-free triangular solve on GB300.
+
+Workload ("step"): the plain FP64 sync-free solves of the deep-vs-wide pair,
+rhs = 1, forward and backward (upper = L^T):
+  (a) lower triangle of the 5-point Laplacian on a 1414 x 1414 mesh
+      (n = 1,999,396, 5,995,360 stored entries, 2,827 level sets);
+  (b) random lower triangle, n = 4,194,304, power-law column counts
+      (alpha 2.1, cap 1000) scaled to ~38M stored entries, rows within
+      j+1..j+50,000.
+One step = 4 solves ((a) fwd, (a) bwd, (b) fwd, (b) bwd) on synthetic seeded
+inputs. The metric is effective GB/s: algorithmic bytes of each solve,
+B = 4(n+1) + nnz(4+8) + 2*8n (column pointers, row indices, values, read b,
+write x), summed over the step and divided by the step's device time. L2 is
+flushed (256 MiB write) before every solve, outside the timed events.
+
+Arms:
+  default          the library (libsptrsv_gb300.so) on cuda:LOCAL_RANK.
+  --impl reference the reference's serial CPU executor for this path (the
+                   oracle: a C restatement of SpTRSV_cuda/sptrsv_syncfree_serialref.h,
+                   or the reference build where it exists), the four solves of a
+                   step run concurrently on four host threads.
+Multi-GPU: every rank solves the same workload independently (replicas).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+for _p in (str(ROOT), str(ROOT / "benchmark-sptrsv_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "SpTRSV effective GB/s (FP64 sync-free solve, rhs=1, Laplacian-2M + power-law-4M, fwd+bwd)"
+WORKLOAD = "laplace1414_2M + powerlaw_4M, FP64, rhs=1, forward+backward (4 solves per step)"
+
+
+def bytes_pass(n: int, nnz: int, rhs: int = 1, sv: int = 8, sx: int = 8) -> int:
+    return 4 * (n + 1) + nnz * (4 + sv) + n * rhs * 2 * sx
+
+
+def make_cases():
+    from sptrsv_gb300 import matgen
+    lap = matgen.system_laplace_2m(lower=True)
+    pl = matgen.system_powerlaw_4m(seed=1, lower=True)
+    cases = []
+    for name, m in (("laplace_fwd", lap), ("laplace_bwd", lap.transpose()),
+                    ("powerlaw_fwd", pl), ("powerlaw_bwd", pl.transpose())):
+        x_true = np.ones(m.n)
+        b = m.matvec(x_true)
+        cases.append(dict(name=name, m=m, b=b))
+    return cases
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def read_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self._t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ reference (CPU) arm
+def run_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import oracle
+    imp = oracle.ref() or oracle.port()
+    kind = "reference" if imp.kind == "ref" else "port"
+    cases = make_cases()
+    degs = [imp.analyser(c["m"].row_idx, c["m"].n) for c in cases]
+    total_bytes = sum(bytes_pass(c["m"].n, c["m"].nnz) for c in cases)
+
+    def one(i):
+        c = cases[i]
+        m = c["m"]
+        return imp.executor(m.col_ptr, m.row_idx, m.val, degs[i], m.n, m.substitution, 1, c["b"])
+
+    threads = len(cases)
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        for _ in range(args.warmup):
+            list(ex.map(one, range(len(cases))))
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            xs = list(ex.map(one, range(len(cases))))
+            times.append(time.perf_counter() - t0)
+    err = max(float(np.max(np.abs(x - 1.0))) for x in xs)
+    ms = 1e3 * sum(times) / len(times)
+    value = total_bytes / (ms * 1e-3) / 1e9
+    sample = f"{args.steps} steps of the full workload (4 serial solves per step, one per thread)"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "GB/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "rhs": 1, "l2": "inputs > L2 for the power-law system; CPU arm"},
+        "cpu_baseline": {"value": round(value, 4), "unit": "GB/s", "cores": threads, "kind": kind,
+                         "sample": sample},
+        "e2e": {"value": round(value, 4), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "max_abs_err_vs_ones": err,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def cpu_baseline_sample(cases):
+    """Serial oracle on the host (1 core), bounded sample: each case solved until ~4 s each."""
+    from oracle import oracle
+    imp = oracle.ref() or oracle.port()
+    kind = "reference" if imp.kind == "ref" else "port"
+    tot_bytes, tot_s, solves = 0, 0.0, 0
+    for c in cases:
+        m = c["m"]
+        deg = imp.analyser(m.row_idx, m.n)
+        t_case = 0.0
+        while t_case < 4.0:
+            t0 = time.perf_counter()
+            imp.executor(m.col_ptr, m.row_idx, m.val, deg, m.n, m.substitution, 1, c["b"])
+            dt = time.perf_counter() - t0
+            t_case += dt
+            tot_s += dt
+            tot_bytes += bytes_pass(m.n, m.nnz)
+            solves += 1
+    return {"value": round(tot_bytes / tot_s / 1e9, 4), "unit": "GB/s", "cores": 1, "kind": kind,
+            "sample": f"{solves} serial FP64 solves over the 4 workload systems (~4 s each), 1 thread"}
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_gpu(args, world, rank, local):
+    import torch
+
+    from sptrsv_gb300 import SyncFreeSolver
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+        pg = dist
+    cases = make_cases()
+    solvers = []
+    for c in cases:
+        m = c["m"]
+        s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, values=m.val, sync_check=False,
+                           profile=True, **args.solver_kw)
+        c["solver"] = s
+        c["b_dev"] = torch.from_numpy(c["b"]).to(dev)
+        c["x_dev"] = torch.empty_like(c["b_dev"])
+        c["bytes"] = bytes_pass(m.n, m.nnz)
+        solvers.append(s)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def step(record):
+        for c in cases:
+            flush.fill_(c["bytes"] & 0xFF)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            c["solver"].solve(c["b_dev"], out=c["x_dev"])
+            e1.record(stream)
+            if record is not None:
+                record.append((c["name"], e0, e1, c))
+
+    for _ in range(args.warmup):
+        step(None)
+    for s in solvers:
+        s.check()
+    torch.cuda.synchronize()
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.2)
+    rec = []
+    exec_ms = {c["name"]: [] for c in cases}
+    t_wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        step(rec)
+        for c in cases:   # executor-kernel events of this step (waits for the kernel)
+            exec_ms[c["name"]].append(c["solver"].exec_ms())
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    clock_info = clocks.stop()
+    for s in solvers:
+        s.check()
+    per_case = {c["name"]: [] for c in cases}
+    for name, e0, e1, c in rec:
+        per_case[name].append(e0.elapsed_time(e1))
+    step_ms = sum(statistics.mean(v) for v in per_case.values())
+    if pg:
+        t = torch.tensor([step_ms], dtype=torch.float64, device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        step_ms = float(t.item())
+    total_bytes = sum(c["bytes"] for c in cases)
+    value = world * total_bytes / (step_ms * 1e-3) / 1e9
+
+    # correctness of the timed outputs (x_true = 1)
+    errs = {c["name"]: float((c["x_dev"] - 1.0).abs().max()) for c in cases}
+
+    # end to end through the public API: pinned host b -> device, solve, device -> host x
+    h2d = d2h = 0
+    for c in cases:
+        c["b_host"] = torch.from_numpy(c["b"]).pin_memory()
+        c["x_host"] = torch.empty_like(c["b_host"]).pin_memory()
+    e2e_ms = []
+    for it in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for c in cases:
+            c["b_dev"].copy_(c["b_host"], non_blocking=True)
+            c["solver"].solve(c["b_dev"], out=c["x_dev"])
+            c["x_host"].copy_(c["x_dev"], non_blocking=True)
+        torch.cuda.synchronize()
+        if it >= args.warmup:
+            e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    for c in cases:
+        h2d += c["b_host"].numel() * 8
+        d2h += c["x_host"].numel() * 8
+    e2e_step = statistics.mean(e2e_ms)
+    if pg:
+        t = torch.tensor([e2e_step], dtype=torch.float64, device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e2e_step = float(t.item())
+    e2e_val = world * total_bytes / (e2e_step * 1e-3) / 1e9
+
+    # roofline of the dominant kernel (the executor on the case with the largest share)
+    peak, peak_kind = read_peaks()
+    dom = max(cases, key=lambda c: statistics.mean(exec_ms[c["name"]]))
+    dom_ms = statistics.mean(exec_ms[dom["name"]])
+    achieved = dom["bytes"] / (dom_ms * 1e-3) / 1e9
+    info = {c["name"]: c["solver"].info() for c in cases}
+    details = {}
+    for c in cases:
+        ms = statistics.mean(per_case[c["name"]])
+        ems = statistics.mean(exec_ms[c["name"]])
+        details[c["name"]] = {
+            "n": c["m"].n, "nnz": c["m"].nnz, "nlevels": info[c["name"]]["nlevels"],
+            "solve_ms": round(ms, 4), "exec_kernel_ms": round(ems, 4),
+            "gbs": round(c["bytes"] / (ms * 1e-3) / 1e9, 2),
+            "roofline_frac": round(c["bytes"] / (ems * 1e-3) / 1e9 / peak, 5),
+            "us_per_level": round(1e3 * ems / max(info[c["name"]]["nlevels"], 1), 3),
+            "max_abs_err": errs[c["name"]], "analysis_ms": round(info[c["name"]]["analysis_ms"], 2),
+        }
+    if rank != 0:
+        return 0
+    cpu = cpu_baseline_sample(cases) if (world == 1 and not args.no_cpu_baseline) else None
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(step_ms, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generators, x_true = 1)",
+        "config": {"workload": WORKLOAD, "rhs": 1, "parallelism": f"replicas x{world}",
+                   "l2": "flushed (256 MiB write) before every solve, outside the timed events",
+                   "solver": args.solver_kw or "auto"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 3), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 5), "traffic": None, "kernel": f"executor on {dom['name']}",
+                     "peak_source": peak_kind},
+        "cpu_baseline": cpu,
+        "e2e": {"value": round(e2e_val, 3), "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": round(e2e_step, 4)},
+        "gpu_launches": args.steps * len(cases),
+        "clocks": clock_info,
+        "wall_s_timed": round(t_wall, 3),
+        "cases": details,
+    }
+    print(json.dumps(line), flush=True)
+    if pg:
+        pg.destroy_process_group()
+    return 0
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--schedule", type=int, default=None)
+    ap.add_argument("--lanes", type=int, default=None)
+    ap.add_argument("--chunk", type=int, default=None)
+    ap.add_argument("--order-block", type=int, default=None)
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        args.warmup = 3
+    kw = {}
+    for k in ("schedule", "lanes", "chunk", "order_block"):
+        v = getattr(args, k)
+        if v is not None:
+            kw[k] = v
+    args.solver_kw = kw
+    world, rank, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+    return run_gpu(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,580 @@
+// Structural analysis on the device: CSC validation, the in-degree analyser,
+// prefix scans, a stable radix sort, level sets, and the position-space
+// layouts the executors read.
+#include <algorithm>
+#include <cstdio>
+
+#include "internal.h"
+
+namespace sptrsv {
+
+namespace {
+constexpr int kThreads = 256;
+
+inline int grid_for(long long count, int threads = kThreads, int cap = 1 << 20) {
+  long long g = (count + threads - 1) / threads;
+  if (g < 1) g = 1;
+  if (g > cap) g = cap;
+  return static_cast<int>(g);
+}
+}  // namespace
+
+// ------------------------------------------------------------ validation
+__global__ void k_validate_ptr(const int* __restrict__ col_ptr, int n, int nnz, int* flags) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c <= n; c += stride) {
+    const int v = col_ptr[c];
+    bool bad = v < 0 || v > nnz;
+    if (c == 0 && v != 0) bad = true;
+    if (c == n && v != nnz) bad = true;
+    if (c < n && col_ptr[c + 1] < v) bad = true;
+    if (bad) atomicOr(flags, SF_BAD_PTR);
+  }
+}
+
+// One thread per column. Requires monotone, in-range column pointers.
+__global__ void k_validate_rows(const int* __restrict__ col_ptr, const int* __restrict__ row_idx, int n,
+                                int substitution, int* flags) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += stride) {
+    const int beg = col_ptr[c], end = col_ptr[c + 1];
+    int f = 0;
+    if (beg == end) {
+      f |= SF_MISSING_DIAG;
+    } else {
+      int prev = -1;
+      bool has_diag = false;
+      for (int e = beg; e < end; ++e) {
+        const int r = row_idx[e];
+        if (r < 0 || r >= n) { f |= SF_ROW_RANGE; break; }
+        if (r <= prev) f |= SF_UNSORTED;
+        prev = r;
+        if (r == c) has_diag = true;
+        if (substitution == 0 ? r < c : r > c) f |= SF_WRONG_TRIANGLE;
+      }
+      if (!(f & SF_ROW_RANGE)) {
+        if (!has_diag) f |= SF_MISSING_DIAG;
+        // The diagonal must open a forward column and close a backward one.
+        const int edge = substitution == 0 ? row_idx[beg] : row_idx[end - 1];
+        if (has_diag && edge != c) f |= SF_UNSORTED;
+      }
+    }
+    if (f) atomicOr(flags, f);
+  }
+}
+
+cudaError_t launch_validate_ptr(const int* col_ptr, int n, int nnz, int* flags, cudaStream_t s) {
+  k_validate_ptr<<<grid_for((long long)n + 1), kThreads, 0, s>>>(col_ptr, n, nnz, flags);
+  return cudaGetLastError();
+}
+cudaError_t launch_validate_rows(const int* col_ptr, const int* row_idx, int n, int substitution,
+                                 int* flags, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  k_validate_rows<<<grid_for(n), kThreads, 0, s>>>(col_ptr, row_idx, n, substitution, flags);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ in-degree analyser
+// inDeg[row] += 1 for every stored entry, diagonal included
+// (reference: SpTRSV_cuda/sptrsv_syncfree_cuda.h:8-19). The caller zeroes inDeg.
+__global__ void k_in_degree(const int* __restrict__ row_idx, int nnz, int* in_degree) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nnz; e += stride)
+    atomicAdd(&in_degree[row_idx[e]], 1);
+}
+cudaError_t launch_in_degree(const int* row_idx, int m, int nnz, int* in_degree, cudaStream_t s) {
+  (void)m;
+  if (nnz == 0) return cudaSuccess;
+  k_in_degree<<<grid_for(nnz), kThreads, 0, s>>>(row_idx, nnz, in_degree);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ exclusive scan
+namespace {
+constexpr int kScanThreads = 512;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int* s_warp, int* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    int w = lane < nw ? s_warp[lane] : 0;
+    int wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += t;
+    }
+    if (lane < nw) s_warp[lane] = wi - w;
+    if (lane == nw - 1) s_warp[32] = wi;
+  }
+  __syncthreads();
+  const int excl = incl - v + s_warp[warp];
+  *total = s_warp[32];
+  __syncthreads();
+  return excl;
+}
+
+__global__ void k_scan_tile_sums(const int* __restrict__ in, int count, int* sums) {
+  __shared__ int s_warp[33];
+  const long long base = (long long)blockIdx.x * kScanTile;
+  int acc = 0;
+  for (int i = 0; i < kScanItems; ++i) {
+    const long long idx = base + (long long)i * kScanThreads + threadIdx.x;
+    if (idx < count) acc += in[idx];
+  }
+  int total;
+  block_exclusive_scan(acc, s_warp, &total);
+  if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+__global__ void k_scan_tiles(const int* __restrict__ in, int* out, int count, const int* __restrict__ carry,
+                             int* total_out) {
+  __shared__ int s_vals[kScanTile];
+  __shared__ int s_warp[33];
+  const long long base = (long long)blockIdx.x * kScanTile;
+  for (int i = 0; i < kScanItems; ++i) {
+    const int li = i * kScanThreads + threadIdx.x;
+    const long long idx = base + li;
+    s_vals[li] = idx < count ? in[idx] : 0;
+  }
+  __syncthreads();
+  int local[kScanItems];
+  int acc = 0;
+  for (int i = 0; i < kScanItems; ++i) {
+    local[i] = s_vals[threadIdx.x * kScanItems + i];
+    acc += local[i];
+  }
+  int total;
+  int run = block_exclusive_scan(acc, s_warp, &total) + (carry ? carry[blockIdx.x] : 0);
+  for (int i = 0; i < kScanItems; ++i) {
+    s_vals[threadIdx.x * kScanItems + i] = run;
+    run += local[i];
+  }
+  __syncthreads();
+  for (int i = 0; i < kScanItems; ++i) {
+    const int li = i * kScanThreads + threadIdx.x;
+    const long long idx = base + li;
+    if (idx < count) out[idx] = s_vals[li];
+  }
+  if (total_out && blockIdx.x == gridDim.x - 1 && threadIdx.x == kScanThreads - 1) {
+    *total_out = run;  // last thread's running value after its items = grand total
+  }
+}
+}  // namespace
+
+cudaError_t exclusive_scan_int(const int* in, int* out, int count, bool with_total, cudaStream_t s) {
+  if (count <= 0) {
+    if (with_total) return cudaMemsetAsync(out, 0, sizeof(int), s);
+    return cudaSuccess;
+  }
+  const int tiles = (count + kScanTile - 1) / kScanTile;
+  int* total_ptr = with_total ? out + count : nullptr;
+  if (tiles == 1) {
+    k_scan_tiles<<<1, kScanThreads, 0, s>>>(in, out, count, nullptr, total_ptr);
+    return cudaGetLastError();
+  }
+  int* sums = nullptr;
+  cudaError_t err = cudaMallocAsync(reinterpret_cast<void**>(&sums), sizeof(int) * (size_t)(tiles + 1), s);
+  if (err != cudaSuccess) return err;
+  k_scan_tile_sums<<<tiles, kScanThreads, 0, s>>>(in, count, sums);
+  err = cudaGetLastError();
+  if (err == cudaSuccess) err = exclusive_scan_int(sums, sums, tiles, false, s);
+  if (err == cudaSuccess) {
+    k_scan_tiles<<<tiles, kScanThreads, 0, s>>>(in, out, count, sums, total_ptr);
+    err = cudaGetLastError();
+  }
+  cudaError_t e2 = cudaFreeAsync(sums, s);
+  return err != cudaSuccess ? err : e2;
+}
+
+// ------------------------------------------------------------ stable radix sort
+namespace {
+constexpr int kRsThreads = 256;
+constexpr int kRsItems = 8;
+constexpr int kRsTile = kRsThreads * kRsItems;
+constexpr int kRsBins = 256;
+
+__global__ void k_rs_hist(const unsigned* __restrict__ keys, int count, int shift, int* hist, int nblocks) {
+  __shared__ int s_h[kRsBins];
+  s_h[threadIdx.x] = 0;
+  __syncthreads();
+  const long long base = (long long)blockIdx.x * kRsTile;
+  for (int i = 0; i < kRsItems; ++i) {
+    const long long idx = base + (long long)i * kRsThreads + threadIdx.x;
+    if (idx < count) atomicAdd(&s_h[(keys[idx] >> shift) & 0xFFu], 1);
+  }
+  __syncthreads();
+  hist[threadIdx.x * nblocks + blockIdx.x] = s_h[threadIdx.x];
+}
+
+// Stable scatter: elements are ranked in index order within the tile (iteration
+// by iteration, warp by warp, lane by lane), so equal digits keep input order.
+__global__ void k_rs_scatter(const unsigned* __restrict__ keys_in, const int* __restrict__ vals_in,
+                             unsigned* keys_out, int* vals_out, int count, int shift,
+                             const int* __restrict__ offsets, int nblocks) {
+  constexpr int kWarps = kRsThreads / 32;
+  __shared__ int s_cnt[kWarps][kRsBins];
+  __shared__ int s_off[kWarps][kRsBins];
+  __shared__ int s_run[kRsBins];
+  __shared__ int s_base[kRsBins];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  s_run[threadIdx.x] = 0;
+  s_base[threadIdx.x] = offsets[threadIdx.x * nblocks + blockIdx.x];
+  const long long base = (long long)blockIdx.x * kRsTile;
+  for (int it = 0; it < kRsItems; ++it) {
+    for (int w = 0; w < kWarps; ++w) s_cnt[w][threadIdx.x] = 0;
+    __syncthreads();
+    const long long idx = base + (long long)it * kRsThreads + threadIdx.x;
+    const bool valid = idx < count;
+    unsigned key = 0;
+    int val = 0;
+    int digit = kRsBins;  // out-of-range elements form their own group
+    if (valid) {
+      key = keys_in[idx];
+      val = vals_in[idx];
+      digit = static_cast<int>((key >> shift) & 0xFFu);
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, digit);
+    const int rank = __popc(peers & ((1u << lane) - 1u));
+    const int leader = __ffs(peers) - 1;
+    if (valid && lane == leader) s_cnt[warp][digit] = __popc(peers);
+    __syncthreads();
+    {
+      int run = s_run[threadIdx.x];
+      for (int w = 0; w < kWarps; ++w) {
+        s_off[w][threadIdx.x] = run;
+        run += s_cnt[w][threadIdx.x];
+      }
+      s_run[threadIdx.x] = run;
+    }
+    __syncthreads();
+    if (valid) {
+      const int pos = s_base[digit] + s_off[warp][digit] + rank;
+      keys_out[pos] = key;
+      vals_out[pos] = val;
+    }
+    __syncthreads();
+  }
+}
+}  // namespace
+
+size_t radix_sort_temp_bytes(int count) {
+  const size_t nblocks = (size_t)((count + kRsTile - 1) / kRsTile);
+  // histogram (+1 for the scan total), ping-pong keys and values
+  return ((nblocks * kRsBins + 1) * sizeof(int) + 255) / 256 * 256 + (size_t)count * 8 + 512;
+}
+
+cudaError_t radix_sort_pairs(const unsigned* keys_in, const int* vals_in, unsigned* keys_out, int* vals_out,
+                             int count, int key_bits, void* temp, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  const int nblocks = (count + kRsTile - 1) / kRsTile;
+  int* hist = static_cast<int*>(temp);
+  const size_t hist_bytes = (((size_t)nblocks * kRsBins + 1) * sizeof(int) + 255) / 256 * 256;
+  unsigned* k_tmp = reinterpret_cast<unsigned*>(static_cast<char*>(temp) + hist_bytes);
+  int* v_tmp = reinterpret_cast<int*>(k_tmp + count);
+  int passes = (key_bits + 7) / 8;
+  if (passes < 1) passes = 1;
+  // Ping-pong so that the last pass lands in the output arrays.
+  const unsigned* src_k = keys_in;
+  const int* src_v = vals_in;
+  for (int p = 0; p < passes; ++p) {
+    const bool to_out = ((passes - 1 - p) % 2) == 0;
+    unsigned* dk = to_out ? keys_out : k_tmp;
+    int* dv = to_out ? vals_out : v_tmp;
+    k_rs_hist<<<nblocks, kRsThreads, 0, s>>>(src_k, count, p * 8, hist, nblocks);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    err = exclusive_scan_int(hist, hist, nblocks * kRsBins, false, s);
+    if (err != cudaSuccess) return err;
+    k_rs_scatter<<<nblocks, kRsThreads, 0, s>>>(src_k, src_v, dk, dv, count, p * 8, hist, nblocks);
+    err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    src_k = dk;
+    src_v = dv;
+  }
+  return cudaSuccess;
+}
+
+// ------------------------------------------------------------ small helpers
+__global__ void k_iota(int* out, int count, int start, int step) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += stride)
+    out[i] = start + static_cast<int>(i) * step;
+}
+cudaError_t launch_iota(int* out, int count, int start, int step, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  k_iota<<<grid_for(count), kThreads, 0, s>>>(out, count, start, step);
+  return cudaGetLastError();
+}
+
+__global__ void k_expand_cols(const int* __restrict__ col_ptr, int n, int* col_of) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += stride)
+    for (int e = col_ptr[c]; e < col_ptr[c + 1]; ++e) col_of[e] = static_cast<int>(c);
+}
+cudaError_t launch_expand_cols(const int* col_ptr, int n, int* col_of, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_expand_cols<<<grid_for(n), kThreads, 0, s>>>(col_ptr, n, col_of);
+  return cudaGetLastError();
+}
+
+__global__ void k_copy_keys(const int* __restrict__ in, unsigned* out, int count) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += stride)
+    out[i] = static_cast<unsigned>(in[i]);
+}
+cudaError_t launch_copy_keys(const int* in, unsigned* out, int count, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  k_copy_keys<<<grid_for(count), kThreads, 0, s>>>(in, out, count);
+  return cudaGetLastError();
+}
+
+__global__ void k_gather_int(const int* __restrict__ src, const int* __restrict__ idx, int* out, int count) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += stride)
+    out[i] = src[idx[i]];
+}
+cudaError_t launch_gather_int(const int* src, const int* idx, int* out, int count, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  k_gather_int<<<grid_for(count), kThreads, 0, s>>>(src, idx, out, count);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ level sets
+// Breadth-first peeling of the in-degree, one grid barrier per level
+// (the level definition of SpTRSV_cuda/findlevel.h:6-69): level 0 holds rows
+// whose only entry is the diagonal; a row joins level l+1 when the last of its
+// dependencies is visited at level l. Cooperative launch (all CTAs resident).
+__global__ void k_levels(const int* __restrict__ col_ptr, const int* __restrict__ row_idx,
+                         const int* __restrict__ in_degree, int n, int* cnt, int* front_a, int* front_b,
+                         int* depth, int* level_sizes, DeviceCtl* ctl, unsigned long long timeout_ns,
+                         int* tails /* [4]: three rotating tails + level count */) {
+  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = tid; i < n; i += stride) {
+    const int d = in_degree[i];
+    cnt[i] = d;
+    if (d == 1) {
+      const int slot = atomicAdd(&tails[0], 1);
+      front_a[slot] = static_cast<int>(i);
+      depth[i] = 0;
+    }
+  }
+  if (!grid_barrier(ctl, timeout_ns)) return;
+  int* cur = front_a;
+  int* nxt = front_b;
+  for (int level = 0;; ++level) {
+    const int cur_tail = level % 3, nxt_tail = (level + 1) % 3, free_tail = (level + 2) % 3;
+    const int size = *reinterpret_cast<volatile int*>(&tails[cur_tail]);
+    if (size == 0) {
+      if (tid == 0) tails[3] = level;
+      break;
+    }
+    if (tid == 0) {
+      level_sizes[level] = size;
+      tails[free_tail] = 0;
+    }
+    for (long long q = tid; q < size; q += stride) {
+      const int node = cur[q];
+      for (int e = col_ptr[node]; e < col_ptr[node + 1]; ++e) {
+        const int r = row_idx[e];
+        if (r == node) continue;
+        const int old = atomicSub(&cnt[r], 1);
+        if (old == 2) {
+          const int slot = atomicAdd(&tails[nxt_tail], 1);
+          nxt[slot] = r;
+          depth[r] = level + 1;
+        }
+      }
+    }
+    if (!grid_barrier(ctl, timeout_ns)) return;
+    int* t = cur;
+    cur = nxt;
+    nxt = t;
+  }
+}
+
+cudaError_t launch_levels(const int* col_ptr, const int* row_idx, const int* in_degree, int n, int* cnt_scratch,
+                          int* front_a, int* front_b, int* depth, int* level_sizes, DeviceCtl* ctl,
+                          unsigned long long timeout_ns, cudaStream_t s) {
+  // tails live right after level_sizes[n+1]
+  int* tails = level_sizes + n + 1;
+  cudaError_t err = cudaMemsetAsync(tails, 0, 4 * sizeof(int), s);
+  if (err != cudaSuccess) return err;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_levels, kThreads, 0);
+  if (per_sm < 1) per_sm = 1;
+  int grid = sms * std::min(per_sm, 4);
+  void* args[] = {(void*)&col_ptr, (void*)&row_idx, (void*)&in_degree, (void*)&n, (void*)&cnt_scratch,
+                  (void*)&front_a, (void*)&front_b, (void*)&depth, (void*)&level_sizes, (void*)&ctl,
+                  (void*)&timeout_ns, (void*)&tails};
+  return cudaLaunchCooperativeKernel((void*)k_levels, dim3(grid), dim3(kThreads), args, 0, s);
+}
+
+// ------------------------------------------------------------ schedule
+// mode 0: key = depth (level order); mode 1: key = natural position / block
+// (second, stable pass of the blocked level order).
+__global__ void k_schedule_keys(const int* __restrict__ rows, const int* __restrict__ depth, int n,
+                                int substitution, int block, int mode, unsigned* keys) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int r = rows[i];
+    if (mode == 0) {
+      keys[i] = static_cast<unsigned>(depth[r]);
+    } else {
+      const int nat = substitution == 0 ? r : n - 1 - r;
+      keys[i] = static_cast<unsigned>(nat / block);
+    }
+  }
+}
+cudaError_t launch_schedule_keys(const int* rows, const int* depth, int n, int substitution, int block, int mode,
+                                 unsigned* keys, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_schedule_keys<<<grid_for(n), kThreads, 0, s>>>(rows, depth, n, substitution, block, mode, keys);
+  return cudaGetLastError();
+}
+
+__global__ void k_inverse_perm(const int* __restrict__ perm, int n, int* iperm) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += stride)
+    iperm[perm[p]] = static_cast<int>(p);
+}
+cudaError_t launch_inverse_perm(const int* perm, int n, int* iperm, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_inverse_perm<<<grid_for(n), kThreads, 0, s>>>(perm, n, iperm);
+  return cudaGetLastError();
+}
+
+__global__ void k_dep_counts(const int* __restrict__ perm, const int* __restrict__ in_degree, int n, int* counts) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += stride)
+    counts[p] = in_degree[perm[p]] - 1;
+}
+cudaError_t launch_dep_counts(const int* perm, const int* in_degree, int n, int* counts, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_dep_counts<<<grid_for(n), kThreads, 0, s>>>(perm, in_degree, n, counts);
+  return cudaGetLastError();
+}
+
+__global__ void k_out_counts(const int* __restrict__ perm, const int* __restrict__ col_ptr, int n, int* counts) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += stride) {
+    const int c = perm[p];
+    counts[p] = col_ptr[c + 1] - col_ptr[c] - 1;
+  }
+}
+cudaError_t launch_out_counts(const int* perm, const int* col_ptr, int n, int* counts, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_out_counts<<<grid_for(n), kThreads, 0, s>>>(perm, col_ptr, n, counts);
+  return cudaGetLastError();
+}
+
+// Dependencies of position p in the order the serial executor accumulates
+// them: ascending column for a forward solve, descending for a backward one
+// (SpTRSV_cuda/sptrsv_syncfree_serialref.h:76-103 and :105-133).
+__global__ void k_fill_pull(const int* __restrict__ perm, const int* __restrict__ iperm,
+                            const int* __restrict__ csr_ptr, const int* __restrict__ csr_col,
+                            const int* __restrict__ csr_src, const int* __restrict__ dep_ptr, int n,
+                            int substitution, int* dep_pos, int* dep_src, int* diag_src) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += stride) {
+    const int r = perm[p];
+    const int beg = csr_ptr[r], end = csr_ptr[r + 1];
+    int out = dep_ptr[p];
+    if (substitution == 0) {
+      for (int k = beg; k < end - 1; ++k, ++out) {
+        dep_pos[out] = iperm[csr_col[k]];
+        dep_src[out] = csr_src[k];
+      }
+      diag_src[p] = csr_src[end - 1];
+    } else {
+      for (int k = end - 1; k > beg; --k, ++out) {
+        dep_pos[out] = iperm[csr_col[k]];
+        dep_src[out] = csr_src[k];
+      }
+      diag_src[p] = csr_src[beg];
+    }
+  }
+}
+cudaError_t launch_fill_pull(const int* perm, const int* iperm, const int* csr_ptr, const int* csr_col,
+                             const int* csr_src, const int* dep_ptr, int n, int substitution, int* dep_pos,
+                             int* dep_src, int* diag_src, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_fill_pull<<<grid_for(n), kThreads, 0, s>>>(perm, iperm, csr_ptr, csr_col, csr_src, dep_ptr, n, substitution,
+                                                dep_pos, dep_src, diag_src);
+  return cudaGetLastError();
+}
+
+__global__ void k_fill_push(const int* __restrict__ perm, const int* __restrict__ iperm,
+                            const int* __restrict__ col_ptr, const int* __restrict__ row_idx,
+                            const int* __restrict__ out_ptr, int n, int substitution, int* out_pos, int* out_src) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += stride) {
+    const int c = perm[p];
+    const int beg = col_ptr[c] + (substitution == 0 ? 1 : 0);
+    const int end = col_ptr[c + 1] - (substitution == 0 ? 0 : 1);
+    int out = out_ptr[p];
+    for (int e = beg; e < end; ++e, ++out) {
+      out_pos[out] = iperm[row_idx[e]];
+      out_src[out] = e;
+    }
+  }
+}
+cudaError_t launch_fill_push(const int* perm, const int* iperm, const int* col_ptr, const int* row_idx,
+                             const int* out_ptr, int n, int substitution, int* out_pos, int* out_src,
+                             cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_fill_push<<<grid_for(n), kThreads, 0, s>>>(perm, iperm, col_ptr, row_idx, out_ptr, n, substitution, out_pos,
+                                                out_src);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ value staging
+template <typename TV, typename T>
+__global__ void k_stage_edges(const TV* __restrict__ val, const int* __restrict__ src, T* out, int count) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += stride)
+    out[i] = static_cast<T>(val[src[i]]);
+}
+template <typename TV, typename T>
+__global__ void k_stage_diag(const TV* __restrict__ val, const int* __restrict__ diag_src, T* diag, T* rcp, int n,
+                             int* flags) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += stride) {
+    const T d = static_cast<T>(val[diag_src[p]]);
+    diag[p] = d;
+    rcp[p] = T(1) / d;
+    if (!(d != T(0)) || !isfinite(d)) atomicOr(flags, SF_ZERO_DIAG);
+  }
+}
+
+template <typename TV, typename T>
+cudaError_t launch_stage_values(const Layout& L, const TV* val, Values<T>& V, int* flags, cudaStream_t s) {
+  if (L.ndep > 0) {
+    k_stage_edges<TV, T><<<grid_for(L.ndep), kThreads, 0, s>>>(val, L.dep_src, V.dep_val, L.ndep);
+    k_stage_edges<TV, T><<<grid_for(L.ndep), kThreads, 0, s>>>(val, L.out_src, V.out_val, L.ndep);
+  }
+  if (L.n > 0) k_stage_diag<TV, T><<<grid_for(L.n), kThreads, 0, s>>>(val, L.diag_src, V.diag, V.rcp, L.n, flags);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_stage_values<double, double>(const Layout&, const double*, Values<double>&, int*,
+                                                          cudaStream_t);
+template cudaError_t launch_stage_values<double, float>(const Layout&, const double*, Values<float>&, int*,
+                                                         cudaStream_t);
+template cudaError_t launch_stage_values<float, float>(const Layout&, const float*, Values<float>&, int*,
+                                                        cudaStream_t);
+
+}  // namespace sptrsv

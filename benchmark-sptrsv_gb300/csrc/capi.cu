@@ -1,0 +1,915 @@
+// C ABI: handles, analysis pipeline, solve dispatch, status mapping, and the
+// reference-compatible host entry point.
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "../../include/sptrsv_gb300.h"
+#include "internal.h"
+
+using namespace sptrsv;
+
+namespace {
+
+int g_verbose = 0;
+int g_bench_repeat = 100;  // BENCH_REPEAT of the reference (common.h:13-15)
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace
+
+struct sptrsv_gb300_handle_s {
+  int device = 0;
+  int num_sms = 0;
+  // options
+  ExecConfig cfg;
+  int order_block = 1024;
+  long long timeout_ms = 1000;
+  int sync_check = 1;
+  int sched_option = SCHED_AUTO;
+  int lanes_option = 0;    // 0: automatic
+  int chunk_option = 0;    // 0: automatic
+  // analysis
+  bool analysed = false;
+  int n = 0, nnz = 0, substitution = 0;
+  int nlevels = 0, pmin = 0, pavg = 0, pmax = 0, max_in_degree = 0;
+  double analysis_ms = 0.0;
+  std::vector<int> level_sizes_host;
+  int* csc_ptr = nullptr;   // owned copy of the structure
+  int* csc_row = nullptr;
+  int* in_degree = nullptr;
+  int* depth = nullptr;
+  int* csr_ptr = nullptr;
+  int* csr_col = nullptr;
+  int* csr_src = nullptr;
+  int* level_item = nullptr;
+  int* level_ptr_nat = nullptr;
+  Layout layout;
+  int layout_block = -1;
+  // staged values
+  Values<double> v64;
+  Values<float> v32;
+  bool staged64 = false, staged32 = false;
+  // workspace
+  DevBuf xw, left_sum, counters;
+  DeviceCtl* ctl = nullptr;
+  int* flags = nullptr;
+  int* host_pinned = nullptr;  // 4 ints
+  int last_sched = 0;
+  size_t device_bytes = 0;
+  int profile = 0;
+  cudaEvent_t ev_exec[2] = {nullptr, nullptr};
+  bool ev_recorded = false;
+};
+
+namespace {
+
+#define CUDA_TRY(...)                                \
+  do {                                               \
+    cudaError_t e_ = (__VA_ARGS__);                  \
+    if (e_ != cudaSuccess) return map_cuda_error(e_); \
+  } while (0)
+
+#define ST_TRY(...)                \
+  do {                             \
+    int s_ = (__VA_ARGS__);        \
+    if (s_ != SPTRSV_OK) return s_; \
+  } while (0)
+
+int map_cuda_error(cudaError_t e) {
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    return SPTRSV_ERR_OOM;
+  }
+  return SPTRSV_ERR_CUDA;
+}
+
+template <typename T>
+int dev_alloc(sptrsv_gb300_handle_s* h, T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * count);
+  if (e != cudaSuccess) return map_cuda_error(e);
+  h->device_bytes += sizeof(T) * count;
+  return SPTRSV_OK;
+}
+
+template <typename T>
+void dev_free(T** p) {
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+}
+
+int bits_for(long long maxval) {
+  int b = 1;
+  while (b < 32 && (1LL << b) <= maxval) ++b;
+  return b;
+}
+
+void free_layout(Layout& L) {
+  dev_free(&L.perm);
+  dev_free(&L.iperm);
+  dev_free(&L.dep_ptr);
+  dev_free(&L.dep_pos);
+  dev_free(&L.dep_src);
+  dev_free(&L.diag_src);
+  dev_free(&L.out_ptr);
+  dev_free(&L.out_pos);
+  dev_free(&L.out_src);
+  dev_free(&L.level_ptr);
+  L = Layout();
+}
+
+template <typename T>
+void free_values(Values<T>& V) {
+  dev_free(&V.dep_val);
+  dev_free(&V.out_val);
+  dev_free(&V.diag);
+  dev_free(&V.rcp);
+}
+
+void free_analysis(sptrsv_gb300_handle_s* h) {
+  dev_free(&h->csc_ptr);
+  dev_free(&h->csc_row);
+  dev_free(&h->in_degree);
+  dev_free(&h->depth);
+  dev_free(&h->csr_ptr);
+  dev_free(&h->csr_col);
+  dev_free(&h->csr_src);
+  dev_free(&h->level_item);
+  dev_free(&h->level_ptr_nat);
+  free_layout(h->layout);
+  free_values(h->v64);
+  free_values(h->v32);
+  h->staged64 = h->staged32 = false;
+  h->analysed = false;
+  h->layout_block = -1;
+}
+
+void free_buf(DevBuf& b) {
+  if (b.p) cudaFree(b.p);
+  b = DevBuf();
+}
+
+int ensure_buf(sptrsv_gb300_handle_s* h, DevBuf& b, size_t bytes, int fill_zero, cudaStream_t s) {
+  if (b.bytes >= bytes && b.p) return SPTRSV_OK;
+  // Growing: make sure nothing in flight still uses the old buffer.
+  CUDA_TRY(cudaStreamSynchronize(s));
+  free_buf(b);
+  CUDA_TRY(cudaMalloc(&b.p, bytes));
+  b.bytes = bytes;
+  h->device_bytes += bytes;
+  if (fill_zero) CUDA_TRY(cudaMemsetAsync(b.p, 0, bytes, s));
+  return SPTRSV_OK;
+}
+
+unsigned long long timeout_ns(const sptrsv_gb300_handle_s* h) {
+  return static_cast<unsigned long long>(h->timeout_ms) * 1000000ull;
+}
+
+// Clears the control block and the self-cleaning push workspace after a
+// failed launch left them dirty.
+int reset_after_failure(sptrsv_gb300_handle_s* h, cudaStream_t s) {
+  cudaGetLastError();
+  CUDA_TRY(cudaMemsetAsync(h->ctl, 0, sizeof(DeviceCtl), s));
+  if (h->left_sum.p) CUDA_TRY(cudaMemsetAsync(h->left_sum.p, 0, h->left_sum.bytes, s));
+  if (h->counters.p) CUDA_TRY(cudaMemsetAsync(h->counters.p, 0, h->counters.bytes, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  return SPTRSV_OK;
+}
+
+int read_device_code(sptrsv_gb300_handle_s* h, cudaStream_t s, int* code) {
+  CUDA_TRY(cudaMemcpyAsync(h->host_pinned, &h->ctl->code, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  *code = h->host_pinned[0];
+  return SPTRSV_OK;
+}
+
+int check_device(sptrsv_gb300_handle_s* h, cudaStream_t s) {
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return map_cuda_error(e);
+  int code = 0;
+  ST_TRY(read_device_code(h, s, &code));
+  if (code != DEV_OK) {
+    ST_TRY(reset_after_failure(h, s));
+    return code == DEV_TIMEOUT ? SPTRSV_ERR_TIMEOUT : SPTRSV_ERR_CUDA;
+  }
+  return SPTRSV_OK;
+}
+
+int read_flags(sptrsv_gb300_handle_s* h, cudaStream_t s, int* flags) {
+  CUDA_TRY(cudaMemcpyAsync(h->host_pinned + 1, h->flags, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  *flags = h->host_pinned[1];
+  return SPTRSV_OK;
+}
+
+// Builds the position-space layout for the given order block.
+int build_layout(sptrsv_gb300_handle_s* h, int block, cudaStream_t s) {
+  free_layout(h->layout);
+  free_values(h->v64);
+  free_values(h->v32);
+  h->staged64 = h->staged32 = false;
+  Layout& L = h->layout;
+  const int n = h->n;
+  const int ndep = h->nnz - n;
+  L.n = n;
+  L.ndep = ndep;
+  ST_TRY(dev_alloc(h, &L.perm, n));
+  ST_TRY(dev_alloc(h, &L.iperm, n));
+  ST_TRY(dev_alloc(h, &L.dep_ptr, (size_t)n + 1));
+  ST_TRY(dev_alloc(h, &L.out_ptr, (size_t)n + 1));
+  ST_TRY(dev_alloc(h, &L.dep_pos, ndep));
+  ST_TRY(dev_alloc(h, &L.dep_src, ndep));
+  ST_TRY(dev_alloc(h, &L.out_pos, ndep));
+  ST_TRY(dev_alloc(h, &L.out_src, ndep));
+  ST_TRY(dev_alloc(h, &L.diag_src, n));
+
+  const bool level_order = block >= n;
+  if (n > 0) {
+    // natural order rows
+    int* rows_nat = nullptr;
+    CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&rows_nat), sizeof(int) * n, s));
+    CUDA_TRY(h->substitution == 0 ? launch_iota(rows_nat, n, 0, 1, s) : launch_iota(rows_nat, n, n - 1, -1, s));
+    if (block <= 1) {
+      CUDA_TRY(cudaMemcpyAsync(L.perm, rows_nat, sizeof(int) * n, cudaMemcpyDeviceToDevice, s));
+    } else {
+      unsigned *keys = nullptr, *keys_sorted = nullptr;
+      int* rows_lv = nullptr;
+      void* temp = nullptr;
+      CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&keys), sizeof(unsigned) * n, s));
+      CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&keys_sorted), sizeof(unsigned) * n, s));
+      CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&rows_lv), sizeof(int) * n, s));
+      CUDA_TRY(cudaMallocAsync(&temp, radix_sort_temp_bytes(n), s));
+      CUDA_TRY(launch_schedule_keys(rows_nat, h->depth, n, h->substitution, block, 0, keys, s));
+      CUDA_TRY(radix_sort_pairs(keys, rows_nat, keys_sorted, level_order ? L.perm : rows_lv, n,
+                                bits_for(h->nlevels - 1), temp, s));
+      if (!level_order) {
+        CUDA_TRY(launch_schedule_keys(rows_lv, h->depth, n, h->substitution, block, 1, keys, s));
+        CUDA_TRY(radix_sort_pairs(keys, rows_lv, keys_sorted, L.perm, n, bits_for((n - 1) / block), temp, s));
+      }
+      CUDA_TRY(cudaFreeAsync(keys, s));
+      CUDA_TRY(cudaFreeAsync(keys_sorted, s));
+      CUDA_TRY(cudaFreeAsync(rows_lv, s));
+      CUDA_TRY(cudaFreeAsync(temp, s));
+    }
+    CUDA_TRY(cudaFreeAsync(rows_nat, s));
+    CUDA_TRY(launch_inverse_perm(L.perm, n, L.iperm, s));
+    CUDA_TRY(launch_dep_counts(L.perm, h->in_degree, n, L.dep_ptr, s));
+    CUDA_TRY(exclusive_scan_int(L.dep_ptr, L.dep_ptr, n, true, s));
+    CUDA_TRY(launch_out_counts(L.perm, h->csc_ptr, n, L.out_ptr, s));
+    CUDA_TRY(exclusive_scan_int(L.out_ptr, L.out_ptr, n, true, s));
+    CUDA_TRY(launch_fill_pull(L.perm, L.iperm, h->csr_ptr, h->csr_col, h->csr_src, L.dep_ptr, n, h->substitution,
+                              L.dep_pos, L.dep_src, L.diag_src, s));
+    CUDA_TRY(launch_fill_push(L.perm, L.iperm, h->csc_ptr, h->csc_row, L.out_ptr, n, h->substitution, L.out_pos,
+                              L.out_src, s));
+  }
+  if (level_order) {
+    L.nlevels = h->nlevels;
+    L.level_ptr_host.assign(h->nlevels + 1, 0);
+    for (int l = 0; l < h->nlevels; ++l) L.level_ptr_host[l + 1] = L.level_ptr_host[l] + h->level_sizes_host[l];
+    ST_TRY(dev_alloc(h, &L.level_ptr, (size_t)h->nlevels + 1));
+    CUDA_TRY(cudaMemcpyAsync(L.level_ptr, L.level_ptr_host.data(), sizeof(int) * (h->nlevels + 1),
+                             cudaMemcpyHostToDevice, s));
+  }
+  CUDA_TRY(cudaStreamSynchronize(s));
+  h->layout_block = block;
+  return SPTRSV_OK;
+}
+
+int effective_block(const sptrsv_gb300_handle_s* h) {
+  if (h->sched_option == SCHED_LEVELSET) return INT_MAX;
+  return h->order_block;
+}
+
+int ensure_layout(sptrsv_gb300_handle_s* h, cudaStream_t s) {
+  const int want = effective_block(h);
+  const int have = h->layout_block;
+  const bool same = (want >= h->n && have >= h->n) || want == have;
+  if (same && h->layout.perm != nullptr) return SPTRSV_OK;
+  if (h->n == 0 && have >= 0) return SPTRSV_OK;
+  return build_layout(h, want, s);
+}
+
+template <typename TV, typename T>
+int stage(sptrsv_gb300_handle_s* h, Values<T>& V, const TV* val, cudaStream_t s, bool check) {
+  const Layout& L = h->layout;
+  if (!V.dep_val) {
+    ST_TRY(dev_alloc(h, &V.dep_val, L.ndep));
+    ST_TRY(dev_alloc(h, &V.out_val, L.ndep));
+    ST_TRY(dev_alloc(h, &V.diag, L.n));
+    ST_TRY(dev_alloc(h, &V.rcp, L.n));
+  }
+  if (check) CUDA_TRY(cudaMemsetAsync(h->flags, 0, sizeof(int), s));
+  CUDA_TRY(launch_stage_values<TV, T>(L, val, V, h->flags, s));
+  if (check) {
+    int f = 0;
+    ST_TRY(read_flags(h, s, &f));
+    if (f & SF_ZERO_DIAG) return SPTRSV_ERR_BAD_STRUCTURE;
+  }
+  return SPTRSV_OK;
+}
+
+int stage_values(sptrsv_gb300_handle_s* h, const void* d_val, int dtype, cudaStream_t s, bool check) {
+  if (dtype == SPTRSV_DTYPE_F64) {
+    ST_TRY(stage<double, double>(h, h->v64, static_cast<const double*>(d_val), s, check));
+    ST_TRY(stage<double, float>(h, h->v32, static_cast<const double*>(d_val), s, false));
+    h->staged64 = h->staged32 = true;
+  } else if (dtype == SPTRSV_DTYPE_F32) {
+    ST_TRY(stage<float, float>(h, h->v32, static_cast<const float*>(d_val), s, check));
+    h->staged32 = true;
+    h->staged64 = false;
+  } else {
+    return SPTRSV_ERR_INVALID;
+  }
+  return SPTRSV_OK;
+}
+
+// Automatic executor settings for a request.
+ExecConfig pick_config(const sptrsv_gb300_handle_s* h, int rhs) {
+  ExecConfig c = h->cfg;
+  c.sched = h->sched_option == SCHED_AUTO ? SCHED_PULL : h->sched_option;
+  c.lanes = h->lanes_option > 0 ? h->lanes_option : 1;
+  c.chunk = h->chunk_option > 0 ? h->chunk_option : (rhs == 1 ? 1024 : 256);
+  return c;
+}
+
+template <typename T>
+int solve_typed(sptrsv_gb300_handle_s* h, const Values<T>& V, int rhs, int layout, const T* b, T* x,
+                cudaStream_t s) {
+  const int n = h->n;
+  VecView<T> v{};
+  v.b = b;
+  v.x = x;
+  if (layout == SPTRSV_LAYOUT_ROW_MAJOR) {
+    v.b_si = v.x_si = rhs;
+    v.b_sk = v.x_sk = 1;
+  } else {
+    v.b_si = v.x_si = 1;
+    v.b_sk = v.x_sk = n;
+  }
+  ExecConfig c = pick_config(h, rhs);
+  h->last_sched = c.sched;
+  const size_t elems = (size_t)n * (size_t)rhs;
+  if (c.sched == SCHED_PUSH) {
+    ST_TRY(ensure_buf(h, h->left_sum, elems * sizeof(T), 1, s));
+    ST_TRY(ensure_buf(h, h->counters, (size_t)n * sizeof(unsigned), 1, s));
+  } else {
+    ST_TRY(ensure_buf(h, h->xw, elems * sizeof(T), 0, s));
+    if (c.sched != SCHED_LEVELSET) CUDA_TRY(cudaMemsetAsync(h->xw.p, 0xFF, elems * sizeof(T), s));
+  }
+  if (h->profile) {
+    if (!h->ev_exec[0]) {
+      CUDA_TRY(cudaEventCreate(&h->ev_exec[0]));
+      CUDA_TRY(cudaEventCreate(&h->ev_exec[1]));
+    }
+    CUDA_TRY(cudaEventRecord(h->ev_exec[0], s));
+  }
+  if (c.sched == SCHED_PUSH) {
+    CUDA_TRY(launch_push<T>(h->layout, V, rhs, v, static_cast<T*>(h->left_sum.p),
+                            static_cast<unsigned*>(h->counters.p), h->ctl, c, timeout_ns(h), h->num_sms, s));
+  } else if (c.sched == SCHED_LEVELSET) {
+    CUDA_TRY(launch_levelset<T>(h->layout, V, rhs, v, static_cast<T*>(h->xw.p), h->ctl, c, timeout_ns(h), s));
+  } else {
+    CUDA_TRY(launch_pull<T>(h->layout, V, rhs, v, static_cast<T*>(h->xw.p), h->ctl, c, timeout_ns(h), h->num_sms,
+                            s));
+  }
+  if (h->profile) {
+    CUDA_TRY(cudaEventRecord(h->ev_exec[1], s));
+    h->ev_recorded = true;
+  }
+  if (h->sync_check) return check_device(h, s);
+  return SPTRSV_OK;
+}
+
+std::mutex g_raw_mutex;
+DeviceCtl* g_raw_ctl[64] = {nullptr};
+
+int raw_ctl(DeviceCtl** out) {
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return SPTRSV_ERR_INVALID;
+  std::lock_guard<std::mutex> lock(g_raw_mutex);
+  if (!g_raw_ctl[dev]) {
+    DeviceCtl* c = nullptr;
+    CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&c), sizeof(DeviceCtl)));
+    CUDA_TRY(cudaMemset(c, 0, sizeof(DeviceCtl)));
+    g_raw_ctl[dev] = c;
+  }
+  *out = g_raw_ctl[dev];
+  return SPTRSV_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* sptrsv_gb300_status_string(int status) {
+  switch (status) {
+    case SPTRSV_OK: return "ok";
+    case SPTRSV_ERR_NOT_SQUARE: return "matrix is not square";
+    case SPTRSV_ERR_BAD_STRUCTURE: return "malformed triangular CSC structure or zero diagonal";
+    case SPTRSV_ERR_INVALID: return "invalid argument";
+    case SPTRSV_ERR_CUDA: return "CUDA runtime error";
+    case SPTRSV_ERR_TIMEOUT: return "bounded device wait ran out";
+    case SPTRSV_ERR_OOM: return "device out of memory";
+    case SPTRSV_ERR_STATE: return "call out of order";
+    case SPTRSV_ERR_NOT_CONVERGED: return "iterative refinement did not converge";
+    case SPTRSV_ERR_UNSUPPORTED: return "unsupported request";
+    default: return "unknown status";
+  }
+}
+
+int sptrsv_gb300_version(void) { return SPTRSV_GB300_VERSION; }
+
+void sptrsv_gb300_set_verbose(int verbose) { g_verbose = verbose; }
+void sptrsv_gb300_set_bench_repeat(int repeat) { g_bench_repeat = repeat > 0 ? repeat : 1; }
+
+int sptrsv_gb300_create(sptrsv_handle_t* handle) {
+  if (!handle) return SPTRSV_ERR_INVALID;
+  *handle = nullptr;
+  auto* h = new (std::nothrow) sptrsv_gb300_handle_s();
+  if (!h) return SPTRSV_ERR_OOM;
+  cudaError_t e = cudaGetDevice(&h->device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
+  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&h->ctl), sizeof(DeviceCtl));
+  if (e == cudaSuccess) e = cudaMemset(h->ctl, 0, sizeof(DeviceCtl));
+  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&h->flags), sizeof(int));
+  if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&h->host_pinned), 4 * sizeof(int));
+  if (e != cudaSuccess) {
+    if (h->ctl) cudaFree(h->ctl);
+    if (h->flags) cudaFree(h->flags);
+    delete h;
+    return map_cuda_error(e);
+  }
+  *handle = h;
+  return SPTRSV_OK;
+}
+
+int sptrsv_gb300_destroy(sptrsv_handle_t h) {
+  if (!h) return SPTRSV_ERR_INVALID;
+  cudaDeviceSynchronize();
+  free_analysis(h);
+  free_buf(h->xw);
+  free_buf(h->left_sum);
+  free_buf(h->counters);
+  if (h->ctl) cudaFree(h->ctl);
+  if (h->flags) cudaFree(h->flags);
+  if (h->host_pinned) cudaFreeHost(h->host_pinned);
+  if (h->ev_exec[0]) cudaEventDestroy(h->ev_exec[0]);
+  if (h->ev_exec[1]) cudaEventDestroy(h->ev_exec[1]);
+  delete h;
+  return SPTRSV_OK;
+}
+
+int sptrsv_gb300_set_option(sptrsv_handle_t h, int option, long long value) {
+  if (!h) return SPTRSV_ERR_INVALID;
+  switch (option) {
+    case SPTRSV_OPTION_SCHEDULE:
+      if (value < SCHED_AUTO || value > SCHED_LEVELSET) return SPTRSV_ERR_INVALID;
+      h->sched_option = static_cast<int>(value);
+      return SPTRSV_OK;
+    case SPTRSV_OPTION_LANES:
+      if (!(value == 0 || value == 1 || value == 2 || value == 4 || value == 8 || value == 16 || value == 32))
+        return SPTRSV_ERR_INVALID;
+      h->lanes_option = static_cast<int>(value);
+      return SPTRSV_OK;
+    case SPTRSV_OPTION_CHUNK:
+      if (value < 0 || value > (1 << 20)) return SPTRSV_ERR_INVALID;
+      h->chunk_option = static_cast<int>(value);
+      return SPTRSV_OK;
+    case SPTRSV_OPTION_SMEM_TIER:
+      h->cfg.smem_tier = value != 0;
+      return SPTRSV_OK;
+    case SPTRSV_OPTION_EXACT:
+      h->cfg.exact = value != 0;
+      return SPTRSV_OK;
+    case SPTRSV_OPTION_ORDER_BLOCK:
+      if (value < 1) return SPTRSV_ERR_INVALID;
+      h->order_block = value > INT_MAX ? INT_MAX : static_cast<int>(value);
+      return SPTRSV_OK;
+    case SPTRSV_OPTION_TIMEOUT_MS:
+      if (value < 1) return SPTRSV_ERR_INVALID;
+      h->timeout_ms = value;
+      return SPTRSV_OK;
+    case SPTRSV_OPTION_SYNC_CHECK:
+      h->sync_check = value != 0;
+      return SPTRSV_OK;
+    case SPTRSV_OPTION_PROFILE:
+      h->profile = value != 0;
+      return SPTRSV_OK;
+    default:
+      return SPTRSV_ERR_INVALID;
+  }
+}
+
+int sptrsv_gb300_get_option(sptrsv_handle_t h, int option, long long* value) {
+  if (!h || !value) return SPTRSV_ERR_INVALID;
+  switch (option) {
+    case SPTRSV_OPTION_SCHEDULE: *value = h->sched_option; break;
+    case SPTRSV_OPTION_LANES: *value = h->lanes_option; break;
+    case SPTRSV_OPTION_CHUNK: *value = h->chunk_option; break;
+    case SPTRSV_OPTION_SMEM_TIER: *value = h->cfg.smem_tier; break;
+    case SPTRSV_OPTION_EXACT: *value = h->cfg.exact; break;
+    case SPTRSV_OPTION_ORDER_BLOCK: *value = h->order_block; break;
+    case SPTRSV_OPTION_TIMEOUT_MS: *value = h->timeout_ms; break;
+    case SPTRSV_OPTION_SYNC_CHECK: *value = h->sync_check; break;
+    case SPTRSV_OPTION_PROFILE: *value = h->profile; break;
+    default: return SPTRSV_ERR_INVALID;
+  }
+  return SPTRSV_OK;
+}
+
+int sptrsv_gb300_analyse(sptrsv_handle_t h, int m, int n, int nnz, const int* d_colPtr, const int* d_rowIdx,
+                         int substitution, void* stream) {
+  if (!h) return SPTRSV_ERR_INVALID;
+  if (m != n) return SPTRSV_ERR_NOT_SQUARE;
+  if (n < 0 || nnz < 0 || (substitution != 0 && substitution != 1)) return SPTRSV_ERR_INVALID;
+  if (nnz < n) return SPTRSV_ERR_BAD_STRUCTURE;  // a diagonal per column at least
+  if (n > 0 && (!d_colPtr || (nnz > 0 && !d_rowIdx))) return SPTRSV_ERR_INVALID;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  free_analysis(h);
+  h->n = n;
+  h->nnz = nnz;
+  h->substitution = substitution;
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  CUDA_TRY(cudaEventRecord(e0, s));
+
+  // 1. structure validation (pointers first, then rows)
+  CUDA_TRY(cudaMemsetAsync(h->flags, 0, sizeof(int), s));
+  CUDA_TRY(launch_validate_ptr(d_colPtr, n, nnz, h->flags, s));
+  int f = 0;
+  ST_TRY(read_flags(h, s, &f));
+  if (f) return SPTRSV_ERR_BAD_STRUCTURE;
+  CUDA_TRY(launch_validate_rows(d_colPtr, d_rowIdx, n, substitution, h->flags, s));
+  ST_TRY(read_flags(h, s, &f));
+  if (f) return SPTRSV_ERR_BAD_STRUCTURE;
+
+  // 2. owned copy of the structure, in-degree analyser
+  ST_TRY(dev_alloc(h, &h->csc_ptr, (size_t)n + 1));
+  ST_TRY(dev_alloc(h, &h->csc_row, nnz));
+  CUDA_TRY(cudaMemcpyAsync(h->csc_ptr, d_colPtr, sizeof(int) * ((size_t)n + 1), cudaMemcpyDeviceToDevice, s));
+  if (nnz) CUDA_TRY(cudaMemcpyAsync(h->csc_row, d_rowIdx, sizeof(int) * (size_t)nnz, cudaMemcpyDeviceToDevice, s));
+  ST_TRY(dev_alloc(h, &h->in_degree, n));
+  CUDA_TRY(cudaMemsetAsync(h->in_degree, 0, sizeof(int) * (size_t)(n > 0 ? n : 1), s));
+  CUDA_TRY(launch_in_degree(h->csc_row, n, nnz, h->in_degree, s));
+
+  // 3. CSR transpose by a stable sort of the CSC entries on their row
+  ST_TRY(dev_alloc(h, &h->csr_ptr, (size_t)n + 1));
+  ST_TRY(dev_alloc(h, &h->csr_col, nnz));
+  ST_TRY(dev_alloc(h, &h->csr_src, nnz));
+  CUDA_TRY(exclusive_scan_int(h->in_degree, h->csr_ptr, n, true, s));
+  if (nnz > 0) {
+    unsigned *keys = nullptr, *keys_sorted = nullptr;
+    int *iota = nullptr, *col_of = nullptr;
+    void* temp = nullptr;
+    CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&keys), sizeof(unsigned) * nnz, s));
+    CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&keys_sorted), sizeof(unsigned) * nnz, s));
+    CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&iota), sizeof(int) * nnz, s));
+    CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&col_of), sizeof(int) * nnz, s));
+    CUDA_TRY(cudaMallocAsync(&temp, radix_sort_temp_bytes(nnz), s));
+    CUDA_TRY(launch_copy_keys(h->csc_row, keys, nnz, s));
+    CUDA_TRY(launch_iota(iota, nnz, 0, 1, s));
+    CUDA_TRY(radix_sort_pairs(keys, iota, keys_sorted, h->csr_src, nnz, bits_for(n - 1), temp, s));
+    CUDA_TRY(launch_expand_cols(h->csc_ptr, n, col_of, s));
+    CUDA_TRY(launch_gather_int(col_of, h->csr_src, h->csr_col, nnz, s));
+    CUDA_TRY(cudaFreeAsync(keys, s));
+    CUDA_TRY(cudaFreeAsync(keys_sorted, s));
+    CUDA_TRY(cudaFreeAsync(iota, s));
+    CUDA_TRY(cudaFreeAsync(col_of, s));
+    CUDA_TRY(cudaFreeAsync(temp, s));
+  }
+
+  // 4. level sets
+  ST_TRY(dev_alloc(h, &h->depth, n));
+  h->nlevels = 0;
+  h->level_sizes_host.clear();
+  if (n > 0) {
+    int *cnt = nullptr, *fa = nullptr, *fb = nullptr, *sizes = nullptr;
+    CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&cnt), sizeof(int) * n, s));
+    CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&fa), sizeof(int) * n, s));
+    CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&fb), sizeof(int) * n, s));
+    CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&sizes), sizeof(int) * ((size_t)n + 5), s));
+    CUDA_TRY(launch_levels(h->csc_ptr, h->csc_row, h->in_degree, n, cnt, fa, fb, h->depth, sizes, h->ctl,
+                           timeout_ns(h), s));
+    int code = 0;
+    ST_TRY(read_device_code(h, s, &code));
+    if (code != DEV_OK) {
+      ST_TRY(reset_after_failure(h, s));
+      return SPTRSV_ERR_TIMEOUT;
+    }
+    int nl = 0;
+    CUDA_TRY(cudaMemcpyAsync(h->host_pinned + 2, sizes + n + 1 + 3, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    nl = h->host_pinned[2];
+    if (nl < 1 || nl > n) return SPTRSV_ERR_BAD_STRUCTURE;
+    h->level_sizes_host.resize(nl);
+    CUDA_TRY(cudaMemcpy(h->level_sizes_host.data(), sizes, sizeof(int) * nl, cudaMemcpyDeviceToHost));
+    long long total = 0;
+    for (int l = 0; l < nl; ++l) total += h->level_sizes_host[l];
+    if (total != n) return SPTRSV_ERR_BAD_STRUCTURE;
+    h->nlevels = nl;
+    // findlevel_csc statistics (findlevel.h:123-136)
+    int lo = h->level_sizes_host[0], hi = lo;
+    for (int l = 1; l < nl; ++l) {
+      const int c = h->level_sizes_host[l];
+      if (c > hi) hi = c;
+      else if (c < lo) lo = c;
+    }
+    h->pmin = lo;
+    h->pmax = hi;
+    h->pavg = n / nl;
+    CUDA_TRY(cudaFreeAsync(cnt, s));
+    CUDA_TRY(cudaFreeAsync(fa, s));
+    CUDA_TRY(cudaFreeAsync(fb, s));
+    CUDA_TRY(cudaFreeAsync(sizes, s));
+
+    // level items: rows sorted by (level, row)
+    ST_TRY(dev_alloc(h, &h->level_item, n));
+    ST_TRY(dev_alloc(h, &h->level_ptr_nat, (size_t)nl + 1));
+    std::vector<int> lp(nl + 1, 0);
+    for (int l = 0; l < nl; ++l) lp[l + 1] = lp[l] + h->level_sizes_host[l];
+    CUDA_TRY(cudaMemcpyAsync(h->level_ptr_nat, lp.data(), sizeof(int) * (nl + 1), cudaMemcpyHostToDevice, s));
+    unsigned *keys = nullptr, *keys_sorted = nullptr;
+    int* iota = nullptr;
+    void* temp = nullptr;
+    CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&keys), sizeof(unsigned) * n, s));
+    CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&keys_sorted), sizeof(unsigned) * n, s));
+    CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&iota), sizeof(int) * n, s));
+    CUDA_TRY(cudaMallocAsync(&temp, radix_sort_temp_bytes(n), s));
+    CUDA_TRY(launch_iota(iota, n, 0, 1, s));
+    CUDA_TRY(launch_schedule_keys(iota, h->depth, n, 0, 1, 0, keys, s));
+    CUDA_TRY(radix_sort_pairs(keys, iota, keys_sorted, h->level_item, n, bits_for(nl - 1), temp, s));
+    CUDA_TRY(cudaFreeAsync(keys, s));
+    CUDA_TRY(cudaFreeAsync(keys_sorted, s));
+    CUDA_TRY(cudaFreeAsync(iota, s));
+    CUDA_TRY(cudaFreeAsync(temp, s));
+  }
+  // max in-degree (host pass over a small copy is avoided: derive from CSR pointers)
+  h->max_in_degree = 0;
+  if (n > 0) {
+    std::vector<int> rp((size_t)n + 1);
+    CUDA_TRY(cudaMemcpyAsync(rp.data(), h->csr_ptr, sizeof(int) * ((size_t)n + 1), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    for (int i = 0; i < n; ++i) h->max_in_degree = std::max(h->max_in_degree, rp[i + 1] - rp[i]);
+  }
+  h->analysed = true;
+  // 5. execution schedule and layouts
+  ST_TRY(build_layout(h, effective_block(h), s));
+  CUDA_TRY(cudaEventRecord(e1, s));
+  CUDA_TRY(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  h->analysis_ms = ms;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return SPTRSV_OK;
+}
+
+int sptrsv_gb300_get_info(sptrsv_handle_t h, sptrsv_info* info) {
+  if (!h || !info) return SPTRSV_ERR_INVALID;
+  std::memset(info, 0, sizeof(*info));
+  info->n = h->n;
+  info->nnz = h->nnz;
+  info->substitution = h->substitution;
+  info->nlevels = h->nlevels;
+  info->parallelism_min = h->pmin;
+  info->parallelism_avg = h->pavg;
+  info->parallelism_max = h->pmax;
+  info->max_in_degree = h->max_in_degree;
+  ExecConfig c = pick_config(h, 1);
+  info->schedule = h->last_sched ? h->last_sched : c.sched;
+  info->lanes = c.lanes;
+  info->chunk = c.chunk;
+  info->order_block = h->layout_block;
+  info->analysis_ms = h->analysis_ms;
+  info->device_bytes = h->device_bytes;
+  return h->analysed ? SPTRSV_OK : SPTRSV_ERR_STATE;
+}
+
+int sptrsv_gb300_levels(sptrsv_handle_t h, int* d_levelPtr, int* d_levelItem, void* stream) {
+  if (!h) return SPTRSV_ERR_INVALID;
+  if (!h->analysed) return SPTRSV_ERR_STATE;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (h->n == 0) return SPTRSV_OK;
+  if (d_levelPtr)
+    CUDA_TRY(cudaMemcpyAsync(d_levelPtr, h->level_ptr_nat, sizeof(int) * (h->nlevels + 1), cudaMemcpyDeviceToDevice, s));
+  if (d_levelItem)
+    CUDA_TRY(cudaMemcpyAsync(d_levelItem, h->level_item, sizeof(int) * h->n, cudaMemcpyDeviceToDevice, s));
+  return SPTRSV_OK;
+}
+
+int sptrsv_gb300_csr(sptrsv_handle_t h, int* d_rowPtr, int* d_colIdx, int* d_srcIdx, void* stream) {
+  if (!h) return SPTRSV_ERR_INVALID;
+  if (!h->analysed) return SPTRSV_ERR_STATE;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (d_rowPtr)
+    CUDA_TRY(cudaMemcpyAsync(d_rowPtr, h->csr_ptr, sizeof(int) * ((size_t)h->n + 1), cudaMemcpyDeviceToDevice, s));
+  if (h->nnz > 0 && d_colIdx)
+    CUDA_TRY(cudaMemcpyAsync(d_colIdx, h->csr_col, sizeof(int) * (size_t)h->nnz, cudaMemcpyDeviceToDevice, s));
+  if (h->nnz > 0 && d_srcIdx)
+    CUDA_TRY(cudaMemcpyAsync(d_srcIdx, h->csr_src, sizeof(int) * (size_t)h->nnz, cudaMemcpyDeviceToDevice, s));
+  return SPTRSV_OK;
+}
+
+int sptrsv_gb300_set_values(sptrsv_handle_t h, const void* d_val, int dtype, void* stream) {
+  if (!h || (!d_val && h->nnz > 0)) return SPTRSV_ERR_INVALID;
+  if (!h->analysed) return SPTRSV_ERR_STATE;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  ST_TRY(ensure_layout(h, s));
+  return stage_values(h, d_val, dtype, s, true);
+}
+
+int sptrsv_gb300_solve(sptrsv_handle_t h, const void* d_val, int dtype, int rhs, int layout, const void* d_b,
+                       void* d_x, void* stream) {
+  if (!h) return SPTRSV_ERR_INVALID;
+  if (!h->analysed) return SPTRSV_ERR_STATE;
+  if (rhs < 1 || (layout != SPTRSV_LAYOUT_ROW_MAJOR && layout != SPTRSV_LAYOUT_COL_MAJOR)) return SPTRSV_ERR_INVALID;
+  if (dtype != SPTRSV_DTYPE_F64 && dtype != SPTRSV_DTYPE_F32) return SPTRSV_ERR_INVALID;
+  if (h->n == 0) return SPTRSV_OK;
+  if (!d_b || !d_x) return SPTRSV_ERR_INVALID;
+  if ((long long)h->n * rhs > INT_MAX) return SPTRSV_ERR_UNSUPPORTED;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int before = h->layout_block;
+  ST_TRY(ensure_layout(h, s));
+  if (d_val) {
+    ST_TRY(stage_values(h, d_val, dtype, s, h->sync_check != 0));
+  } else if (h->layout_block != before) {
+    return SPTRSV_ERR_STATE;  // schedule changed since the values were staged
+  }
+  if (dtype == SPTRSV_DTYPE_F64) {
+    if (!h->staged64) return SPTRSV_ERR_STATE;
+    return solve_typed<double>(h, h->v64, rhs, layout, static_cast<const double*>(d_b), static_cast<double*>(d_x), s);
+  }
+  if (!h->staged32) return SPTRSV_ERR_STATE;
+  return solve_typed<float>(h, h->v32, rhs, layout, static_cast<const float*>(d_b), static_cast<float*>(d_x), s);
+}
+
+int sptrsv_gb300_check(sptrsv_handle_t h, void* stream) {
+  if (!h) return SPTRSV_ERR_INVALID;
+  return check_device(h, static_cast<cudaStream_t>(stream));
+}
+
+int sptrsv_gb300_exec_ms(sptrsv_handle_t h, double* ms) {
+  if (!h || !ms) return SPTRSV_ERR_INVALID;
+  if (!h->ev_recorded) return SPTRSV_ERR_STATE;
+  CUDA_TRY(cudaEventSynchronize(h->ev_exec[1]));
+  float t = 0.f;
+  CUDA_TRY(cudaEventElapsedTime(&t, h->ev_exec[0], h->ev_exec[1]));
+  *ms = t;
+  return SPTRSV_OK;
+}
+
+// ---------------------------------------------------------------- kernel-level surface
+int sptrsv_gb300_analyser(const int* d_cscRowIdx, int m, int nnz, int* d_graphInDegree, void* stream) {
+  if (m < 0 || nnz < 0 || (m > 0 && !d_graphInDegree) || (nnz > 0 && !d_cscRowIdx)) return SPTRSV_ERR_INVALID;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (m > 0) CUDA_TRY(cudaMemsetAsync(d_graphInDegree, 0, sizeof(int) * (size_t)m, s));
+  CUDA_TRY(launch_in_degree(d_cscRowIdx, m, nnz, d_graphInDegree, s));
+  return SPTRSV_OK;
+}
+
+int sptrsv_gb300_executor(const int* d_cscColPtr, const int* d_cscRowIdx, const double* d_cscVal,
+                          int* d_graphInDegree, double* d_left_sum, int m, int substitution, int rhs, int opt,
+                          const double* d_b, double* d_x, void* stream) {
+  if (m < 0 || rhs < 1 || (substitution != 0 && substitution != 1)) return SPTRSV_ERR_INVALID;
+  if (m > 0 && (!d_cscColPtr || !d_cscRowIdx || !d_cscVal || !d_graphInDegree || !d_left_sum || !d_b || !d_x))
+    return SPTRSV_ERR_INVALID;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  DeviceCtl* ctl = nullptr;
+  ST_TRY(raw_ctl(&ctl));
+  CUDA_TRY(launch_ref_executor<double>(d_cscColPtr, d_cscRowIdx, d_cscVal, d_graphInDegree, d_left_sum, m,
+                                       substitution, rhs, opt, d_b, d_x, ctl, 1000000000ull, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  int code = 0;
+  CUDA_TRY(cudaMemcpy(&code, &ctl->code, sizeof(int), cudaMemcpyDeviceToHost));
+  if (code != DEV_OK) {
+    CUDA_TRY(cudaMemset(ctl, 0, sizeof(DeviceCtl)));
+    return SPTRSV_ERR_TIMEOUT;
+  }
+  return SPTRSV_OK;
+}
+
+// ---------------------------------------------------------------- reference-compatible entry
+int sptrsv_gb300_syncfree_host(const int* cscColPtrTR, const int* cscRowIdxTR, const double* cscValTR, int m, int n,
+                               int nnzTR, int substitution, int rhs, int opt, double* x, const double* b,
+                               const double* x_ref, double* gflops, double* solve_ms, double* analysis_ms,
+                               double* l1_err) {
+  (void)opt;
+  if (m != n) {
+    if (g_verbose) printf("This is not a square matrix, return.\n");
+    return SPTRSV_ERR_NOT_SQUARE;
+  }
+  if (n < 0 || nnzTR < 0 || rhs < 1 || !x || !b || (n > 0 && (!cscColPtrTR || !cscRowIdxTR || !cscValTR)))
+    return SPTRSV_ERR_INVALID;
+  int *d_ptr = nullptr, *d_row = nullptr, *d_indeg = nullptr;
+  double *d_val = nullptr, *d_b = nullptr, *d_x = nullptr;
+  sptrsv_handle_t h = nullptr;
+  int st = SPTRSV_OK;
+  const size_t vec = (size_t)n * (size_t)rhs;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  double t_solve = 0.0, t_an = 0.0;
+  auto fail = [&](int code) { st = code; };
+  do {
+    if (cudaMalloc(&d_ptr, sizeof(int) * ((size_t)n + 1)) != cudaSuccess) { fail(SPTRSV_ERR_OOM); break; }
+    if (cudaMalloc(&d_row, sizeof(int) * (nnzTR ? nnzTR : 1)) != cudaSuccess) { fail(SPTRSV_ERR_OOM); break; }
+    if (cudaMalloc(&d_val, sizeof(double) * (nnzTR ? nnzTR : 1)) != cudaSuccess) { fail(SPTRSV_ERR_OOM); break; }
+    if (cudaMalloc(&d_b, sizeof(double) * (vec ? vec : 1)) != cudaSuccess) { fail(SPTRSV_ERR_OOM); break; }
+    if (cudaMalloc(&d_x, sizeof(double) * (vec ? vec : 1)) != cudaSuccess) { fail(SPTRSV_ERR_OOM); break; }
+    if (cudaMalloc(&d_indeg, sizeof(int) * (n ? n : 1)) != cudaSuccess) { fail(SPTRSV_ERR_OOM); break; }
+    cudaMemcpy(d_ptr, cscColPtrTR, sizeof(int) * ((size_t)n + 1), cudaMemcpyHostToDevice);
+    if (nnzTR) {
+      cudaMemcpy(d_row, cscRowIdxTR, sizeof(int) * nnzTR, cudaMemcpyHostToDevice);
+      cudaMemcpy(d_val, cscValTR, sizeof(double) * nnzTR, cudaMemcpyHostToDevice);
+    }
+    if (vec) cudaMemcpy(d_b, b, sizeof(double) * vec, cudaMemcpyHostToDevice);
+    if (vec) cudaMemset(d_x, 0, sizeof(double) * vec);
+    if (cudaGetLastError() != cudaSuccess) { fail(SPTRSV_ERR_CUDA); break; }
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    // analysis time: the in-degree analyser, averaged like the reference (:456-483)
+    for (int i = 0; i < g_bench_repeat; ++i) {
+      float ms = 0.f;
+      cudaEventRecord(e0, 0);
+      int r = sptrsv_gb300_analyser(d_row, m, nnzTR, d_indeg, nullptr);
+      cudaEventRecord(e1, 0);
+      cudaEventSynchronize(e1);
+      cudaEventElapsedTime(&ms, e0, e1);
+      t_an += ms;
+      if (r != SPTRSV_OK) { fail(r); break; }
+    }
+    if (st != SPTRSV_OK) break;
+    t_an /= g_bench_repeat;
+    if (g_verbose) printf("cuda syncfree SpTRSV analysis on L used %4.2f ms\n", t_an);
+    if ((st = sptrsv_gb300_create(&h)) != SPTRSV_OK) break;
+    if ((st = sptrsv_gb300_analyse(h, m, n, nnzTR, d_ptr, d_row, substitution, nullptr)) != SPTRSV_OK) break;
+    if ((st = sptrsv_gb300_set_values(h, d_val, SPTRSV_DTYPE_F64, nullptr)) != SPTRSV_OK) break;
+    for (int i = 0; i < g_bench_repeat; ++i) {
+      float ms = 0.f;
+      cudaEventRecord(e0, 0);
+      int r = sptrsv_gb300_solve(h, nullptr, SPTRSV_DTYPE_F64, rhs, SPTRSV_LAYOUT_ROW_MAJOR, d_b, d_x, nullptr);
+      cudaEventRecord(e1, 0);
+      cudaEventSynchronize(e1);
+      cudaEventElapsedTime(&ms, e0, e1);
+      t_solve += ms;
+      if (r != SPTRSV_OK) { fail(r); break; }
+    }
+    if (st != SPTRSV_OK) break;
+    t_solve /= g_bench_repeat;
+    const double flop = 2.0 * (double)rhs * (double)nnzTR;
+    const double gf = t_solve > 0 ? flop / (1e6 * t_solve) : 0.0;
+    if (gflops) *gflops = gf;
+    if (g_verbose) printf("cuda syncfree SpTRSV solve used %4.2f ms, throughput is %4.2f gflops\n", t_solve, gf);
+    if (vec && cudaMemcpy(x, d_x, sizeof(double) * vec, cudaMemcpyDeviceToHost) != cudaSuccess) {
+      fail(SPTRSV_ERR_CUDA);
+      break;
+    }
+    double err = NAN;
+    if (x_ref) {
+      double ref = 0.0, res = 0.0;
+      for (size_t i = 0; i < vec; ++i) {
+        ref += std::fabs(x_ref[i]);
+        res += std::fabs(x[i] - x_ref[i]);
+      }
+      err = ref == 0.0 ? res : res / ref;
+      if (g_verbose) {
+        if (err < 1e-4)
+          printf("cuda syncfree SpTRSV executor passed! |x-xref|/|xref| = %8.2e\n", err);
+        else
+          printf("cuda syncfree SpTRSV executor _NOT_ passed! |x-xref|/|xref| = %8.2e\n", err);
+      }
+    }
+    if (l1_err) *l1_err = err;
+  } while (false);
+  if (solve_ms) *solve_ms = t_solve;
+  if (analysis_ms) *analysis_ms = t_an;
+  if (h) sptrsv_gb300_destroy(h);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(d_ptr);
+  cudaFree(d_row);
+  cudaFree(d_val);
+  cudaFree(d_b);
+  cudaFree(d_x);
+  cudaFree(d_indeg);
+  return st;
+}
+
+int sptrsv_syncfree_cuda(const int* cscColPtrTR, const int* cscRowIdxTR, const double* cscValTR, int m, int n,
+                         int nnzTR, int substitution, int rhs, int opt, double* x, const double* b,
+                         const double* x_ref, double* gflops) {
+  return sptrsv_gb300_syncfree_host(cscColPtrTR, cscRowIdxTR, cscValTR, m, n, nnzTR, substitution, rhs, opt, x, b,
+                                    x_ref, gflops, nullptr, nullptr, nullptr);
+}
+
+}  // extern "C"

@@ -1,0 +1,683 @@
+// Sync-free triangular-solve executors.
+//
+// All executors walk "positions": position p is the p-th unknown of the
+// schedule built at analysis time (row perm[p]); every dependency of p sits at
+// a smaller position, so a CTA that owns position p only ever waits on work
+// that was handed out before it (forward progress without co-residency).
+// Work is handed out in chunks of consecutive positions through a ticket
+// counter; inside a chunk, groups of `G` lanes take positions in order.
+//
+//  pull   : p gathers x of its dependencies (CSR row, value-as-flag words,
+//           relaxed loads), then publishes x_p. Deterministic summation;
+//           EXACT reproduces the serial executor's operation order.
+//  push   : the reference's scheme (SpTRSV_cuda/sptrsv_syncfree_cuda.h:21-107,
+//           :290-407): p waits for its in-degree counter, reads its partial
+//           sum, finishes x_p and pushes x_p*L(r,p) into the partial sums of
+//           its dependents with atomics, then bumps their counters.
+//  levelset: one grid barrier per level (cooperative launch).
+//
+// Every wait is bounded (DeviceCtl::code = DEV_TIMEOUT on expiry) and a CTA
+// that sees a failure drains to its barriers and leaves.
+#include <algorithm>
+
+#include "internal.h"
+
+namespace sptrsv {
+
+namespace {
+
+template <typename T>
+struct ExecArgs {
+  int n, rhs, chunk, nchunks, smem_tier;
+  const int* perm;
+  const int* dep_ptr;
+  const int* dep_pos;
+  const T* dep_val;
+  const int* out_ptr;
+  const int* out_pos;
+  const T* out_val;
+  const T* diag;
+  const T* rcp;
+  const T* b;
+  T* x;
+  long long b_si, b_sk, x_si, x_sk;
+  T* xw;             // pull / levelset: position-major value flags [n * rhs]
+  T* left_sum;       // push: position-major partial sums [n * rhs] (zero between solves)
+  unsigned* counters;  // push: arrivals per position (zero between solves)
+  DeviceCtl* ctl;
+  unsigned long long timeout_ns;
+  const int* level_ptr;
+  int nlevels;
+};
+
+template <typename T>
+__device__ __forceinline__ T mul_add(T acc, T v, T xq, bool exact);
+template <>
+__device__ __forceinline__ double mul_add<double>(double acc, double v, double xq, bool exact) {
+  return exact ? __dadd_rn(acc, __dmul_rn(xq, v)) : fma(v, xq, acc);
+}
+template <>
+__device__ __forceinline__ float mul_add<float>(float acc, float v, float xq, bool exact) {
+  return exact ? __fadd_rn(acc, __fmul_rn(xq, v)) : fmaf(v, xq, acc);
+}
+template <typename T>
+__device__ __forceinline__ T finish(T bi, T acc, T d, T r, bool exact);
+template <>
+__device__ __forceinline__ double finish<double>(double bi, double acc, double d, double r, bool exact) {
+  return exact ? __ddiv_rn(__dsub_rn(bi, acc), d) : (bi - acc) * r;
+}
+template <>
+__device__ __forceinline__ float finish<float>(float bi, float acc, float d, float r, bool exact) {
+  return exact ? __fdiv_rn(__fsub_rn(bi, acc), d) : (bi - acc) * r;
+}
+
+__device__ __forceinline__ unsigned group_mask(int G) {
+  if (G >= 32) return 0xffffffffu;
+  const int lane32 = threadIdx.x & 31;
+  return ((1u << G) - 1u) << (lane32 & ~(G - 1));
+}
+
+// Claim the next chunk for this CTA (uniform across the CTA).
+__device__ __forceinline__ unsigned next_chunk(DeviceCtl* ctl, unsigned nchunks, unsigned* s_chunk) {
+  if (threadIdx.x == 0) *s_chunk = ctl_failed(ctl) ? nchunks : atomicAdd(&ctl->ticket, 1u);
+  __syncthreads();
+  const unsigned c = *s_chunk;
+  __syncthreads();
+  return c;
+}
+
+// The last CTA to leave resets the ticket so the next launch starts at 0.
+__device__ __forceinline__ void leave(DeviceCtl* ctl) {
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned d = atomicAdd(&ctl->done, 1u);
+    if (d == gridDim.x - 1) {
+      ctl->ticket = 0;
+      ctl->done = 0;
+      __threadfence();
+    }
+  }
+}
+
+// Wait until the word at p is published; returns EMPTY on timeout/failure.
+template <typename T, bool SHARED>
+__device__ __forceinline__ typename Flag<T>::Bits wait_flag(const T* p, DeviceCtl* ctl, unsigned long long timeout,
+                                                            int where) {
+  using F = Flag<T>;
+  typename F::Bits bits = SHARED ? F::load_shared(p) : F::load(p);
+  if (bits != F::EMPTY) return bits;
+  WaitBudget w(timeout);
+  do {
+    if (!w.poll(ctl, where)) return F::EMPTY;
+    bits = SHARED ? F::load_shared(p) : F::load(p);
+  } while (bits == F::EMPTY);
+  return bits;
+}
+
+// ------------------------------------------------------------------ pull, one rhs
+template <typename T, int G, bool EXACT>
+__global__ void __launch_bounds__(256) k_pull_vec(ExecArgs<T> a) {
+  using F = Flag<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* s_x = reinterpret_cast<T*>(smem_raw);
+  __shared__ unsigned s_chunk;
+  const int NG = blockDim.x / G;
+  const int g = threadIdx.x / G, lane = threadIdx.x % G;
+  const unsigned gmask = group_mask(G);
+  for (;;) {
+    const unsigned c = next_chunk(a.ctl, a.nchunks, &s_chunk);
+    if (c >= (unsigned)a.nchunks) break;
+    const int base = static_cast<int>(c) * a.chunk;
+    const int cend = min(base + a.chunk, a.n);
+    if (a.smem_tier)
+      for (int i = threadIdx.x; i < cend - base; i += blockDim.x)
+        *reinterpret_cast<typename F::Bits*>(&s_x[i]) = F::EMPTY;
+    __syncthreads();
+    bool fail = false;
+    for (int p = base + g; p < cend; p += NG) {
+      const int row = a.perm[p];
+      const int e0 = a.dep_ptr[p], e1 = a.dep_ptr[p + 1];
+      const T bi = a.b[(long long)row * a.b_si];
+      const T dg = EXACT ? a.diag[p] : T(0);
+      const T rc = EXACT ? T(0) : a.rcp[p];
+      T acc = T(0);
+      for (int e = e0 + lane; e < e1; e += G) {
+        const int q = a.dep_pos[e];
+        const T v = a.dep_val[e];
+        typename F::Bits bits;
+        if (a.smem_tier && q >= base)
+          bits = wait_flag<T, true>(&s_x[q - base], a.ctl, a.timeout_ns, p);
+        else
+          bits = wait_flag<T, false>(&a.xw[q], a.ctl, a.timeout_ns, p);
+        if (bits == F::EMPTY) { fail = true; break; }
+        acc = mul_add<T>(acc, v, F::value(bits), EXACT);
+      }
+      if (G > 1) {
+        fail = __any_sync(gmask, fail);
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(gmask, acc, o);
+      }
+      if (fail) break;
+      const T xi = finish<T>(bi, acc, dg, rc, EXACT);
+      if (lane == 0) {
+        if (a.smem_tier) F::store_shared(&s_x[p - base], xi);
+        F::store(&a.xw[p], xi);
+        a.x[(long long)row * a.x_si] = xi;
+      }
+    }
+    if (__syncthreads_or(fail)) break;
+  }
+  leave(a.ctl);
+}
+
+// ------------------------------------------------------------------ pull, many rhs
+// Lanes of a group cover right-hand sides; dependencies are walked in order.
+template <typename T, int G, int RPL, bool EXACT>
+__global__ void __launch_bounds__(256) k_pull_multi(ExecArgs<T> a) {
+  using F = Flag<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* s_x = reinterpret_cast<T*>(smem_raw);
+  __shared__ unsigned s_chunk;
+  const int NG = blockDim.x / G;
+  const int g = threadIdx.x / G, lane = threadIdx.x % G;
+  const unsigned gmask = group_mask(G);
+  const int rhs = a.rhs;
+  for (;;) {
+    const unsigned c = next_chunk(a.ctl, a.nchunks, &s_chunk);
+    if (c >= (unsigned)a.nchunks) break;
+    const int base = static_cast<int>(c) * a.chunk;
+    const int cend = min(base + a.chunk, a.n);
+    if (a.smem_tier)
+      for (long long i = threadIdx.x; i < (long long)(cend - base) * rhs; i += blockDim.x)
+        *reinterpret_cast<typename F::Bits*>(&s_x[i]) = F::EMPTY;
+    __syncthreads();
+    bool fail = false;
+    for (int p = base + g; p < cend && !fail; p += NG) {
+      const int row = a.perm[p];
+      const int e0 = a.dep_ptr[p], e1 = a.dep_ptr[p + 1];
+      const T dg = EXACT ? a.diag[p] : T(0);
+      const T rc = EXACT ? T(0) : a.rcp[p];
+      for (int kt = 0; kt < rhs && !fail; kt += G * RPL) {
+        T acc[RPL];
+#pragma unroll
+        for (int j = 0; j < RPL; ++j) acc[j] = T(0);
+        for (int e = e0; e < e1 && !fail; ++e) {
+          const int q = a.dep_pos[e];
+          const T v = a.dep_val[e];
+          const bool local = a.smem_tier && q >= base;
+#pragma unroll
+          for (int j = 0; j < RPL; ++j) {
+            const int k = kt + lane + j * G;
+            if (k < rhs && !fail) {
+              typename F::Bits bits;
+              if (local)
+                bits = wait_flag<T, true>(&s_x[(long long)(q - base) * rhs + k], a.ctl, a.timeout_ns, p);
+              else
+                bits = wait_flag<T, false>(&a.xw[(long long)q * rhs + k], a.ctl, a.timeout_ns, p);
+              if (bits == F::EMPTY) fail = true;
+              else acc[j] = mul_add<T>(acc[j], v, F::value(bits), EXACT);
+            }
+          }
+        }
+        fail = __any_sync(gmask, fail);
+        if (fail) break;
+#pragma unroll
+        for (int j = 0; j < RPL; ++j) {
+          const int k = kt + lane + j * G;
+          if (k < rhs) {
+            const T bi = a.b[(long long)row * a.b_si + (long long)k * a.b_sk];
+            const T xi = finish<T>(bi, acc[j], dg, rc, EXACT);
+            if (a.smem_tier) F::store_shared(&s_x[(long long)(p - base) * rhs + k], xi);
+            F::store(&a.xw[(long long)p * rhs + k], xi);
+            a.x[(long long)row * a.x_si + (long long)k * a.x_sk] = xi;
+          }
+        }
+      }
+    }
+    if (__syncthreads_or(fail)) break;
+  }
+  leave(a.ctl);
+}
+
+// ------------------------------------------------------------------ push, one rhs
+template <typename T>
+__device__ __forceinline__ void smem_atomic_add(T* p, T v) { atomicAdd(p, v); }
+
+template <typename T, int G>
+__global__ void __launch_bounds__(256) k_push_vec(ExecArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* s_sum = reinterpret_cast<T*>(smem_raw);
+  unsigned* s_cnt = reinterpret_cast<unsigned*>(s_sum + a.chunk);
+  __shared__ unsigned s_chunk;
+  const int NG = blockDim.x / G;
+  const int g = threadIdx.x / G, lane = threadIdx.x % G;
+  const unsigned gmask = group_mask(G);
+  const int lane0 = (threadIdx.x & 31) & ~(G - 1);
+  for (;;) {
+    const unsigned c = next_chunk(a.ctl, a.nchunks, &s_chunk);
+    if (c >= (unsigned)a.nchunks) break;
+    const int base = static_cast<int>(c) * a.chunk;
+    const int cend = min(base + a.chunk, a.n);
+    if (a.smem_tier)
+      for (int i = threadIdx.x; i < cend - base; i += blockDim.x) { s_sum[i] = T(0); s_cnt[i] = 0u; }
+    __syncthreads();
+    bool fail = false;
+    for (int p = base + g; p < cend; p += NG) {
+      const int col = a.perm[p];
+      const unsigned target = static_cast<unsigned>(a.dep_ptr[p + 1] - a.dep_ptr[p]);
+      const T bi = a.b[(long long)col * a.b_si];
+      const T rc = a.rcp[p];
+      T sum = T(0);
+      if (lane == 0) {
+        // Consumer: wait until global + shared arrivals cover the in-degree.
+        WaitBudget w(a.timeout_ns);
+        for (;;) {
+          unsigned got = target == 0u ? 0u : ld_acquire_u32(&a.counters[p]);
+          if (a.smem_tier && target != 0u) got += ld_shared_acquire_u32(&s_cnt[p - base]);
+          if (got == target) break;
+          if (!w.poll(a.ctl, p)) { fail = true; break; }
+        }
+        if (!fail) {
+          if (target != 0u) {
+            sum = Flag<T>::value(Flag<T>::load(&a.left_sum[p]));
+            if (a.smem_tier) sum += *reinterpret_cast<volatile T*>(&s_sum[p - base]);
+            // Self-clean the global slots for the next solve (all producers are done).
+            a.counters[p] = 0u;
+            a.left_sum[p] = T(0);
+          }
+        }
+      }
+      if (G > 1) {
+        fail = __shfl_sync(gmask, fail ? 1 : 0, lane0) != 0;
+        sum = __shfl_sync(gmask, sum, lane0);
+      }
+      if (fail) break;
+      const T xi = (bi - sum) * rc;
+      // Producer: partial sums first, one fence, then the arrival counters.
+      const int o0 = a.out_ptr[p], o1 = a.out_ptr[p + 1];
+      for (int e = o0 + lane; e < o1; e += G) {
+        const int tp = a.out_pos[e];
+        const T contrib = xi * a.out_val[e];
+        if (a.smem_tier && tp < cend) smem_atomic_add(&s_sum[tp - base], contrib);
+        else if (sizeof(T) == 8) red_add_f64(reinterpret_cast<double*>(&a.left_sum[tp]), (double)contrib);
+        else red_add_f32(reinterpret_cast<float*>(&a.left_sum[tp]), (float)contrib);
+      }
+      __threadfence();
+      for (int e = o0 + lane; e < o1; e += G) {
+        const int tp = a.out_pos[e];
+        if (a.smem_tier && tp < cend) atomicAdd(&s_cnt[tp - base], 1u);
+        else red_relaxed_add_u32(&a.counters[tp], 1u);
+      }
+      if (lane == 0) a.x[(long long)col * a.x_si] = xi;
+    }
+    if (__syncthreads_or(fail)) break;
+  }
+  leave(a.ctl);
+}
+
+// ------------------------------------------------------------------ push, many rhs
+template <typename T, int G, int RPL>
+__global__ void __launch_bounds__(256) k_push_multi(ExecArgs<T> a) {
+  __shared__ unsigned s_chunk;
+  const int NG = blockDim.x / G;
+  const int g = threadIdx.x / G, lane = threadIdx.x % G;
+  const unsigned gmask = group_mask(G);
+  const int lane0 = (threadIdx.x & 31) & ~(G - 1);
+  const int rhs = a.rhs;
+  for (;;) {
+    const unsigned c = next_chunk(a.ctl, a.nchunks, &s_chunk);
+    if (c >= (unsigned)a.nchunks) break;
+    const int base = static_cast<int>(c) * a.chunk;
+    const int cend = min(base + a.chunk, a.n);
+    bool fail = false;
+    for (int p = base + g; p < cend; p += NG) {
+      const int col = a.perm[p];
+      const unsigned target = static_cast<unsigned>(a.dep_ptr[p + 1] - a.dep_ptr[p]);
+      if (lane == 0 && target != 0u) {
+        WaitBudget w(a.timeout_ns);
+        while (ld_acquire_u32(&a.counters[p]) != target) {
+          if (!w.poll(a.ctl, p)) { fail = true; break; }
+        }
+      }
+      fail = __shfl_sync(gmask, fail ? 1 : 0, lane0) != 0;
+      if (fail) break;
+      // Make lane 0's acquire cover the whole group before its loads.
+      __syncwarp(gmask);
+      const T rc = a.rcp[p];
+      const int o0 = a.out_ptr[p], o1 = a.out_ptr[p + 1];
+      for (int kt = 0; kt < rhs; kt += G * RPL) {
+        T xi[RPL];
+#pragma unroll
+        for (int j = 0; j < RPL; ++j) {
+          const int k = kt + lane + j * G;
+          xi[j] = T(0);
+          if (k < rhs) {
+            T s = T(0);
+            if (target != 0u) {
+              T* slot = &a.left_sum[(long long)p * rhs + k];
+              s = Flag<T>::value(Flag<T>::load(slot));
+              *slot = T(0);
+            }
+            xi[j] = (a.b[(long long)col * a.b_si + (long long)k * a.b_sk] - s) * rc;
+            a.x[(long long)col * a.x_si + (long long)k * a.x_sk] = xi[j];
+          }
+        }
+        for (int e = o0; e < o1; ++e) {
+          const int tp = a.out_pos[e];
+          const T v = a.out_val[e];
+#pragma unroll
+          for (int j = 0; j < RPL; ++j) {
+            const int k = kt + lane + j * G;
+            if (k < rhs) {
+              T* dst = &a.left_sum[(long long)tp * rhs + k];
+              if (sizeof(T) == 8) red_add_f64(reinterpret_cast<double*>(dst), (double)(xi[j] * v));
+              else red_add_f32(reinterpret_cast<float*>(dst), (float)(xi[j] * v));
+            }
+          }
+        }
+      }
+      if (target != 0u && lane == 0) a.counters[p] = 0u;
+      // All lanes' partial sums, then one fence, then the counters (one lane).
+      __syncwarp(gmask);
+      if (lane == 0) {
+        __threadfence();
+        for (int e = o0; e < o1; ++e) red_relaxed_add_u32(&a.counters[a.out_pos[e]], 1u);
+      }
+    }
+    if (__syncthreads_or(fail)) break;
+  }
+  leave(a.ctl);
+}
+
+// ------------------------------------------------------------------ level sets
+template <typename T, int G>
+__global__ void __launch_bounds__(256) k_levelset(ExecArgs<T> a) {
+  using F = Flag<T>;
+  const int NG = blockDim.x / G;
+  const long long gstride = (long long)gridDim.x * NG;
+  const int g = threadIdx.x / G, lane = threadIdx.x % G;
+  const unsigned gmask = group_mask(G);
+  const int rhs = a.rhs;
+  for (int l = 0; l < a.nlevels; ++l) {
+    const int p0 = a.level_ptr[l], p1 = a.level_ptr[l + 1];
+    for (long long pp = p0 + (long long)blockIdx.x * NG + g; pp < p1; pp += gstride) {
+      const int p = static_cast<int>(pp);
+      const int row = a.perm[p];
+      const int e0 = a.dep_ptr[p], e1 = a.dep_ptr[p + 1];
+      const T rc = a.rcp[p];
+      for (int k = 0; k < rhs; ++k) {
+        T acc = T(0);
+        for (int e = e0 + lane; e < e1; e += G)
+          acc = fma(a.dep_val[e], F::value(F::load(&a.xw[(long long)a.dep_pos[e] * rhs + k])), acc);
+        if (G > 1) {
+#pragma unroll
+          for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(gmask, acc, o);
+        }
+        if (lane == 0) {
+          const T xi = (a.b[(long long)row * a.b_si + (long long)k * a.b_sk] - acc) * rc;
+          F::store(&a.xw[(long long)p * rhs + k], xi);
+          a.x[(long long)row * a.x_si + (long long)k * a.x_sk] = xi;
+        }
+      }
+    }
+    if (!grid_barrier(a.ctl, a.timeout_ns)) return;
+  }
+}
+
+template <typename T>
+ExecArgs<T> make_args(const Layout& L, const Values<T>& V, int rhs, const VecView<T>& v, int chunk) {
+  ExecArgs<T> a{};
+  a.n = L.n;
+  a.rhs = rhs;
+  a.chunk = chunk;
+  a.nchunks = (L.n + chunk - 1) / chunk;
+  a.perm = L.perm;
+  a.dep_ptr = L.dep_ptr;
+  a.dep_pos = L.dep_pos;
+  a.dep_val = V.dep_val;
+  a.out_ptr = L.out_ptr;
+  a.out_pos = L.out_pos;
+  a.out_val = V.out_val;
+  a.diag = V.diag;
+  a.rcp = V.rcp;
+  a.b = v.b;
+  a.x = v.x;
+  a.b_si = v.b_si;
+  a.b_sk = v.b_sk;
+  a.x_si = v.x_si;
+  a.x_sk = v.x_sk;
+  return a;
+}
+
+template <typename K>
+int persistent_grid(K kernel, int block, size_t smem, int num_sms, int nchunks) {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
+  if (per_sm < 1) per_sm = 1;
+  long long grid = (long long)num_sms * per_sm;
+  if (grid > nchunks) grid = nchunks;
+  if (grid < 1) grid = 1;
+  return static_cast<int>(grid);
+}
+
+template <typename K>
+cudaError_t launch_persistent(K kernel, const ExecArgs<int>*, int, size_t, int, cudaStream_t);
+
+template <typename T, typename K>
+cudaError_t run(K kernel, const ExecArgs<T>& a, int block, size_t smem, int num_sms, cudaStream_t s) {
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  const int grid = persistent_grid(kernel, block, smem, num_sms, a.nchunks);
+  kernel<<<grid, block, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t pull_smem_bytes(int chunk, int rhs, size_t elem) { return (size_t)chunk * (size_t)rhs * elem; }
+
+template <typename T>
+cudaError_t launch_pull(const Layout& L, const Values<T>& V, int rhs, const VecView<T>& v, T* xw, DeviceCtl* ctl,
+                        const ExecConfig& cfg, unsigned long long timeout_ns, int num_sms, cudaStream_t s) {
+  if (L.n == 0) return cudaSuccess;
+  ExecArgs<T> a = make_args<T>(L, V, rhs, v, cfg.chunk);
+  a.xw = xw;
+  a.ctl = ctl;
+  a.timeout_ns = timeout_ns;
+  size_t smem = 0;
+  a.smem_tier = 0;
+  if (cfg.smem_tier) {
+    smem = pull_smem_bytes(cfg.chunk, rhs, sizeof(T));
+    if (smem <= 200 * 1024) a.smem_tier = 1;
+    else smem = 0;
+  }
+  const int block = 256;
+  if (rhs == 1) {
+    if (cfg.exact) return run(k_pull_vec<T, 1, true>, a, block, smem, num_sms, s);
+    switch (cfg.lanes) {
+      case 1: return run(k_pull_vec<T, 1, false>, a, block, smem, num_sms, s);
+      case 2: return run(k_pull_vec<T, 2, false>, a, block, smem, num_sms, s);
+      case 4: return run(k_pull_vec<T, 4, false>, a, block, smem, num_sms, s);
+      case 8: return run(k_pull_vec<T, 8, false>, a, block, smem, num_sms, s);
+      case 16: return run(k_pull_vec<T, 16, false>, a, block, smem, num_sms, s);
+      default: return run(k_pull_vec<T, 32, false>, a, block, smem, num_sms, s);
+    }
+  }
+  // many right-hand sides: lanes over rhs
+  if (cfg.exact) {
+    if (rhs <= 8) return run(k_pull_multi<T, 8, 1, true>, a, block, smem, num_sms, s);
+    return run(k_pull_multi<T, 32, 2, true>, a, block, smem, num_sms, s);
+  }
+  if (rhs <= 4) return run(k_pull_multi<T, 4, 1, false>, a, block, smem, num_sms, s);
+  if (rhs <= 8) return run(k_pull_multi<T, 8, 1, false>, a, block, smem, num_sms, s);
+  if (rhs <= 16) return run(k_pull_multi<T, 16, 1, false>, a, block, smem, num_sms, s);
+  if (rhs <= 32) return run(k_pull_multi<T, 32, 1, false>, a, block, smem, num_sms, s);
+  return run(k_pull_multi<T, 32, 2, false>, a, block, smem, num_sms, s);
+}
+
+template <typename T>
+cudaError_t launch_push(const Layout& L, const Values<T>& V, int rhs, const VecView<T>& v, T* left_sum,
+                        unsigned* counters, DeviceCtl* ctl, const ExecConfig& cfg, unsigned long long timeout_ns,
+                        int num_sms, cudaStream_t s) {
+  if (L.n == 0) return cudaSuccess;
+  ExecArgs<T> a = make_args<T>(L, V, rhs, v, cfg.chunk);
+  a.left_sum = left_sum;
+  a.counters = counters;
+  a.ctl = ctl;
+  a.timeout_ns = timeout_ns;
+  const int block = 256;
+  if (rhs == 1) {
+    size_t smem = 0;
+    a.smem_tier = 0;
+    if (cfg.smem_tier) {
+      smem = (size_t)cfg.chunk * (sizeof(T) + sizeof(unsigned));
+      if (smem <= 200 * 1024) a.smem_tier = 1;
+      else smem = 0;
+    }
+    switch (cfg.lanes) {
+      case 1: return run(k_push_vec<T, 1>, a, block, smem, num_sms, s);
+      case 2: return run(k_push_vec<T, 2>, a, block, smem, num_sms, s);
+      case 4: return run(k_push_vec<T, 4>, a, block, smem, num_sms, s);
+      case 8: return run(k_push_vec<T, 8>, a, block, smem, num_sms, s);
+      case 16: return run(k_push_vec<T, 16>, a, block, smem, num_sms, s);
+      default: return run(k_push_vec<T, 32>, a, block, smem, num_sms, s);
+    }
+  }
+  a.smem_tier = 0;
+  if (rhs <= 4) return run(k_push_multi<T, 4, 1>, a, block, 0, num_sms, s);
+  if (rhs <= 8) return run(k_push_multi<T, 8, 1>, a, block, 0, num_sms, s);
+  if (rhs <= 16) return run(k_push_multi<T, 16, 1>, a, block, 0, num_sms, s);
+  if (rhs <= 32) return run(k_push_multi<T, 32, 1>, a, block, 0, num_sms, s);
+  return run(k_push_multi<T, 32, 2>, a, block, 0, num_sms, s);
+}
+
+template <typename T>
+cudaError_t launch_levelset(const Layout& L, const Values<T>& V, int rhs, const VecView<T>& v, T* xw, DeviceCtl* ctl,
+                            const ExecConfig& cfg, unsigned long long timeout_ns, cudaStream_t s) {
+  if (L.n == 0) return cudaSuccess;
+  ExecArgs<T> a = make_args<T>(L, V, rhs, v, cfg.chunk);
+  a.xw = xw;
+  a.ctl = ctl;
+  a.timeout_ns = timeout_ns;
+  a.level_ptr = L.level_ptr;
+  a.nlevels = L.nlevels;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int block = 256;
+  auto kernel = cfg.lanes >= 8 ? k_levelset<T, 8> : k_levelset<T, 1>;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+  if (per_sm < 1) per_sm = 1;
+  const int grid = sms * std::min(per_sm, 4);
+  void* args[] = {(void*)&a};
+  return cudaLaunchCooperativeKernel((void*)kernel, dim3(grid), dim3(block), args, 0, s);
+}
+
+// ------------------------------------------------------------------ reference kernel surface
+// Natural column order, one warp per column, a ticket so warps start in
+// dependency order (SpTRSV_cuda/sptrsv_syncfree_cuda.h:110-172, :290-407).
+// in_degree counts down from the analysed in-degree; a column is ready when
+// its count reaches 1. The caller zeroes left_sum and restores in_degree
+// between solves, as with the reference.
+template <typename T>
+__global__ void __launch_bounds__(128) k_ref_exec(const int* __restrict__ col_ptr, const int* __restrict__ row_idx,
+                                                  const T* __restrict__ val, int* in_degree, T* left_sum, int m,
+                                                  int substitution, int rhs, int opt, const T* __restrict__ b, T* x,
+                                                  DeviceCtl* ctl, unsigned long long timeout_ns) {
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    int id = 0;
+    if (lane == 0) id = ctl_failed(ctl) ? m : static_cast<int>(atomicAdd(&ctl->ticket, 1u));
+    id = __shfl_sync(0xffffffffu, id, 0);
+    if (id >= m) break;
+    const int col = substitution == 0 ? id : m - 1 - id;
+    const int beg = col_ptr[col], end = col_ptr[col + 1];
+    const int dpos = substitution == 0 ? beg : end - 1;
+    const T coef = T(1) / val[dpos];
+    int ok = 1;
+    if (lane == 0) {
+      WaitBudget w(timeout_ns);
+      while (ld_acquire_u32(reinterpret_cast<const unsigned*>(&in_degree[col])) != 1u) {
+        if (!w.poll(ctl, col)) { ok = 0; break; }
+      }
+    }
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    if (!ok) break;
+    __syncwarp();
+    const int s0 = substitution == 0 ? beg + 1 : beg;
+    const int s1 = substitution == 0 ? end : end - 1;
+    const int len = s1 - s0;
+    // Lanes over right-hand sides (RHS mode) or over entries (NNZ mode); AUTO
+    // follows the reference's rule (sptrsv_syncfree_cuda.h:262).
+    const bool rhs_mode = rhs > 1 && (opt == 2 || (opt == 3 && (len <= rhs || rhs > 16) && len < 2048));
+    for (int k = lane; k < rhs; k += 32) {
+      const long long p = (long long)col * rhs + k;
+      x[p] = (b[p] - Flag<T>::value(Flag<T>::load(&left_sum[p]))) * coef;
+    }
+    __syncwarp();
+    if (rhs_mode) {
+      for (int e = s0; e < s1; ++e) {
+        const int r = row_idx[e];
+        const T v = val[e];
+        for (int k = lane; k < rhs; k += 32) atomicAdd(&left_sum[(long long)r * rhs + k], x[(long long)col * rhs + k] * v);
+      }
+      __syncwarp();
+      if (lane == 0) {
+        __threadfence();
+        for (int e = s0; e < s1; ++e) atomicSub(&in_degree[row_idx[e]], 1);
+      }
+    } else {
+      for (int e = s0 + lane; e < s1; e += 32) {
+        const int r = row_idx[e];
+        const T v = val[e];
+        for (int k = 0; k < rhs; ++k) atomicAdd(&left_sum[(long long)r * rhs + k], x[(long long)col * rhs + k] * v);
+      }
+      __threadfence();
+      for (int e = s0 + lane; e < s1; e += 32) atomicSub(&in_degree[row_idx[e]], 1);
+    }
+  }
+  if (lane == 0) {
+    __threadfence();
+    const unsigned total_warps = gridDim.x * (blockDim.x / 32);
+    const unsigned d = atomicAdd(&ctl->done, 1u);
+    if (d == total_warps - 1) {
+      ctl->ticket = 0;
+      ctl->done = 0;
+      __threadfence();
+    }
+  }
+}
+
+template <typename T>
+cudaError_t launch_ref_executor(const int* col_ptr, const int* row_idx, const T* val, int* in_degree, T* left_sum,
+                                int m, int substitution, int rhs, int opt, const T* b, T* x, DeviceCtl* ctl,
+                                unsigned long long timeout_ns, cudaStream_t s) {
+  if (m == 0) return cudaSuccess;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ref_exec<T>, 128, 0);
+  if (per_sm < 1) per_sm = 1;
+  long long grid = (long long)sms * per_sm;
+  const long long need = ((long long)m + 3) / 4;
+  if (grid > need) grid = need;
+  k_ref_exec<T><<<(int)grid, 128, 0, s>>>(col_ptr, row_idx, val, in_degree, left_sum, m, substitution, rhs, opt, b,
+                                          x, ctl, timeout_ns);
+  return cudaGetLastError();
+}
+
+#define SPTRSV_INSTANTIATE(T)                                                                                    \
+  template cudaError_t launch_pull<T>(const Layout&, const Values<T>&, int, const VecView<T>&, T*, DeviceCtl*,   \
+                                      const ExecConfig&, unsigned long long, int, cudaStream_t);                 \
+  template cudaError_t launch_push<T>(const Layout&, const Values<T>&, int, const VecView<T>&, T*, unsigned*,    \
+                                      DeviceCtl*, const ExecConfig&, unsigned long long, int, cudaStream_t);     \
+  template cudaError_t launch_levelset<T>(const Layout&, const Values<T>&, int, const VecView<T>&, T*,           \
+                                          DeviceCtl*, const ExecConfig&, unsigned long long, cudaStream_t);      \
+  template cudaError_t launch_ref_executor<T>(const int*, const int*, const T*, int*, T*, int, int, int, int,    \
+                                              const T*, T*, DeviceCtl*, unsigned long long, cudaStream_t);
+SPTRSV_INSTANTIATE(double)
+SPTRSV_INSTANTIATE(float)
+
+}  // namespace sptrsv

@@ -1,0 +1,129 @@
+// Library-internal declarations shared by the .cu translation units and the
+// C-ABI layer. Nothing here is exported.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <vector>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace sptrsv {
+
+// Structural defects found by the validation kernels (bitmask).
+enum StructFlags : int {
+  SF_BAD_PTR = 1,         // column pointers not monotone or not [0, nnz]
+  SF_ROW_RANGE = 2,       // a row index outside [0, n)
+  SF_UNSORTED = 4,        // rows not strictly ascending inside a column
+  SF_MISSING_DIAG = 8,    // column without its diagonal entry
+  SF_WRONG_TRIANGLE = 16, // entry on the wrong side of the diagonal
+  SF_ZERO_DIAG = 32,      // zero (or non-finite) diagonal value
+};
+
+// Executor families.
+enum Sched : int { SCHED_AUTO = 0, SCHED_PUSH = 1, SCHED_PULL = 2, SCHED_LEVELSET = 3 };
+
+struct ExecConfig {
+  int sched = SCHED_PULL;
+  int lanes = 1;          // lanes per unknown (1, 2, 4, 8, 16, 32)
+  int chunk = 1024;       // positions per CTA work unit
+  int smem_tier = 1;      // resolve in-chunk dependencies through shared memory
+  int exact = 0;          // oracle-order arithmetic (pull only)
+  int block = 256;        // threads per CTA
+};
+
+// Solve-time description of one right-hand-side block. Element (i, k) of b
+// (x) lives at i*si + k*sk.
+template <typename T>
+struct VecView {
+  const T* b;
+  T* x;
+  long long b_si, b_sk, x_si, x_sk;
+};
+
+// Device arrays describing one analysed triangle in "position" space:
+// position p is the p-th unknown in the execution schedule, row perm[p].
+struct Layout {
+  int n = 0;
+  int ndep = 0;
+  int* perm = nullptr;       // [n] position -> row
+  int* iperm = nullptr;      // [n] row -> position
+  // pull layout (dependencies of each position, diagonal excluded; listed in
+  // the order the serial executor accumulates them)
+  int* dep_ptr = nullptr;    // [n+1]
+  int* dep_pos = nullptr;    // [ndep]
+  int* dep_src = nullptr;    // [ndep] CSC entry index (for value staging)
+  int* diag_src = nullptr;   // [n]
+  // push layout (dependents of each position, diagonal excluded)
+  int* out_ptr = nullptr;    // [n+1]
+  int* out_pos = nullptr;    // [ndep]
+  int* out_src = nullptr;    // [ndep]
+  // level sets in position space (valid when the schedule is pure level order)
+  int nlevels = 0;
+  std::vector<int> level_ptr_host;
+  int* level_ptr = nullptr;  // [nlevels+1] (positions)
+};
+
+template <typename T>
+struct Values {
+  T* dep_val = nullptr;  // [ndep]
+  T* out_val = nullptr;  // [ndep]
+  T* diag = nullptr;     // [n]
+  T* rcp = nullptr;      // [n] correctly rounded 1/diag
+};
+
+// ---------------------------------------------------------------- analysis
+cudaError_t launch_validate_ptr(const int* col_ptr, int n, int nnz, int* flags, cudaStream_t s);
+cudaError_t launch_validate_rows(const int* col_ptr, const int* row_idx, int n, int substitution,
+                                 int* flags, cudaStream_t s);
+cudaError_t launch_in_degree(const int* row_idx, int m, int nnz, int* in_degree, cudaStream_t s);
+// exclusive scan of `count` ints; out may alias in; out[count] receives the total when with_total.
+cudaError_t exclusive_scan_int(const int* in, int* out, int count, bool with_total, cudaStream_t s);
+size_t radix_sort_temp_bytes(int count);
+// Stable LSD radix sort of (key, value) pairs on the low `key_bits` bits.
+cudaError_t radix_sort_pairs(const unsigned* keys_in, const int* vals_in, unsigned* keys_out,
+                             int* vals_out, int count, int key_bits, void* temp, cudaStream_t s);
+cudaError_t launch_iota(int* out, int count, int start, int step, cudaStream_t s);
+cudaError_t launch_expand_cols(const int* col_ptr, int n, int* col_of, cudaStream_t s);
+cudaError_t launch_copy_keys(const int* in, unsigned* out, int count, cudaStream_t s);
+cudaError_t launch_gather_int(const int* src, const int* idx, int* out, int count, cudaStream_t s);
+cudaError_t launch_levels(const int* col_ptr, const int* row_idx, const int* in_degree, int n,
+                          int* cnt_scratch, int* front_a, int* front_b, int* depth, int* level_sizes,
+                          DeviceCtl* ctl, unsigned long long timeout_ns, cudaStream_t s);
+cudaError_t launch_schedule_keys(const int* rows, const int* depth, int n, int substitution, int block,
+                                 int mode, unsigned* keys, cudaStream_t s);
+cudaError_t launch_inverse_perm(const int* perm, int n, int* iperm, cudaStream_t s);
+cudaError_t launch_dep_counts(const int* perm, const int* in_degree, int n, int* counts, cudaStream_t s);
+cudaError_t launch_out_counts(const int* perm, const int* col_ptr, int n, int* counts, cudaStream_t s);
+cudaError_t launch_fill_pull(const int* perm, const int* iperm, const int* csr_ptr, const int* csr_col,
+                             const int* csr_src, const int* dep_ptr, int n, int substitution,
+                             int* dep_pos, int* dep_src, int* diag_src, cudaStream_t s);
+cudaError_t launch_fill_push(const int* perm, const int* iperm, const int* col_ptr, const int* row_idx,
+                             const int* out_ptr, int n, int substitution, int* out_pos, int* out_src,
+                             cudaStream_t s);
+template <typename TV, typename T>
+cudaError_t launch_stage_values(const Layout& L, const TV* val, Values<T>& V, int* flags, cudaStream_t s);
+
+// ---------------------------------------------------------------- execution
+template <typename T>
+cudaError_t launch_pull(const Layout& L, const Values<T>& V, int rhs, const VecView<T>& v, T* xw,
+                        DeviceCtl* ctl, const ExecConfig& cfg, unsigned long long timeout_ns,
+                        int num_sms, cudaStream_t s);
+template <typename T>
+cudaError_t launch_push(const Layout& L, const Values<T>& V, int rhs, const VecView<T>& v, T* left_sum,
+                        unsigned* counters, DeviceCtl* ctl, const ExecConfig& cfg,
+                        unsigned long long timeout_ns, int num_sms, cudaStream_t s);
+template <typename T>
+cudaError_t launch_levelset(const Layout& L, const Values<T>& V, int rhs, const VecView<T>& v, T* xw,
+                            DeviceCtl* ctl, const ExecConfig& cfg, unsigned long long timeout_ns,
+                            cudaStream_t s);
+size_t pull_smem_bytes(int chunk, int rhs, size_t elem);
+
+// Kernel-level surface of the reference: in-degree countdown counters owned by
+// the caller, natural column order, one warp per column.
+template <typename T>
+cudaError_t launch_ref_executor(const int* col_ptr, const int* row_idx, const T* val, int* in_degree,
+                                T* left_sum, int m, int substitution, int rhs, int opt, const T* b, T* x,
+                                DeviceCtl* ctl, unsigned long long timeout_ns, cudaStream_t s);
+
+}  // namespace sptrsv

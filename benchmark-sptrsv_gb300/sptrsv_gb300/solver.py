@@ -1,0 +1,235 @@
+"""Host-side mirror of the reference's solver interface over the C ABI.
+
+``sptrsv_syncfree_cuda`` keeps the reference signature and meaning
+(SpTRSV_cuda/sptrsv_syncfree_cuda.h:409-421) on NumPy host arrays;
+``analyser`` / ``executor`` mirror its two kernels (:8-19, :21-107/:290-407)
+on device tensors; ``SyncFreeSolver`` is the analyse-once / solve-many handle.
+PyTorch only supplies device memory and the current stream.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import (DTYPE_F32, DTYPE_F64, LAYOUT_COL_MAJOR, LAYOUT_ROW_MAJOR, SCHED_AUTO, SptrsvError, check,
+                   load)
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _ptr(t) -> ctypes.c_void_p:
+    return ctypes.c_void_p(0 if t is None else int(t.data_ptr()))
+
+
+def _stream_ptr(stream=None) -> ctypes.c_void_p:
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(int(s.cuda_stream))
+
+
+def _np_ptr(a) -> ctypes.c_void_p:
+    return ctypes.c_void_p(0 if a is None else a.ctypes.data)
+
+
+# ------------------------------------------------------------------ reference host surface
+def sptrsv_syncfree_cuda(col_ptr, row_idx, val, m, n, nnz, substitution, rhs, opt, x, b, x_ref=None,
+                         repeat: int | None = None, verbose: bool = False):
+    """Reference-compatible host entry (sptrsv_syncfree_cuda.h:409-421) on NumPy arrays.
+
+    ``x`` (float64, n*rhs, row-major) is written in place. Returns a dict with the
+    status (0, or -1 for a non-square matrix like the reference), GFLOPS of the
+    average solve, solve/analysis milliseconds and the L1-relative error vs x_ref.
+    """
+    lib = load()
+    col_ptr = np.ascontiguousarray(col_ptr, dtype=np.int32)
+    row_idx = np.ascontiguousarray(row_idx, dtype=np.int32)
+    val = np.ascontiguousarray(val, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    if x_ref is not None:
+        x_ref = np.ascontiguousarray(x_ref, dtype=np.float64)
+    if not (x.flags["C_CONTIGUOUS"] and x.dtype == np.float64):
+        raise ValueError("x must be a C-contiguous float64 array")
+    if repeat is not None:
+        lib.sptrsv_gb300_set_bench_repeat(int(repeat))
+    lib.sptrsv_gb300_set_verbose(1 if verbose else 0)
+    gflops = ctypes.c_double(0.0)
+    solve_ms = ctypes.c_double(0.0)
+    an_ms = ctypes.c_double(0.0)
+    err = ctypes.c_double(float("nan"))
+    st = lib.sptrsv_gb300_syncfree_host(_np_ptr(col_ptr), _np_ptr(row_idx), _np_ptr(val), int(m), int(n),
+                                        int(nnz), int(substitution), int(rhs), int(opt), _np_ptr(x), _np_ptr(b),
+                                        _np_ptr(x_ref), ctypes.byref(gflops), ctypes.byref(solve_ms),
+                                        ctypes.byref(an_ms), ctypes.byref(err))
+    if repeat is not None:
+        lib.sptrsv_gb300_set_bench_repeat(100)
+    return {"status": st, "gflops": gflops.value, "solve_ms": solve_ms.value, "analysis_ms": an_ms.value,
+            "l1_err": err.value}
+
+
+# ------------------------------------------------------------------ reference kernel surface
+def analyser(row_idx, m: int, nnz: int, in_degree, stream=None) -> None:
+    """in_degree[r] = stored entries of row r, diagonal included (sptrsv_syncfree_cuda.h:8-19)."""
+    check(load().sptrsv_gb300_analyser(_ptr(row_idx), int(m), int(nnz), _ptr(in_degree), _stream_ptr(stream)),
+          "analyser")
+
+
+def executor(col_ptr, row_idx, val, in_degree, left_sum, m: int, substitution: int, rhs: int, opt: int, b, x,
+             stream=None) -> None:
+    """Warp-per-column push executor on caller-owned counters (sptrsv_syncfree_cuda.h:21-107, :290-407).
+    in_degree is consumed (counts down to 1) and left_sum accumulates, as in the reference."""
+    check(load().sptrsv_gb300_executor(_ptr(col_ptr), _ptr(row_idx), _ptr(val), _ptr(in_degree), _ptr(left_sum),
+                                       int(m), int(substitution), int(rhs), int(opt), _ptr(b), _ptr(x),
+                                       _stream_ptr(stream)), "executor")
+
+
+# ------------------------------------------------------------------ handle API
+class SyncFreeSolver:
+    """Analyse once, solve many: a handle of libsptrsv_gb300 bound to torch CUDA tensors."""
+
+    def __init__(self, col_ptr, row_idx, n: int | None = None, substitution: int = 0, *, values=None,
+                 schedule: int = SCHED_AUTO, lanes: int = 0, chunk: int = 0, order_block: int | None = None,
+                 exact: bool = False, smem_tier: bool = True, timeout_ms: int = 1000, sync_check: bool = True,
+                 profile: bool = False, stream=None):
+        torch = _torch()
+        self._lib = load()
+        self.device = torch.device("cuda", torch.cuda.current_device())
+        self.col_ptr = self._as_dev(col_ptr, torch.int32)
+        self.row_idx = self._as_dev(row_idx, torch.int32)
+        self.n = int(self.col_ptr.numel() - 1) if n is None else int(n)
+        self.nnz = int(self.row_idx.numel())
+        self.substitution = int(substitution)
+        h = ctypes.c_void_p()
+        check(self._lib.sptrsv_gb300_create(ctypes.byref(h)), "create")
+        self._h = h
+        self.set_option(_lib.OPTION_SCHEDULE, schedule)
+        self.set_option(_lib.OPTION_LANES, lanes)
+        self.set_option(_lib.OPTION_CHUNK, chunk)
+        if order_block is not None:
+            self.set_option(_lib.OPTION_ORDER_BLOCK, order_block)
+        self.set_option(_lib.OPTION_EXACT, int(exact))
+        self.set_option(_lib.OPTION_SMEM_TIER, int(smem_tier))
+        self.set_option(_lib.OPTION_TIMEOUT_MS, timeout_ms)
+        self.set_option(_lib.OPTION_SYNC_CHECK, int(sync_check))
+        self.set_option(_lib.OPTION_PROFILE, int(profile))
+        self._stream = stream
+        self.analyse()
+        self.values = None
+        if values is not None:
+            self.set_values(values)
+
+    def _as_dev(self, a, dtype):
+        torch = _torch()
+        if isinstance(a, np.ndarray):
+            a = torch.from_numpy(np.ascontiguousarray(a))
+        return a.to(device=self.device, dtype=dtype).contiguous()
+
+    def set_option(self, option: int, value: int) -> None:
+        check(self._lib.sptrsv_gb300_set_option(self._h, int(option), int(value)), f"set_option({option})")
+
+    def get_option(self, option: int) -> int:
+        v = ctypes.c_longlong(0)
+        check(self._lib.sptrsv_gb300_get_option(self._h, int(option), ctypes.byref(v)), "get_option")
+        return int(v.value)
+
+    def analyse(self) -> None:
+        check(self._lib.sptrsv_gb300_analyse(self._h, self.n, self.n, self.nnz, _ptr(self.col_ptr),
+                                             _ptr(self.row_idx), self.substitution, _stream_ptr(self._stream)),
+              "analyse")
+
+    def set_values(self, values) -> None:
+        torch = _torch()
+        v = values if isinstance(values, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(values))
+        v = v.to(self.device).contiguous()
+        if v.dtype not in (torch.float64, torch.float32):
+            v = v.to(torch.float64)
+        dt = DTYPE_F64 if v.dtype == torch.float64 else DTYPE_F32
+        check(self._lib.sptrsv_gb300_set_values(self._h, _ptr(v), dt, _stream_ptr(self._stream)), "set_values")
+        self.values = v
+
+    def solve(self, b, values=None, *, out=None):
+        """Solve op(L) X = B. ``b``: [n] or [n, rhs] float64/float32 CUDA tensor; a column-major
+        [n, rhs] view (stride (1, n)) is solved in place of layout without a copy. Returns x with
+        b's layout and dtype."""
+        torch = _torch()
+        if b.dim() == 1:
+            b2 = b.reshape(-1, 1)
+        else:
+            b2 = b
+        if b2.shape[0] != self.n:
+            raise ValueError(f"b has {b2.shape[0]} rows, the matrix has {self.n}")
+        rhs = int(b2.shape[1])
+        if b2.is_contiguous():
+            layout = LAYOUT_ROW_MAJOR
+        elif b2.t().is_contiguous():
+            layout = LAYOUT_COL_MAJOR
+        else:
+            b2 = b2.contiguous()
+            layout = LAYOUT_ROW_MAJOR
+        if b2.dtype == torch.float64:
+            dt = DTYPE_F64
+        elif b2.dtype == torch.float32:
+            dt = DTYPE_F32
+        else:
+            raise TypeError("b must be float64 or float32")
+        if out is None:
+            if layout == LAYOUT_ROW_MAJOR:
+                out = torch.empty_like(b2, memory_format=torch.contiguous_format)
+            else:
+                out = torch.empty((rhs, self.n), dtype=b2.dtype, device=b2.device).t()
+        vptr = ctypes.c_void_p(0)
+        if values is not None:
+            v = values.to(self.device).contiguous()
+            self.values = v
+            vptr = _ptr(v)
+        st = self._lib.sptrsv_gb300_solve(self._h, vptr, dt, rhs, layout, _ptr(b2), _ptr(out),
+                                          _stream_ptr(self._stream))
+        check(st, "solve")
+        return out.reshape(b.shape) if b.dim() == 1 else out
+
+    def exec_ms(self) -> float:
+        """Device time of the last executor launch (needs profile=True)."""
+        ms = ctypes.c_double(0.0)
+        check(self._lib.sptrsv_gb300_exec_ms(self._h, ctypes.byref(ms)), "exec_ms")
+        return float(ms.value)
+
+    def check(self) -> None:
+        check(self._lib.sptrsv_gb300_check(self._h, _stream_ptr(self._stream)), "check")
+
+    def info(self) -> dict:
+        inf = _lib.Info()
+        check(self._lib.sptrsv_gb300_get_info(self._h, ctypes.byref(inf)), "get_info")
+        return {f: getattr(inf, f) for f, _ in _lib.Info._fields_}
+
+    def levels(self):
+        """(level_ptr [nlevels+1], level_item [n]) as int32 CUDA tensors (findlevel.h:6-69)."""
+        torch = _torch()
+        nl = self.info()["nlevels"]
+        lp = torch.empty(nl + 1, dtype=torch.int32, device=self.device)
+        li = torch.empty(max(self.n, 1), dtype=torch.int32, device=self.device)
+        check(self._lib.sptrsv_gb300_levels(self._h, _ptr(lp), _ptr(li), _stream_ptr(self._stream)), "levels")
+        return lp, li[: self.n]
+
+    def csr(self):
+        """(row_ptr, col_idx, src) of the analysed triangle (tranpose.h:6-43)."""
+        torch = _torch()
+        rp = torch.empty(self.n + 1, dtype=torch.int32, device=self.device)
+        ci = torch.empty(max(self.nnz, 1), dtype=torch.int32, device=self.device)
+        src = torch.empty(max(self.nnz, 1), dtype=torch.int32, device=self.device)
+        check(self._lib.sptrsv_gb300_csr(self._h, _ptr(rp), _ptr(ci), _ptr(src), _stream_ptr(self._stream)), "csr")
+        return rp, ci[: self.nnz], src[: self.nnz]
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.sptrsv_gb300_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

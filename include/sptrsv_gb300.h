@@ -1,0 +1,206 @@
+/*
+ * sptrsv_gb300 — sync-free sparse triangular solve for GB300 (sm_103a).
+ *
+ * C ABI of the library (libsptrsv_gb300.so). Plain pointers and sizes only.
+ * Matrices use the reference's storage: square CSC, 0-based int32 column
+ * pointers [n+1] and row indices [nnz], rows strictly ascending inside each
+ * column, the diagonal first in every column of a lower triangle (forward
+ * substitution) and last in every column of an upper triangle (backward
+ * substitution). Right-hand sides and solutions are n x rhs blocks, row-major
+ * by default (x[i*rhs+k], as the reference stores them) or column-major.
+ *
+ * Conventions
+ *  - Every function returns an sptrsv_status (0 on success); none prints,
+ *    aborts or exits.
+ *  - Handle functions take DEVICE pointers and a CUDA stream (cudaStream_t
+ *    passed as void*, NULL = legacy default stream). Work is stream-ordered.
+ *  - A handle is not thread-safe; separate handles are independent.
+ *  - Device waits are bounded. A wait that runs out makes the affected call
+ *    report SPTRSV_ERR_TIMEOUT instead of hanging (default limit 1000 ms per
+ *    wait, see SPTRSV_OPTION_TIMEOUT_MS).
+ *
+ * Reference interfaces this header replaces (harunsasmaz/Benchmark-SpTRSV,
+ * directory SpTRSV_cuda/) are cited next to each entry point.
+ */
+#ifndef SPTRSV_GB300_H
+#define SPTRSV_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPTRSV_GB300_VERSION 100
+
+/* Substitution and multi-RHS lane modes: same values as common.h:25-30. */
+#define SPTRSV_SUBSTITUTION_FORWARD 0
+#define SPTRSV_SUBSTITUTION_BACKWARD 1
+#define SPTRSV_OPT_WARP_NNZ 1
+#define SPTRSV_OPT_WARP_RHS 2
+#define SPTRSV_OPT_WARP_AUTO 3
+
+typedef enum sptrsv_status {
+  SPTRSV_OK = 0,
+  SPTRSV_ERR_NOT_SQUARE = -1,     /* m != n; same value the reference returns (sptrsv_syncfree_cuda.h:423-427) */
+  SPTRSV_ERR_BAD_STRUCTURE = -2,  /* unsorted rows, missing/zero diagonal, wrong triangle, bad pointers */
+  SPTRSV_ERR_INVALID = -3,        /* bad argument (NULL pointer, negative size, unknown enum) */
+  SPTRSV_ERR_CUDA = -4,           /* a CUDA runtime call failed */
+  SPTRSV_ERR_TIMEOUT = -5,        /* a bounded device wait ran out */
+  SPTRSV_ERR_OOM = -6,            /* device allocation failed */
+  SPTRSV_ERR_STATE = -7,          /* call out of order (e.g. solve before analyse) */
+  SPTRSV_ERR_NOT_CONVERGED = -8,  /* iterative refinement missed its tolerance */
+  SPTRSV_ERR_UNSUPPORTED = -9     /* valid request this build does not serve */
+} sptrsv_status;
+
+typedef enum sptrsv_layout {
+  SPTRSV_LAYOUT_ROW_MAJOR = 0,    /* x[i*rhs + k] (reference layout, main.cu:332) */
+  SPTRSV_LAYOUT_COL_MAJOR = 1     /* x[k*n + i] */
+} sptrsv_layout;
+
+typedef enum sptrsv_dtype {
+  SPTRSV_DTYPE_F64 = 0,
+  SPTRSV_DTYPE_F32 = 1
+} sptrsv_dtype;
+
+typedef enum sptrsv_schedule {
+  SPTRSV_SCHED_AUTO = 0,      /* autotuned choice (pull unless tuned otherwise) */
+  SPTRSV_SCHED_PUSH = 1,      /* in-degree counters + atomic partial sums (the reference scheme) */
+  SPTRSV_SCHED_PULL = 2,      /* dependency gather with value-as-flag words (deterministic) */
+  SPTRSV_SCHED_LEVELSET = 3   /* level sets with one grid barrier per level */
+} sptrsv_schedule;
+
+/* Tunable options (sptrsv_gb300_set_option / get_option). */
+typedef enum sptrsv_option {
+  SPTRSV_OPTION_SCHEDULE = 0,     /* sptrsv_schedule */
+  SPTRSV_OPTION_LANES = 1,        /* lanes per unknown: 1, 2, 4, 8, 16, 32 */
+  SPTRSV_OPTION_CHUNK = 2,        /* unknowns per CTA work unit (>= 1) */
+  SPTRSV_OPTION_SMEM_TIER = 3,    /* 1: in-chunk dependencies through shared memory */
+  SPTRSV_OPTION_EXACT = 4,        /* 1: pull executor in the serial executor's operation order */
+  SPTRSV_OPTION_ORDER_BLOCK = 5,  /* schedule: level order inside blocks of this many unknowns
+                                     (1 = natural order, >= n = global level order); re-layout on change */
+  SPTRSV_OPTION_TIMEOUT_MS = 6,   /* bound of every device wait, milliseconds */
+  SPTRSV_OPTION_SYNC_CHECK = 7,   /* 1 (default): solve calls synchronise and report device errors;
+                                     0: fully asynchronous, errors surface in sptrsv_gb300_check */
+  SPTRSV_OPTION_PROFILE = 8       /* 1: record CUDA events around each executor launch
+                                     (read with sptrsv_gb300_exec_ms) */
+} sptrsv_option;
+
+typedef struct sptrsv_info {
+  int n;
+  int nnz;
+  int substitution;
+  int nlevels;          /* level sets (findlevel.h:6-69) */
+  int parallelism_min;  /* findlevel_csc statistics (findlevel.h:123-136) */
+  int parallelism_avg;
+  int parallelism_max;
+  int max_in_degree;
+  int schedule;         /* executor used by the last solve */
+  int lanes;
+  int chunk;
+  int order_block;
+  double analysis_ms;   /* device time of the last analyse */
+  size_t device_bytes;  /* device memory held by the handle */
+} sptrsv_info;
+
+typedef struct sptrsv_gb300_handle_s *sptrsv_handle_t;
+
+const char *sptrsv_gb300_status_string(int status);
+int sptrsv_gb300_version(void);
+
+/* ---------------------------------------------------------------------------
+ * Reference-compatible host entry point.
+ * Replaces int sptrsv_syncfree_cuda(...) of sptrsv_syncfree_cuda.h:409-421
+ * (VALUE_TYPE = double): host arrays in, x out (row-major n x rhs); runs the
+ * analysis and the solve `repeat` times (default 100, the reference's
+ * BENCH_REPEAT, see sptrsv_gb300_set_bench_repeat), writes the GFLOPS of the
+ * average solve (2*rhs*nnz / t, :546-550) into *gflops, and validates x
+ * against x_ref with the L1-relative test of :554-570 (x_ref may be NULL to
+ * skip it). Returns 0, -1 when m != n, or another sptrsv_status. Prints the
+ * reference's report lines only after sptrsv_gb300_set_verbose(1).
+ * ------------------------------------------------------------------------- */
+int sptrsv_syncfree_cuda(const int *cscColPtrTR, const int *cscRowIdxTR, const double *cscValTR, int m, int n,
+                         int nnzTR, int substitution, int rhs, int opt, double *x, const double *b,
+                         const double *x_ref, double *gflops);
+void sptrsv_gb300_set_verbose(int verbose);
+void sptrsv_gb300_set_bench_repeat(int repeat);
+/* Same call with explicit outputs: average solve and analysis times (ms) and
+ * the L1-relative error against x_ref (NaN when x_ref is NULL). */
+int sptrsv_gb300_syncfree_host(const int *cscColPtrTR, const int *cscRowIdxTR, const double *cscValTR, int m, int n,
+                               int nnzTR, int substitution, int rhs, int opt, double *x, const double *b,
+                               const double *x_ref, double *gflops, double *solve_ms, double *analysis_ms,
+                               double *l1_err);
+
+/* ---------------------------------------------------------------------------
+ * Kernel-level surface (device pointers, stream-ordered).
+ * sptrsv_gb300_analyser   replaces the kernel sptrsv_syncfree_cuda_analyser
+ *                         (sptrsv_syncfree_cuda.h:8-19): d_graphInDegree[r] =
+ *                         number of stored entries in row r, diagonal included
+ *                         (the array is zeroed first).
+ * sptrsv_gb300_executor   replaces sptrsv_syncfree_cuda_executor (:21-107) and
+ *                         sptrsm_syncfree_cuda_executor_update (:290-407): one
+ *                         warp per column in natural order, started in ticket
+ *                         order; consumes d_graphInDegree as countdown counters
+ *                         (a column is ready at 1) and accumulates into
+ *                         d_left_sum (n*rhs, zero on entry). Like the reference,
+ *                         the caller restores d_graphInDegree and zeroes
+ *                         d_left_sum before the next call. Synchronises and
+ *                         reports SPTRSV_ERR_TIMEOUT if a wait ran out.
+ * ------------------------------------------------------------------------- */
+int sptrsv_gb300_analyser(const int *d_cscRowIdx, int m, int nnz, int *d_graphInDegree, void *stream);
+int sptrsv_gb300_executor(const int *d_cscColPtr, const int *d_cscRowIdx, const double *d_cscVal,
+                          int *d_graphInDegree, double *d_left_sum, int m, int substitution, int rhs, int opt,
+                          const double *d_b, double *d_x, void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Handle API: analyse once, solve many.
+ * ------------------------------------------------------------------------- */
+int sptrsv_gb300_create(sptrsv_handle_t *handle);
+int sptrsv_gb300_destroy(sptrsv_handle_t handle);
+int sptrsv_gb300_set_option(sptrsv_handle_t handle, int option, long long value);
+int sptrsv_gb300_get_option(sptrsv_handle_t handle, int option, long long *value);
+
+/* Validates the CSC structure, runs the in-degree analyser, builds the CSR
+ * transpose (tranpose.h:6-43), the level sets (findlevel.h:6-69) and the
+ * execution schedule. d_colPtr/d_rowIdx are read during this call only.
+ * Synchronises `stream`. Returns SPTRSV_ERR_NOT_SQUARE when m != n and
+ * SPTRSV_ERR_BAD_STRUCTURE for malformed input. */
+int sptrsv_gb300_analyse(sptrsv_handle_t handle, int m, int n, int nnz, const int *d_colPtr, const int *d_rowIdx,
+                         int substitution, void *stream);
+int sptrsv_gb300_get_info(sptrsv_handle_t handle, sptrsv_info *info);
+
+/* Copies level sets out (device pointers; level_ptr[nlevels+1] with the
+ * row counts of findlevel, level_item[n] the rows of each level in ascending
+ * natural order). */
+int sptrsv_gb300_levels(sptrsv_handle_t handle, int *d_levelPtr, int *d_levelItem, void *stream);
+/* CSR of the analysed triangle (tranpose.h:6-43 applied to the CSC input):
+ * d_rowPtr[n+1], d_colIdx[nnz]; d_srcIdx[nnz] (optional) gets the CSC entry of
+ * each CSR entry. */
+int sptrsv_gb300_csr(sptrsv_handle_t handle, int *d_rowPtr, int *d_colIdx, int *d_srcIdx, void *stream);
+
+/* Stages matrix values (CSC order, dtype F64 or F32) for later solves that
+ * pass d_val = NULL. Returns SPTRSV_ERR_BAD_STRUCTURE on a zero diagonal. */
+int sptrsv_gb300_set_values(sptrsv_handle_t handle, const void *d_val, int dtype, void *stream);
+
+/* Solves op(L) X = B for rhs right-hand sides with the analysed pattern.
+ * dtype selects the arithmetic: F64 (values, b, x double) or F32 (values, b,
+ * x float; F64 values are accepted and rounded). d_val = NULL uses the staged
+ * values. b and x must not overlap. */
+int sptrsv_gb300_solve(sptrsv_handle_t handle, const void *d_val, int dtype, int rhs, int layout, const void *d_b,
+                       void *d_x, void *stream);
+
+/* Synchronises `stream` and reports (then clears) a device error raised by
+ * asynchronous solves since the last check. */
+int sptrsv_gb300_check(sptrsv_handle_t handle, void *stream);
+
+/* Device time (ms) of the executor kernel of the last solve, measured with
+ * CUDA events on the solve's stream when SPTRSV_OPTION_PROFILE is 1 (waits
+ * for that kernel to finish). Workspace preparation is excluded. */
+int sptrsv_gb300_exec_ms(sptrsv_handle_t handle, double *ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPTRSV_GB300_H */

@@ -1,0 +1,59 @@
+"""The C-ABI library builds for sm_103a, loads, and exports every entry point
+declared in include/sptrsv_gb300.h (host-only checks, no GPU work)."""
+from __future__ import annotations
+
+import ctypes
+import re
+
+from conftest import ROOT
+
+
+def _declared_functions():
+    text = (ROOT / "include" / "sptrsv_gb300.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = set(re.findall(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(sptrsv_\w+)\s*\(", text, flags=re.M))
+    return names
+
+
+def test_header_declares_reference_entry_points():
+    names = _declared_functions()
+    for required in ("sptrsv_syncfree_cuda", "sptrsv_gb300_analyser", "sptrsv_gb300_executor",
+                     "sptrsv_gb300_create", "sptrsv_gb300_analyse", "sptrsv_gb300_solve", "sptrsv_gb300_destroy"):
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    names = _declared_functions()
+    assert len(names) >= 15
+    for name in sorted(names):
+        assert hasattr(built_lib, name), f"{name} declared but not exported"
+
+
+def test_binding_covers_header():
+    from sptrsv_gb300 import _lib
+    assert _declared_functions() == set(_lib.SIGNATURES)
+
+
+def test_status_strings_and_version(built_lib):
+    from sptrsv_gb300 import _lib
+    assert built_lib.sptrsv_gb300_version() == 100
+    for code in range(-9, 1):
+        s = _lib.status_string(code)
+        assert s and s != "unknown status"
+    assert _lib.status_string(-42) == "unknown status"
+
+
+def test_invalid_arguments_rejected_on_host(built_lib):
+    from sptrsv_gb300 import _lib
+    assert built_lib.sptrsv_gb300_create(None) == _lib.ERR_INVALID
+    assert built_lib.sptrsv_gb300_destroy(None) == _lib.ERR_INVALID
+    assert built_lib.sptrsv_gb300_set_option(None, 0, 0) == _lib.ERR_INVALID
+    # m != n is reported before any device work, with the reference's -1
+    rc = built_lib.sptrsv_gb300_syncfree_host(None, None, None, 3, 4, 0, 0, 1, 3, None, None, None, None, None,
+                                              None, None)
+    assert rc == _lib.ERR_NOT_SQUARE == -1
+
+
+def test_build_targets_sm103a_only():
+    import build as pkg_build
+    assert pkg_build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]

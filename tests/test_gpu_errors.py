@@ -1,0 +1,93 @@
+"""Error paths on the GPU: malformed structure is rejected on the host side of
+the analysis, and a wait that can never finish returns SPTRSV_ERR_TIMEOUT
+(bounded waits; nothing faults or hangs) and leaves the context usable."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _solver(cuda, cp, ri, n, sub=0, **kw):
+    from sptrsv_gb300 import SyncFreeSolver
+    return SyncFreeSolver(np.asarray(cp, np.int32), np.asarray(ri, np.int32), n, sub, **kw)
+
+
+def _status(fn):
+    from sptrsv_gb300 import SptrsvError
+    try:
+        fn()
+    except SptrsvError as e:
+        return e.status
+    return 0
+
+
+@pytest.mark.parametrize("cp,ri,sub", [
+    ([0, 1, 2, 3], [0, 2, 2], 0),           # column 1 misses its diagonal
+    ([0, 2, 3, 4], [1, 0, 1, 2], 0),        # unsorted rows in column 0
+    ([0, 1, 3, 4], [0, 0, 1, 2], 0),        # entry above the diagonal in a lower solve
+    ([0, 2, 3, 4], [0, 1, 1, 2], 1),        # entry below the diagonal in an upper solve
+    ([0, 1, 1, 3], [0, 1, 2], 0),           # empty column
+    ([0, 2, 1, 3], [0, 1, 2], 0),           # decreasing column pointers
+    ([0, 1, 2, 5], [0, 1, 2], 0),           # colPtr[n] != nnz
+    ([0, 1, 2, 3], [0, 1, 7], 0),           # row out of range
+])
+def test_bad_structure_rejected(cuda, cp, ri, sub):
+    from sptrsv_gb300 import _lib
+    n = len(cp) - 1
+    st = _status(lambda: _solver(cuda, cp, ri, n, sub))
+    assert st == _lib.ERR_BAD_STRUCTURE
+
+
+def test_zero_diagonal_rejected(cuda):
+    from sptrsv_gb300 import _lib
+    st = _status(lambda: _solver(cuda, [0, 2, 3], [0, 1, 1], 2, values=np.array([0.0, 1.0, 2.0])))
+    assert st == _lib.ERR_BAD_STRUCTURE
+
+
+def test_not_square(cuda, built_lib):
+    import ctypes
+    from sptrsv_gb300 import _lib
+    h = ctypes.c_void_p()
+    assert built_lib.sptrsv_gb300_create(ctypes.byref(h)) == 0
+    assert built_lib.sptrsv_gb300_analyse(h, 3, 4, 4, None, None, 0, None) == _lib.ERR_NOT_SQUARE
+    assert built_lib.sptrsv_gb300_solve(h, None, 0, 1, 0, None, None, None) == _lib.ERR_STATE
+    assert built_lib.sptrsv_gb300_destroy(h) == 0
+
+
+def test_undercounted_in_degree_times_out_then_recovers(cuda):
+    """Kernel-level executor fed an in-degree one higher than the truth: the
+    affected column can never become ready; the bounded wait reports a timeout."""
+    from sptrsv_gb300 import _lib, analyser, executor, matgen, SptrsvError
+    m = matgen.poisson_band(2000, 4.0, 100, seed=1)
+    cp = cuda.from_numpy(m.col_ptr).cuda()
+    ri = cuda.from_numpy(m.row_idx).cuda()
+    va = cuda.from_numpy(m.val).cuda()
+    b = cuda.ones(m.n, dtype=cuda.float64, device="cuda")
+    deg = cuda.empty(m.n, dtype=cuda.int32, device="cuda")
+    analyser(ri, m.n, m.nnz, deg)
+    bad = deg.clone()
+    bad[m.n // 2] += 1
+    left = cuda.zeros(m.n, dtype=cuda.float64, device="cuda")
+    x = cuda.zeros(m.n, dtype=cuda.float64, device="cuda")
+    with pytest.raises(SptrsvError) as ei:
+        executor(cp, ri, va, bad, left, m.n, 0, 1, 3, b, x)
+    assert ei.value.status == _lib.ERR_TIMEOUT
+    # the context is still usable and a correct call succeeds
+    good = deg.clone()
+    left.zero_()
+    executor(cp, ri, va, good, left, m.n, 0, 1, 3, b, x)
+    ref = m.to_scipy()
+    r = ref @ x.cpu().numpy() - 1.0
+    assert np.max(np.abs(r)) < 1e-12
+
+
+def test_handle_timeout_option(cuda):
+    """Timeouts are configurable per handle and validated."""
+    from sptrsv_gb300 import _lib, matgen, SyncFreeSolver, SptrsvError
+    m = matgen.poisson_band(500, 3.0, 50, seed=2)
+    s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, 0, values=m.val, timeout_ms=250)
+    assert s.get_option(_lib.OPTION_TIMEOUT_MS) == 250
+    with pytest.raises(SptrsvError):
+        s.set_option(_lib.OPTION_TIMEOUT_MS, 0)

@@ -1,0 +1,190 @@
+"""CUDA path vs the oracle, through the C ABI (ctypes binding).
+
+Tolerances: the FP64 push executor accumulates with atomics in arbitrary
+order, so it is checked to 1e-12 relative in the max norm against the FP64
+oracle; the pull executor in exact mode repeats the serial executor's
+operation order and must be bit-identical; FP32 solves are checked to 1e-5
+relative against the FP64 oracle (and bit-identical to the FP32 oracle in
+exact mode)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOL32 = 1e-5
+
+
+def relerr(x, ref):
+    x = np.asarray(x, dtype=np.float64).ravel()
+    ref = np.asarray(ref, dtype=np.float64).ravel()
+    return float(np.max(np.abs(x - ref)) / max(np.max(np.abs(ref)), 1e-300))
+
+
+def make_solver(cuda, g, **kw):
+    from sptrsv_gb300 import SyncFreeSolver
+    sub = 0 if int(g["lower"]) else 1
+    return SyncFreeSolver(g["col_ptr"], g["row_idx"], int(g["n"]), sub, values=g["val"], **kw)
+
+
+def b_tensor(cuda, g, dtype=np.float64):
+    n, rhs = int(g["n"]), int(g["rhs"])
+    return cuda.from_numpy(g["b"].reshape(n, rhs).astype(dtype)).cuda()
+
+
+CONFIGS = [
+    dict(schedule=1, lanes=1),
+    dict(schedule=1, lanes=4),
+    dict(schedule=1, lanes=32, order_block=1),
+    dict(schedule=1, lanes=8, smem_tier=False, order_block=10**9),
+    dict(schedule=2, lanes=1),
+    dict(schedule=2, lanes=2, order_block=1),
+    dict(schedule=2, lanes=8, order_block=10**9, chunk=64),
+    dict(schedule=2, lanes=32, smem_tier=False),
+    dict(schedule=3, lanes=1),
+    dict(schedule=3, lanes=8),
+]
+
+
+@pytest.mark.parametrize("name", golden_names())
+@pytest.mark.parametrize("cfg", CONFIGS, ids=lambda c: "-".join(f"{k}{v}" for k, v in c.items()))
+def test_fp64_matches_oracle(cuda, name, cfg):
+    g = load_golden(name)
+    s = make_solver(cuda, g, **cfg)
+    x = s.solve(b_tensor(cuda, g)).cpu().numpy()
+    assert relerr(x, g["x64"]) <= TOL64
+    # a second solve on the same handle (self-cleaning workspace) gives the same answer
+    x2 = s.solve(b_tensor(cuda, g)).cpu().numpy()
+    assert relerr(x2, g["x64"]) <= TOL64
+
+
+@pytest.mark.parametrize("name", golden_names())
+@pytest.mark.parametrize("order_block", [1, 256, 10**9])
+def test_exact_pull_is_bit_identical(cuda, name, order_block):
+    g = load_golden(name)
+    s = make_solver(cuda, g, schedule=2, exact=True, order_block=order_block)
+    x = s.solve(b_tensor(cuda, g)).cpu().numpy().ravel()
+    assert np.array_equal(x.view(np.uint64), g["x64"].view(np.uint64))
+    x32 = s.solve(b_tensor(cuda, g, np.float32)).cpu().numpy().ravel()
+    assert np.array_equal(x32.view(np.uint32), g["x32"].view(np.uint32))
+
+
+@pytest.mark.parametrize("name", golden_names())
+@pytest.mark.parametrize("schedule", [1, 2, 3])
+def test_fp32_close_to_fp64_oracle(cuda, name, schedule):
+    g = load_golden(name)
+    s = make_solver(cuda, g, schedule=schedule)
+    x = s.solve(b_tensor(cuda, g, np.float32)).cpu().numpy()
+    assert relerr(x, g["x64"]) <= TOL32
+
+
+@pytest.mark.parametrize("schedule", [1, 2, 3])
+def test_column_major_rhs(cuda, schedule):
+    g = load_golden("uneven3000_bwd")
+    n, rhs = int(g["n"]), int(g["rhs"])
+    s = make_solver(cuda, g, schedule=schedule)
+    b_rm = g["b"].reshape(n, rhs)
+    b_cm = cuda.from_numpy(np.ascontiguousarray(b_rm.T)).cuda().t()   # [n, rhs] with stride (1, n)
+    assert not b_cm.is_contiguous()
+    x = s.solve(b_cm)
+    assert x.stride() == (1, n)
+    assert relerr(x.cpu().numpy(), g["x64"].reshape(n, rhs)) <= TOL64
+
+
+@pytest.mark.parametrize("rhs", [1, 5, 16, 33, 64, 70])
+@pytest.mark.parametrize("schedule", [1, 2, 3])
+def test_many_rhs_against_oracle(cuda, oracle_port, rhs, schedule):
+    from sptrsv_gb300 import matgen
+    m = matgen.poisson_band(3000, 6.0, 300, seed=rhs, lower=(rhs % 2 == 0))
+    b = np.random.default_rng(rhs).standard_normal((m.n, rhs))
+    ref = oracle_port.solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, b)
+    from sptrsv_gb300 import SyncFreeSolver
+    s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, values=m.val, schedule=schedule)
+    x = s.solve(cuda.from_numpy(b).cuda()).cpu().numpy()
+    assert relerr(x, ref) <= TOL64
+    s.set_option(4, 1)  # exact
+    if schedule == 2:
+        xe = s.solve(cuda.from_numpy(b).cuda()).cpu().numpy()
+        assert np.array_equal(xe.view(np.uint64), ref.view(np.uint64))
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_analysis_products_match_reference(cuda, name):
+    g = load_golden(name)
+    s = make_solver(cuda, g)
+    info = s.info()
+    assert info["nlevels"] == int(g["nlevel"])
+    nl, pmin, pavg, pmax = (int(v) for v in g["level_stats"])
+    assert (info["parallelism_min"], info["parallelism_avg"], info["parallelism_max"]) == (pmin, pavg, pmax)
+    lp, li = s.levels()
+    lp, li = lp.cpu().numpy(), li.cpu().numpy()
+    np.testing.assert_array_equal(lp, g["level_ptr"])
+    for lv in range(nl):   # same rows per level (the reference lists them in discovery order)
+        a, b = lp[lv], lp[lv + 1]
+        np.testing.assert_array_equal(np.sort(li[a:b]), np.sort(g["level_item"][a:b]))
+    rp, ci, src = (t.cpu().numpy() for t in s.csr())
+    np.testing.assert_array_equal(rp, g["csr_ptr"])
+    np.testing.assert_array_equal(ci, g["csr_idx"])
+    np.testing.assert_array_equal(g["val"][src], g["csr_val"])
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_kernel_level_surface(cuda, name):
+    from sptrsv_gb300 import analyser, executor
+    g = load_golden(name)
+    n, rhs = int(g["n"]), int(g["rhs"])
+    sub = 0 if int(g["lower"]) else 1
+    cp = cuda.from_numpy(g["col_ptr"]).cuda()
+    ri = cuda.from_numpy(g["row_idx"]).cuda()
+    va = cuda.from_numpy(g["val"]).cuda()
+    deg = cuda.empty(n, dtype=cuda.int32, device="cuda")
+    analyser(ri, n, ri.numel(), deg)
+    np.testing.assert_array_equal(deg.cpu().numpy(), g["in_degree"])
+    for opt in (1, 2, 3):
+        d2 = deg.clone()
+        left = cuda.zeros(n * rhs, dtype=cuda.float64, device="cuda")
+        x = cuda.zeros(n * rhs, dtype=cuda.float64, device="cuda")
+        executor(cp, ri, va, d2, left, n, sub, rhs, opt, cuda.from_numpy(g["b"]).cuda(), x)
+        assert relerr(x.cpu().numpy(), g["x64"]) <= TOL64
+
+
+@pytest.mark.parametrize("name", ["hand4_fwd", "unitrand_band1500_fwd", "unitrand_band1500_bwd", "random500_rhs3_bwd"])
+def test_reference_compatible_host_entry(cuda, name):
+    from sptrsv_gb300 import sptrsv_syncfree_cuda
+    g = load_golden(name)
+    n, rhs = int(g["n"]), int(g["rhs"])
+    sub = 0 if int(g["lower"]) else 1
+    x = np.zeros(n * rhs)
+    r = sptrsv_syncfree_cuda(g["col_ptr"], g["row_idx"], g["val"], n, n, g["row_idx"].size, sub, rhs, 3, x, g["b"],
+                             g["x_true"], repeat=3)
+    assert r["status"] == 0
+    assert r["l1_err"] < 1e-4           # the reference's own acceptance test
+    assert relerr(x, g["x64"]) <= TOL64
+    assert r["gflops"] > 0
+    r = sptrsv_syncfree_cuda(g["col_ptr"], g["row_idx"], g["val"], n, n + 1, g["row_idx"].size, sub, rhs, 3, x,
+                             g["b"], None, repeat=1)
+    assert r["status"] == -1
+
+
+def test_full_size_properties_laplace(cuda, oracle_port):
+    """The 2M-row Laplacian at full size: every schedule agrees with the oracle."""
+    from sptrsv_gb300 import SyncFreeSolver, matgen
+    for lower in (True, False):
+        m = matgen.system_laplace_2m(lower=lower)
+        x_true = np.ones(m.n)
+        b = m.matvec(x_true)
+        ref = oracle_port.solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, b)
+        for sched in (1, 2):
+            s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, values=m.val, schedule=sched)
+            x = s.solve(cuda.from_numpy(b).cuda()).cpu().numpy()
+            assert relerr(x, ref) <= TOL64
+            assert relerr(x, x_true) <= 1e-10
+            s.close()
+        s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, values=m.val, schedule=2, exact=True)
+        x = s.solve(cuda.from_numpy(b).cuda()).cpu().numpy()
+        assert np.array_equal(x.view(np.uint64), ref.view(np.uint64))
+        assert s.info()["nlevels"] == 2 * 1414 - 1
