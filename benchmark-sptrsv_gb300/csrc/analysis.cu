@@ -384,9 +384,13 @@ __global__ void k_levels(const int* __restrict__ col_ptr, const int* __restrict_
       level_sizes[level] = size;
       tails[free_tail] = 0;
     }
-    for (long long q = tid; q < size; q += stride) {
+    // one warp per frontier node, lanes over the node's column entries
+    const long long warp = tid >> 5;
+    const long long nwarps = stride >> 5;
+    const int lane = static_cast<int>(tid & 31);
+    for (long long q = warp; q < size; q += nwarps) {
       const int node = cur[q];
-      for (int e = col_ptr[node]; e < col_ptr[node + 1]; ++e) {
+      for (int e = col_ptr[node] + lane; e < col_ptr[node + 1]; e += 32) {
         const int r = row_idx[e];
         if (r == node) continue;
         const int old = atomicSub(&cnt[r], 1);
@@ -487,7 +491,7 @@ cudaError_t launch_out_counts(const int* perm, const int* col_ptr, int n, int* c
 __global__ void k_fill_pull(const int* __restrict__ perm, const int* __restrict__ iperm,
                             const int* __restrict__ csr_ptr, const int* __restrict__ csr_col,
                             const int* __restrict__ csr_src, const int* __restrict__ dep_ptr, int n,
-                            int substitution, int* dep_pos, int* dep_src, int* diag_src) {
+                            int substitution, int* dep_pos, int* dep_src, int* dep_col, int* diag_src) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += stride) {
     const int r = perm[p];
@@ -497,12 +501,14 @@ __global__ void k_fill_pull(const int* __restrict__ perm, const int* __restrict_
       for (int k = beg; k < end - 1; ++k, ++out) {
         dep_pos[out] = iperm[csr_col[k]];
         dep_src[out] = csr_src[k];
+        dep_col[out] = csr_col[k];
       }
       diag_src[p] = csr_src[end - 1];
     } else {
       for (int k = end - 1; k > beg; --k, ++out) {
         dep_pos[out] = iperm[csr_col[k]];
         dep_src[out] = csr_src[k];
+        dep_col[out] = csr_col[k];
       }
       diag_src[p] = csr_src[beg];
     }
@@ -510,25 +516,34 @@ __global__ void k_fill_pull(const int* __restrict__ perm, const int* __restrict_
 }
 cudaError_t launch_fill_pull(const int* perm, const int* iperm, const int* csr_ptr, const int* csr_col,
                              const int* csr_src, const int* dep_ptr, int n, int substitution, int* dep_pos,
-                             int* dep_src, int* diag_src, cudaStream_t s) {
+                             int* dep_src, int* dep_col, int* diag_src, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   k_fill_pull<<<grid_for(n), kThreads, 0, s>>>(perm, iperm, csr_ptr, csr_col, csr_src, dep_ptr, n, substitution,
-                                                dep_pos, dep_src, diag_src);
+                                                dep_pos, dep_src, dep_col, diag_src);
   return cudaGetLastError();
 }
 
+// Dependents of position p (its column's off-diagonal entries), listed in the
+// order the serial executor run on the transpose accumulates them: descending
+// row for a lower triangle (its transpose is solved backward), ascending for an
+// upper one. The push executor is order-agnostic; the adjoint solve relies on it.
 __global__ void k_fill_push(const int* __restrict__ perm, const int* __restrict__ iperm,
                             const int* __restrict__ col_ptr, const int* __restrict__ row_idx,
                             const int* __restrict__ out_ptr, int n, int substitution, int* out_pos, int* out_src) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += stride) {
     const int c = perm[p];
-    const int beg = col_ptr[c] + (substitution == 0 ? 1 : 0);
-    const int end = col_ptr[c + 1] - (substitution == 0 ? 0 : 1);
     int out = out_ptr[p];
-    for (int e = beg; e < end; ++e, ++out) {
-      out_pos[out] = iperm[row_idx[e]];
-      out_src[out] = e;
+    if (substitution == 0) {
+      for (int e = col_ptr[c + 1] - 1; e > col_ptr[c]; --e, ++out) {
+        out_pos[out] = iperm[row_idx[e]];
+        out_src[out] = e;
+      }
+    } else {
+      for (int e = col_ptr[c]; e < col_ptr[c + 1] - 1; ++e, ++out) {
+        out_pos[out] = iperm[row_idx[e]];
+        out_src[out] = e;
+      }
     }
   }
 }
@@ -560,6 +575,18 @@ __global__ void k_stage_diag(const TV* __restrict__ val, const int* __restrict__
   }
 }
 
+// w = v * (1/diag of the dependent row): x_p = b_p/d_p - sum_j w_j x_j needs one
+// fused multiply-add per dependency once the reciprocal is folded in.
+template <typename T>
+__global__ void k_stage_scaled(const int* __restrict__ dep_ptr, const T* __restrict__ dep_val,
+                               const T* __restrict__ rcp, T* dep_w, int n) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += stride) {
+    const T r = rcp[p];
+    for (int e = dep_ptr[p]; e < dep_ptr[p + 1]; ++e) dep_w[e] = dep_val[e] * r;
+  }
+}
+
 template <typename TV, typename T>
 cudaError_t launch_stage_values(const Layout& L, const TV* val, Values<T>& V, int* flags, cudaStream_t s) {
   if (L.ndep > 0) {
@@ -567,6 +594,10 @@ cudaError_t launch_stage_values(const Layout& L, const TV* val, Values<T>& V, in
     k_stage_edges<TV, T><<<grid_for(L.ndep), kThreads, 0, s>>>(val, L.out_src, V.out_val, L.ndep);
   }
   if (L.n > 0) k_stage_diag<TV, T><<<grid_for(L.n), kThreads, 0, s>>>(val, L.diag_src, V.diag, V.rcp, L.n, flags);
+  if (L.n > 0 && L.ndep > 0) {
+    k_stage_scaled<T><<<grid_for(L.n), kThreads, 0, s>>>(L.dep_ptr, V.dep_val, V.rcp, V.dep_w, L.n);
+    k_stage_scaled<T><<<grid_for(L.n), kThreads, 0, s>>>(L.out_ptr, V.out_val, V.rcp, V.out_w, L.n);
+  }
   return cudaGetLastError();
 }
 

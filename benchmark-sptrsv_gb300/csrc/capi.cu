@@ -37,6 +37,9 @@ struct sptrsv_gb300_handle_s {
   int sched_option = SCHED_AUTO;
   int lanes_option = 0;    // 0: automatic
   int chunk_option = 0;    // 0: automatic
+  int block_option = 0;    // 0: automatic
+  long long backoff_ns = 256;
+  int ctas_per_sm = 0;
   // analysis
   bool analysed = false;
   int n = 0, nnz = 0, substitution = 0;
@@ -45,6 +48,7 @@ struct sptrsv_gb300_handle_s {
   std::vector<int> level_sizes_host;
   int* csc_ptr = nullptr;   // owned copy of the structure
   int* csc_row = nullptr;
+  int* csc_col = nullptr;   // column of every CSC entry
   int* in_degree = nullptr;
   int* depth = nullptr;
   int* csr_ptr = nullptr;
@@ -120,6 +124,7 @@ void free_layout(Layout& L) {
   dev_free(&L.dep_ptr);
   dev_free(&L.dep_pos);
   dev_free(&L.dep_src);
+  dev_free(&L.dep_col);
   dev_free(&L.diag_src);
   dev_free(&L.out_ptr);
   dev_free(&L.out_pos);
@@ -131,6 +136,8 @@ void free_layout(Layout& L) {
 template <typename T>
 void free_values(Values<T>& V) {
   dev_free(&V.dep_val);
+  dev_free(&V.dep_w);
+  dev_free(&V.out_w);
   dev_free(&V.out_val);
   dev_free(&V.diag);
   dev_free(&V.rcp);
@@ -139,6 +146,7 @@ void free_values(Values<T>& V) {
 void free_analysis(sptrsv_gb300_handle_s* h) {
   dev_free(&h->csc_ptr);
   dev_free(&h->csc_row);
+  dev_free(&h->csc_col);
   dev_free(&h->in_degree);
   dev_free(&h->depth);
   dev_free(&h->csr_ptr);
@@ -229,6 +237,7 @@ int build_layout(sptrsv_gb300_handle_s* h, int block, cudaStream_t s) {
   ST_TRY(dev_alloc(h, &L.out_ptr, (size_t)n + 1));
   ST_TRY(dev_alloc(h, &L.dep_pos, ndep));
   ST_TRY(dev_alloc(h, &L.dep_src, ndep));
+  ST_TRY(dev_alloc(h, &L.dep_col, ndep));
   ST_TRY(dev_alloc(h, &L.out_pos, ndep));
   ST_TRY(dev_alloc(h, &L.out_src, ndep));
   ST_TRY(dev_alloc(h, &L.diag_src, n));
@@ -268,7 +277,7 @@ int build_layout(sptrsv_gb300_handle_s* h, int block, cudaStream_t s) {
     CUDA_TRY(launch_out_counts(L.perm, h->csc_ptr, n, L.out_ptr, s));
     CUDA_TRY(exclusive_scan_int(L.out_ptr, L.out_ptr, n, true, s));
     CUDA_TRY(launch_fill_pull(L.perm, L.iperm, h->csr_ptr, h->csr_col, h->csr_src, L.dep_ptr, n, h->substitution,
-                              L.dep_pos, L.dep_src, L.diag_src, s));
+                              L.dep_pos, L.dep_src, L.dep_col, L.diag_src, s));
     CUDA_TRY(launch_fill_push(L.perm, L.iperm, h->csc_ptr, h->csc_row, L.out_ptr, n, h->substitution, L.out_pos,
                               L.out_src, s));
   }
@@ -304,6 +313,8 @@ int stage(sptrsv_gb300_handle_s* h, Values<T>& V, const TV* val, cudaStream_t s,
   const Layout& L = h->layout;
   if (!V.dep_val) {
     ST_TRY(dev_alloc(h, &V.dep_val, L.ndep));
+    ST_TRY(dev_alloc(h, &V.dep_w, L.ndep));
+    ST_TRY(dev_alloc(h, &V.out_w, L.ndep));
     ST_TRY(dev_alloc(h, &V.out_val, L.ndep));
     ST_TRY(dev_alloc(h, &V.diag, L.n));
     ST_TRY(dev_alloc(h, &V.rcp, L.n));
@@ -339,12 +350,15 @@ ExecConfig pick_config(const sptrsv_gb300_handle_s* h, int rhs) {
   c.sched = h->sched_option == SCHED_AUTO ? SCHED_PULL : h->sched_option;
   c.lanes = h->lanes_option > 0 ? h->lanes_option : 1;
   c.chunk = h->chunk_option > 0 ? h->chunk_option : (rhs == 1 ? 1024 : 256);
+  c.block = h->block_option > 0 ? h->block_option : 256;
+  c.sleep_max = static_cast<unsigned>(h->backoff_ns);
+  c.ctas_per_sm = h->ctas_per_sm;
   return c;
 }
 
 template <typename T>
 int solve_typed(sptrsv_gb300_handle_s* h, const Values<T>& V, int rhs, int layout, const T* b, T* x,
-                cudaStream_t s) {
+                cudaStream_t s, const AdjointArgs<T>* adj = nullptr) {
   const int n = h->n;
   VecView<T> v{};
   v.b = b;
@@ -357,6 +371,7 @@ int solve_typed(sptrsv_gb300_handle_s* h, const Values<T>& V, int rhs, int layou
     v.b_sk = v.x_sk = n;
   }
   ExecConfig c = pick_config(h, rhs);
+  if (adj) c.sched = SCHED_PULL;  // the transposed solve walks the analysis in reverse with the pull executor
   h->last_sched = c.sched;
   const size_t elems = (size_t)n * (size_t)rhs;
   if (c.sched == SCHED_PUSH) {
@@ -380,7 +395,7 @@ int solve_typed(sptrsv_gb300_handle_s* h, const Values<T>& V, int rhs, int layou
     CUDA_TRY(launch_levelset<T>(h->layout, V, rhs, v, static_cast<T*>(h->xw.p), h->ctl, c, timeout_ns(h), s));
   } else {
     CUDA_TRY(launch_pull<T>(h->layout, V, rhs, v, static_cast<T*>(h->xw.p), h->ctl, c, timeout_ns(h), h->num_sms,
-                            s));
+                            s, adj));
   }
   if (h->profile) {
     CUDA_TRY(cudaEventRecord(h->ev_exec[1], s));
@@ -506,6 +521,18 @@ int sptrsv_gb300_set_option(sptrsv_handle_t h, int option, long long value) {
     case SPTRSV_OPTION_PROFILE:
       h->profile = value != 0;
       return SPTRSV_OK;
+    case SPTRSV_OPTION_BLOCK:
+      if (!(value == 0 || value == 64 || value == 128 || value == 256)) return SPTRSV_ERR_INVALID;
+      h->block_option = static_cast<int>(value);
+      return SPTRSV_OK;
+    case SPTRSV_OPTION_BACKOFF_NS:
+      if (value < 0 || value > 100000) return SPTRSV_ERR_INVALID;
+      h->backoff_ns = value;
+      return SPTRSV_OK;
+    case SPTRSV_OPTION_CTAS_PER_SM:
+      if (value < 0 || value > 32) return SPTRSV_ERR_INVALID;
+      h->ctas_per_sm = static_cast<int>(value);
+      return SPTRSV_OK;
     default:
       return SPTRSV_ERR_INVALID;
   }
@@ -523,6 +550,9 @@ int sptrsv_gb300_get_option(sptrsv_handle_t h, int option, long long* value) {
     case SPTRSV_OPTION_TIMEOUT_MS: *value = h->timeout_ms; break;
     case SPTRSV_OPTION_SYNC_CHECK: *value = h->sync_check; break;
     case SPTRSV_OPTION_PROFILE: *value = h->profile; break;
+    case SPTRSV_OPTION_BLOCK: *value = h->block_option; break;
+    case SPTRSV_OPTION_BACKOFF_NS: *value = h->backoff_ns; break;
+    case SPTRSV_OPTION_CTAS_PER_SM: *value = h->ctas_per_sm; break;
     default: return SPTRSV_ERR_INVALID;
   }
   return SPTRSV_OK;
@@ -583,6 +613,8 @@ int sptrsv_gb300_analyse(sptrsv_handle_t h, int m, int n, int nnz, const int* d_
     CUDA_TRY(radix_sort_pairs(keys, iota, keys_sorted, h->csr_src, nnz, bits_for(n - 1), temp, s));
     CUDA_TRY(launch_expand_cols(h->csc_ptr, n, col_of, s));
     CUDA_TRY(launch_gather_int(col_of, h->csr_src, h->csr_col, nnz, s));
+    ST_TRY(dev_alloc(h, &h->csc_col, nnz));
+    CUDA_TRY(cudaMemcpyAsync(h->csc_col, col_of, sizeof(int) * (size_t)nnz, cudaMemcpyDeviceToDevice, s));
     CUDA_TRY(cudaFreeAsync(keys, s));
     CUDA_TRY(cudaFreeAsync(keys_sorted, s));
     CUDA_TRY(cudaFreeAsync(iota, s));
@@ -753,6 +785,67 @@ int sptrsv_gb300_solve(sptrsv_handle_t h, const void* d_val, int dtype, int rhs,
   }
   if (!h->staged32) return SPTRSV_ERR_STATE;
   return solve_typed<float>(h, h->v32, rhs, layout, static_cast<const float*>(d_b), static_cast<float*>(d_x), s);
+}
+
+int sptrsv_gb300_solve_adjoint(sptrsv_handle_t h, const void* d_val, int dtype, int rhs, int layout, const void* d_g,
+                               void* d_lambda, const void* d_x, void* d_dval, void* stream) {
+  if (!h) return SPTRSV_ERR_INVALID;
+  if (!h->analysed) return SPTRSV_ERR_STATE;
+  if (rhs < 1 || (layout != SPTRSV_LAYOUT_ROW_MAJOR && layout != SPTRSV_LAYOUT_COL_MAJOR)) return SPTRSV_ERR_INVALID;
+  if (dtype != SPTRSV_DTYPE_F64 && dtype != SPTRSV_DTYPE_F32) return SPTRSV_ERR_INVALID;
+  if (h->n == 0) return SPTRSV_OK;
+  if (!d_g || !d_lambda || (d_dval && !d_x)) return SPTRSV_ERR_INVALID;
+  if (h->sched_option == SCHED_LEVELSET) return SPTRSV_ERR_UNSUPPORTED;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int before = h->layout_block;
+  ST_TRY(ensure_layout(h, s));
+  if (d_val) {
+    ST_TRY(stage_values(h, d_val, dtype, s, h->sync_check != 0));
+  } else if (h->layout_block != before) {
+    return SPTRSV_ERR_STATE;
+  }
+  const long long si = layout == SPTRSV_LAYOUT_ROW_MAJOR ? rhs : 1;
+  const long long sk = layout == SPTRSV_LAYOUT_ROW_MAJOR ? 1 : h->n;
+  if (dtype == SPTRSV_DTYPE_F64) {
+    if (!h->staged64) return SPTRSV_ERR_STATE;
+    AdjointArgs<double> adj;
+    adj.grad = static_cast<double*>(d_dval);
+    adj.xf = static_cast<const double*>(d_x);
+    adj.xf_si = si;
+    adj.xf_sk = sk;
+    return solve_typed<double>(h, h->v64, rhs, layout, static_cast<const double*>(d_g), static_cast<double*>(d_lambda),
+                               s, &adj);
+  }
+  if (!h->staged32) return SPTRSV_ERR_STATE;
+  AdjointArgs<float> adj;
+  adj.grad = static_cast<float*>(d_dval);
+  adj.xf = static_cast<const float*>(d_x);
+  adj.xf_si = si;
+  adj.xf_sk = sk;
+  return solve_typed<float>(h, h->v32, rhs, layout, static_cast<const float*>(d_g), static_cast<float*>(d_lambda), s,
+                            &adj);
+}
+
+int sptrsv_gb300_grad_values(sptrsv_handle_t h, int dtype, int rhs, int layout, const void* d_lambda, const void* d_x,
+                             void* d_dval, void* stream) {
+  if (!h) return SPTRSV_ERR_INVALID;
+  if (!h->analysed) return SPTRSV_ERR_STATE;
+  if (rhs < 1 || (layout != SPTRSV_LAYOUT_ROW_MAJOR && layout != SPTRSV_LAYOUT_COL_MAJOR)) return SPTRSV_ERR_INVALID;
+  if (h->nnz == 0) return SPTRSV_OK;
+  if (!d_lambda || !d_x || !d_dval) return SPTRSV_ERR_INVALID;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const long long si = layout == SPTRSV_LAYOUT_ROW_MAJOR ? rhs : 1;
+  const long long sk = layout == SPTRSV_LAYOUT_ROW_MAJOR ? 1 : h->n;
+  if (dtype == SPTRSV_DTYPE_F64)
+    CUDA_TRY(launch_grad_values<double>(h->csc_row, h->csc_col, h->nnz, rhs, static_cast<const double*>(d_lambda),
+                                        static_cast<const double*>(d_x), si, sk, static_cast<double*>(d_dval), s));
+  else if (dtype == SPTRSV_DTYPE_F32)
+    CUDA_TRY(launch_grad_values<float>(h->csc_row, h->csc_col, h->nnz, rhs, static_cast<const float*>(d_lambda),
+                                       static_cast<const float*>(d_x), si, sk, static_cast<float*>(d_dval), s));
+  else
+    return SPTRSV_ERR_INVALID;
+  if (h->sync_check) return check_device(h, s);
+  return SPTRSV_OK;
 }
 
 int sptrsv_gb300_check(sptrsv_handle_t h, void* stream) {

@@ -118,18 +118,27 @@ template <> struct Flag<float> {
   }
 };
 
-// Bounded-wait bookkeeping. `poll` is called once per failed poll; every 64
-// failed polls it reads the global timer and the shared status word. It
-// returns false once the wait must be abandoned (timeout here, or an error
-// raised elsewhere), after recording DEV_TIMEOUT the first time.
+// Bounded-wait bookkeeping. `poll` is called once per failed poll. It backs
+// off with __nanosleep (doubling from sleep_min up to sleep_max nanoseconds;
+// 0 = spin) so that thousands of waiting threads do not flood L2 with polls,
+// and every 16 failed polls it reads the global timer and the shared status
+// word. It returns false once the wait must be abandoned (timeout here, or an
+// error raised elsewhere), after recording DEV_TIMEOUT the first time.
 struct WaitBudget {
   unsigned long long start;
   unsigned long long limit_ns;
   unsigned iters;
-  __device__ __forceinline__ explicit WaitBudget(unsigned long long limit) : start(0), limit_ns(limit), iters(0) {}
+  unsigned sleep_ns;
+  unsigned sleep_max;
+  __device__ __forceinline__ explicit WaitBudget(unsigned long long limit, unsigned smin = 0, unsigned smax = 0)
+      : start(0), limit_ns(limit), iters(0), sleep_ns(smin), sleep_max(smax) {}
   __device__ __forceinline__ bool poll(DeviceCtl* ctl, int where) {
     ++iters;
-    if ((iters & 63u) != 0u) return true;
+    if (sleep_max) {
+      __nanosleep(sleep_ns);
+      sleep_ns = sleep_ns * 2u < sleep_max ? sleep_ns * 2u : sleep_max;
+    }
+    if ((iters & 15u) != 0u) return true;
     const unsigned long long now = globaltimer_ns();
     if (start == 0) { start = now; return true; }
     if (*reinterpret_cast<volatile int*>(&ctl->code) != DEV_OK) return false;
@@ -161,7 +170,7 @@ __device__ __forceinline__ bool grid_barrier(DeviceCtl* ctl, unsigned long long 
       __threadfence();
       red_release_add_u32(&ctl->barrier_gen, 1u);
     } else {
-      WaitBudget w(limit_ns);
+      WaitBudget w(limit_ns, 32, 256);
       while (ld_acquire_u32(&ctl->barrier_gen) == gen) {
         if (!w.poll(ctl, -1)) { ok = 0; break; }
       }

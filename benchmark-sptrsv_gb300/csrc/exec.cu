@@ -28,14 +28,22 @@ namespace {
 
 template <typename T>
 struct ExecArgs {
-  int n, rhs, chunk, nchunks, smem_tier;
+  int n, rhs, chunk, nchunks, smem_tier, ctas_per_sm;
   const int* perm;
   const int* dep_ptr;
   const int* dep_pos;
   const T* dep_val;
+  const T* dep_w;
+  const int* dep_src;
+  const int* dep_col;
+  const int* diag_src;
   const int* out_ptr;
   const int* out_pos;
   const T* out_val;
+  const T* out_w;
+  T* grad;           // adjoint: gradient w.r.t. the stored values (CSC order), or null
+  const T* xf;       // adjoint: forward solution x (row-indexed)
+  long long xf_si, xf_sk;
   const T* diag;
   const T* rcp;
   const T* b;
@@ -46,6 +54,7 @@ struct ExecArgs {
   unsigned* counters;  // push: arrivals per position (zero between solves)
   DeviceCtl* ctl;
   unsigned long long timeout_ns;
+  unsigned sleep_min, sleep_max;  // backoff of global polls (ns)
   const int* level_ptr;
   int nlevels;
 };
@@ -100,13 +109,15 @@ __device__ __forceinline__ void leave(DeviceCtl* ctl) {
 }
 
 // Wait until the word at p is published; returns EMPTY on timeout/failure.
+// Global words back off between polls (sleep_min..sleep_max ns); shared-memory
+// words are polled without sleeping.
 template <typename T, bool SHARED>
 __device__ __forceinline__ typename Flag<T>::Bits wait_flag(const T* p, DeviceCtl* ctl, unsigned long long timeout,
-                                                            int where) {
+                                                            int where, unsigned sleep_min, unsigned sleep_max) {
   using F = Flag<T>;
   typename F::Bits bits = SHARED ? F::load_shared(p) : F::load(p);
   if (bits != F::EMPTY) return bits;
-  WaitBudget w(timeout);
+  WaitBudget w(timeout, SHARED ? 0u : sleep_min, SHARED ? 0u : sleep_max);
   do {
     if (!w.poll(ctl, where)) return F::EMPTY;
     bits = SHARED ? F::load_shared(p) : F::load(p);
@@ -115,15 +126,32 @@ __device__ __forceinline__ typename Flag<T>::Bits wait_flag(const T* p, DeviceCt
 }
 
 // ------------------------------------------------------------------ pull, one rhs
-template <typename T, int G, bool EXACT>
+// x_p = b_p/d_p - sum_j w_j x_j with w = L(p,j)/d_p staged in advance, so each
+// dependency costs one fused multiply-add once its value is published
+// (EXACT keeps the serial executor's product, sum and true division instead).
+// Each lane issues the index, value and flag loads of U dependencies together
+// before consuming them in order.
+//
+// ADJ runs the transposed (adjoint) solve on the same analysis: positions are
+// walked in reverse, and the dependencies of p are its dependents in the
+// forward solve (the push lists, stored in the order the serial executor
+// applied to L^T accumulates them). With a.grad set it also writes the
+// gradient of every stored entry of row p, dL(p,j) = -lambda_p * x_j, as soon
+// as lambda_p is known (fused adjoint + gradient).
+template <typename T, int G, bool EXACT, int U, bool ADJ>
 __global__ void __launch_bounds__(256) k_pull_vec(ExecArgs<T> a) {
   using F = Flag<T>;
+  using Bits = typename F::Bits;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* s_x = reinterpret_cast<T*>(smem_raw);
   __shared__ unsigned s_chunk;
   const int NG = blockDim.x / G;
   const int g = threadIdx.x / G, lane = threadIdx.x % G;
   const unsigned gmask = group_mask(G);
+  const int* __restrict__ lptr = ADJ ? a.out_ptr : a.dep_ptr;
+  const int* __restrict__ lpos = ADJ ? a.out_pos : a.dep_pos;
+  const T* __restrict__ vals = ADJ ? (EXACT ? a.out_val : a.out_w) : (EXACT ? a.dep_val : a.dep_w);
+  const int last = a.n - 1;
   for (;;) {
     const unsigned c = next_chunk(a.ctl, a.nchunks, &s_chunk);
     if (c >= (unsigned)a.nchunks) break;
@@ -131,26 +159,45 @@ __global__ void __launch_bounds__(256) k_pull_vec(ExecArgs<T> a) {
     const int cend = min(base + a.chunk, a.n);
     if (a.smem_tier)
       for (int i = threadIdx.x; i < cend - base; i += blockDim.x)
-        *reinterpret_cast<typename F::Bits*>(&s_x[i]) = F::EMPTY;
+        *reinterpret_cast<Bits*>(&s_x[i]) = F::EMPTY;
     __syncthreads();
     bool fail = false;
-    for (int p = base + g; p < cend; p += NG) {
+    for (int pr = base + g; pr < cend; pr += NG) {
+      const int p = ADJ ? last - pr : pr;
       const int row = a.perm[p];
-      const int e0 = a.dep_ptr[p], e1 = a.dep_ptr[p + 1];
+      const int e0 = lptr[p], e1 = lptr[p + 1];
       const T bi = a.b[(long long)row * a.b_si];
-      const T dg = EXACT ? a.diag[p] : T(0);
-      const T rc = EXACT ? T(0) : a.rcp[p];
       T acc = T(0);
-      for (int e = e0 + lane; e < e1; e += G) {
-        const int q = a.dep_pos[e];
-        const T v = a.dep_val[e];
-        typename F::Bits bits;
-        if (a.smem_tier && q >= base)
-          bits = wait_flag<T, true>(&s_x[q - base], a.ctl, a.timeout_ns, p);
-        else
-          bits = wait_flag<T, false>(&a.xw[q], a.ctl, a.timeout_ns, p);
-        if (bits == F::EMPTY) { fail = true; break; }
-        acc = mul_add<T>(acc, v, F::value(bits), EXACT);
+      if (!EXACT && lane == 0) acc = bi * a.rcp[p];
+      for (int eb = e0 + lane; eb < e1 && !fail; eb += G * U) {
+        int q[U];
+        T w[U];
+        Bits bits[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int e = eb + u * G;
+          q[u] = e < e1 ? lpos[e] : -1;
+          w[u] = e < e1 ? vals[e] : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          bits[u] = F::EMPTY;
+          if (q[u] >= 0) {
+            const int qr = ADJ ? last - q[u] : q[u];
+            bits[u] = (a.smem_tier && qr >= base) ? F::load_shared(&s_x[qr - base]) : F::load(&a.xw[q[u]]);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          if (q[u] < 0 || fail) continue;
+          if (bits[u] == F::EMPTY) {
+            const int qr = ADJ ? last - q[u] : q[u];
+            bits[u] = (a.smem_tier && qr >= base) ? wait_flag<T, true>(&s_x[qr - base], a.ctl, a.timeout_ns, p, a.sleep_min, a.sleep_max)
+                                                  : wait_flag<T, false>(&a.xw[q[u]], a.ctl, a.timeout_ns, p, a.sleep_min, a.sleep_max);
+            if (bits[u] == F::EMPTY) { fail = true; continue; }
+          }
+          acc = EXACT ? mul_add<T>(acc, w[u], F::value(bits[u]), true) : fma(-w[u], F::value(bits[u]), acc);
+        }
       }
       if (G > 1) {
         fail = __any_sync(gmask, fail);
@@ -158,11 +205,16 @@ __global__ void __launch_bounds__(256) k_pull_vec(ExecArgs<T> a) {
         for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(gmask, acc, o);
       }
       if (fail) break;
-      const T xi = finish<T>(bi, acc, dg, rc, EXACT);
+      const T xi = EXACT ? finish<T>(bi, acc, a.diag[p], T(0), true) : acc;
       if (lane == 0) {
-        if (a.smem_tier) F::store_shared(&s_x[p - base], xi);
+        if (a.smem_tier) F::store_shared(&s_x[pr - base], xi);
         F::store(&a.xw[p], xi);
         a.x[(long long)row * a.x_si] = xi;
+      }
+      if (ADJ && a.grad) {
+        for (int e = a.dep_ptr[p] + lane; e < a.dep_ptr[p + 1]; e += G)
+          a.grad[a.dep_src[e]] = -xi * a.xf[(long long)a.dep_col[e] * a.xf_si];
+        if (lane == 0) a.grad[a.diag_src[p]] = -xi * a.xf[(long long)row * a.xf_si];
       }
     }
     if (__syncthreads_or(fail)) break;
@@ -172,7 +224,7 @@ __global__ void __launch_bounds__(256) k_pull_vec(ExecArgs<T> a) {
 
 // ------------------------------------------------------------------ pull, many rhs
 // Lanes of a group cover right-hand sides; dependencies are walked in order.
-template <typename T, int G, int RPL, bool EXACT>
+template <typename T, int G, int RPL, bool EXACT, bool ADJ>
 __global__ void __launch_bounds__(256) k_pull_multi(ExecArgs<T> a) {
   using F = Flag<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -182,6 +234,10 @@ __global__ void __launch_bounds__(256) k_pull_multi(ExecArgs<T> a) {
   const int g = threadIdx.x / G, lane = threadIdx.x % G;
   const unsigned gmask = group_mask(G);
   const int rhs = a.rhs;
+  const int* __restrict__ lptr = ADJ ? a.out_ptr : a.dep_ptr;
+  const int* __restrict__ lpos = ADJ ? a.out_pos : a.dep_pos;
+  const T* __restrict__ vals = ADJ ? (EXACT ? a.out_val : a.out_w) : (EXACT ? a.dep_val : a.dep_w);
+  const int last = a.n - 1;
   for (;;) {
     const unsigned c = next_chunk(a.ctl, a.nchunks, &s_chunk);
     if (c >= (unsigned)a.nchunks) break;
@@ -192,30 +248,35 @@ __global__ void __launch_bounds__(256) k_pull_multi(ExecArgs<T> a) {
         *reinterpret_cast<typename F::Bits*>(&s_x[i]) = F::EMPTY;
     __syncthreads();
     bool fail = false;
-    for (int p = base + g; p < cend && !fail; p += NG) {
+    for (int pr = base + g; pr < cend && !fail; pr += NG) {
+      const int p = ADJ ? last - pr : pr;
       const int row = a.perm[p];
-      const int e0 = a.dep_ptr[p], e1 = a.dep_ptr[p + 1];
+      const int e0 = lptr[p], e1 = lptr[p + 1];
       const T dg = EXACT ? a.diag[p] : T(0);
       const T rc = EXACT ? T(0) : a.rcp[p];
       for (int kt = 0; kt < rhs && !fail; kt += G * RPL) {
         T acc[RPL];
 #pragma unroll
-        for (int j = 0; j < RPL; ++j) acc[j] = T(0);
+        for (int j = 0; j < RPL; ++j) {
+          const int k = kt + lane + j * G;
+          acc[j] = (!EXACT && k < rhs) ? a.b[(long long)row * a.b_si + (long long)k * a.b_sk] * rc : T(0);
+        }
         for (int e = e0; e < e1 && !fail; ++e) {
-          const int q = a.dep_pos[e];
-          const T v = a.dep_val[e];
-          const bool local = a.smem_tier && q >= base;
+          const int q = lpos[e];
+          const int qr = ADJ ? last - q : q;
+          const T v = vals[e];
+          const bool local = a.smem_tier && qr >= base;
 #pragma unroll
           for (int j = 0; j < RPL; ++j) {
             const int k = kt + lane + j * G;
             if (k < rhs && !fail) {
               typename F::Bits bits;
               if (local)
-                bits = wait_flag<T, true>(&s_x[(long long)(q - base) * rhs + k], a.ctl, a.timeout_ns, p);
+                bits = wait_flag<T, true>(&s_x[(long long)(qr - base) * rhs + k], a.ctl, a.timeout_ns, p, a.sleep_min, a.sleep_max);
               else
-                bits = wait_flag<T, false>(&a.xw[(long long)q * rhs + k], a.ctl, a.timeout_ns, p);
+                bits = wait_flag<T, false>(&a.xw[(long long)q * rhs + k], a.ctl, a.timeout_ns, p, a.sleep_min, a.sleep_max);
               if (bits == F::EMPTY) fail = true;
-              else acc[j] = mul_add<T>(acc[j], v, F::value(bits), EXACT);
+              else acc[j] = EXACT ? mul_add<T>(acc[j], v, F::value(bits), true) : fma(-v, F::value(bits), acc[j]);
             }
           }
         }
@@ -225,11 +286,30 @@ __global__ void __launch_bounds__(256) k_pull_multi(ExecArgs<T> a) {
         for (int j = 0; j < RPL; ++j) {
           const int k = kt + lane + j * G;
           if (k < rhs) {
-            const T bi = a.b[(long long)row * a.b_si + (long long)k * a.b_sk];
-            const T xi = finish<T>(bi, acc[j], dg, rc, EXACT);
-            if (a.smem_tier) F::store_shared(&s_x[(long long)(p - base) * rhs + k], xi);
+            const T xi = EXACT ? finish<T>(a.b[(long long)row * a.b_si + (long long)k * a.b_sk], acc[j], dg, rc, true)
+                               : acc[j];
+            acc[j] = xi;
+            if (a.smem_tier) F::store_shared(&s_x[(long long)(pr - base) * rhs + k], xi);
             F::store(&a.xw[(long long)p * rhs + k], xi);
             a.x[(long long)row * a.x_si + (long long)k * a.x_sk] = xi;
+          }
+        }
+        if (ADJ && a.grad) {
+          // dL(p,j) = -sum_k lambda_{p,k} x_{j,k}: this tile's share, reduced over the group
+          for (int e = a.dep_ptr[p] - 1; e < a.dep_ptr[p + 1]; ++e) {
+            const int col = e < a.dep_ptr[p] ? row : a.dep_col[e];
+            T part = T(0);
+#pragma unroll
+            for (int j = 0; j < RPL; ++j) {
+              const int k = kt + lane + j * G;
+              if (k < rhs) part = fma(acc[j], a.xf[(long long)col * a.xf_si + (long long)k * a.xf_sk], part);
+            }
+#pragma unroll
+            for (int o = G / 2; o > 0; o >>= 1) part += __shfl_xor_sync(gmask, part, o);
+            if (lane == 0) {
+              T* dst = &a.grad[e < a.dep_ptr[p] ? a.diag_src[p] : a.dep_src[e]];
+              *dst = (kt == 0 ? T(0) : *dst) - part;
+            }
           }
         }
       }
@@ -270,7 +350,7 @@ __global__ void __launch_bounds__(256) k_push_vec(ExecArgs<T> a) {
       T sum = T(0);
       if (lane == 0) {
         // Consumer: wait until global + shared arrivals cover the in-degree.
-        WaitBudget w(a.timeout_ns);
+        WaitBudget w(a.timeout_ns, a.sleep_min, a.sleep_max);
         for (;;) {
           unsigned got = target == 0u ? 0u : ld_acquire_u32(&a.counters[p]);
           if (a.smem_tier && target != 0u) got += ld_shared_acquire_u32(&s_cnt[p - base]);
@@ -334,7 +414,7 @@ __global__ void __launch_bounds__(256) k_push_multi(ExecArgs<T> a) {
       const int col = a.perm[p];
       const unsigned target = static_cast<unsigned>(a.dep_ptr[p + 1] - a.dep_ptr[p]);
       if (lane == 0 && target != 0u) {
-        WaitBudget w(a.timeout_ns);
+        WaitBudget w(a.timeout_ns, a.sleep_min, a.sleep_max);
         while (ld_acquire_u32(&a.counters[p]) != target) {
           if (!w.poll(a.ctl, p)) { fail = true; break; }
         }
@@ -406,15 +486,15 @@ __global__ void __launch_bounds__(256) k_levelset(ExecArgs<T> a) {
       const int e0 = a.dep_ptr[p], e1 = a.dep_ptr[p + 1];
       const T rc = a.rcp[p];
       for (int k = 0; k < rhs; ++k) {
-        T acc = T(0);
+        T acc = lane == 0 ? a.b[(long long)row * a.b_si + (long long)k * a.b_sk] * rc : T(0);
         for (int e = e0 + lane; e < e1; e += G)
-          acc = fma(a.dep_val[e], F::value(F::load(&a.xw[(long long)a.dep_pos[e] * rhs + k])), acc);
+          acc = fma(-a.dep_w[e], F::value(F::load(&a.xw[(long long)a.dep_pos[e] * rhs + k])), acc);
         if (G > 1) {
 #pragma unroll
           for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(gmask, acc, o);
         }
         if (lane == 0) {
-          const T xi = (a.b[(long long)row * a.b_si + (long long)k * a.b_sk] - acc) * rc;
+          const T xi = acc;
           F::store(&a.xw[(long long)p * rhs + k], xi);
           a.x[(long long)row * a.x_si + (long long)k * a.x_sk] = xi;
         }
@@ -427,6 +507,8 @@ __global__ void __launch_bounds__(256) k_levelset(ExecArgs<T> a) {
 template <typename T>
 ExecArgs<T> make_args(const Layout& L, const Values<T>& V, int rhs, const VecView<T>& v, int chunk) {
   ExecArgs<T> a{};
+  a.sleep_min = 0;
+  a.sleep_max = 0;
   a.n = L.n;
   a.rhs = rhs;
   a.chunk = chunk;
@@ -435,6 +517,11 @@ ExecArgs<T> make_args(const Layout& L, const Values<T>& V, int rhs, const VecVie
   a.dep_ptr = L.dep_ptr;
   a.dep_pos = L.dep_pos;
   a.dep_val = V.dep_val;
+  a.dep_w = V.dep_w;
+  a.dep_src = L.dep_src;
+  a.dep_col = L.dep_col;
+  a.diag_src = L.diag_src;
+  a.out_w = V.out_w;
   a.out_ptr = L.out_ptr;
   a.out_pos = L.out_pos;
   a.out_val = V.out_val;
@@ -450,10 +537,11 @@ ExecArgs<T> make_args(const Layout& L, const Values<T>& V, int rhs, const VecVie
 }
 
 template <typename K>
-int persistent_grid(K kernel, int block, size_t smem, int num_sms, int nchunks) {
+int persistent_grid(K kernel, int block, size_t smem, int num_sms, int nchunks, int cap_per_sm) {
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
   if (per_sm < 1) per_sm = 1;
+  if (cap_per_sm > 0 && per_sm > cap_per_sm) per_sm = cap_per_sm;
   long long grid = (long long)num_sms * per_sm;
   if (grid > nchunks) grid = nchunks;
   if (grid < 1) grid = 1;
@@ -469,7 +557,7 @@ cudaError_t run(K kernel, const ExecArgs<T>& a, int block, size_t smem, int num_
     cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  const int grid = persistent_grid(kernel, block, smem, num_sms, a.nchunks);
+  const int grid = persistent_grid(kernel, block, smem, num_sms, a.nchunks, a.ctas_per_sm);
   kernel<<<grid, block, smem, s>>>(a);
   return cudaGetLastError();
 }
@@ -478,14 +566,45 @@ cudaError_t run(K kernel, const ExecArgs<T>& a, int block, size_t smem, int num_
 
 size_t pull_smem_bytes(int chunk, int rhs, size_t elem) { return (size_t)chunk * (size_t)rhs * elem; }
 
+template <typename T, bool ADJ>
+cudaError_t launch_pull_impl(ExecArgs<T>& a, int rhs, const ExecConfig& cfg, size_t smem, int num_sms,
+                             cudaStream_t s) {
+  const int block = cfg.block;
+  if (rhs == 1) {
+    if (cfg.exact) return run(k_pull_vec<T, 1, true, 4, ADJ>, a, block, smem, num_sms, s);
+    switch (cfg.lanes) {
+      case 1: return run(k_pull_vec<T, 1, false, 4, ADJ>, a, block, smem, num_sms, s);
+      case 2: return run(k_pull_vec<T, 2, false, 2, ADJ>, a, block, smem, num_sms, s);
+      case 4: return run(k_pull_vec<T, 4, false, 2, ADJ>, a, block, smem, num_sms, s);
+      case 8: return run(k_pull_vec<T, 8, false, 1, ADJ>, a, block, smem, num_sms, s);
+      case 16: return run(k_pull_vec<T, 16, false, 1, ADJ>, a, block, smem, num_sms, s);
+      default: return run(k_pull_vec<T, 32, false, 1, ADJ>, a, block, smem, num_sms, s);
+    }
+  }
+  // many right-hand sides: lanes over rhs
+  if (cfg.exact) {
+    if (rhs <= 8) return run(k_pull_multi<T, 8, 1, true, ADJ>, a, block, smem, num_sms, s);
+    return run(k_pull_multi<T, 32, 2, true, ADJ>, a, block, smem, num_sms, s);
+  }
+  if (rhs <= 4) return run(k_pull_multi<T, 4, 1, false, ADJ>, a, block, smem, num_sms, s);
+  if (rhs <= 8) return run(k_pull_multi<T, 8, 1, false, ADJ>, a, block, smem, num_sms, s);
+  if (rhs <= 16) return run(k_pull_multi<T, 16, 1, false, ADJ>, a, block, smem, num_sms, s);
+  if (rhs <= 32) return run(k_pull_multi<T, 32, 1, false, ADJ>, a, block, smem, num_sms, s);
+  return run(k_pull_multi<T, 32, 2, false, ADJ>, a, block, smem, num_sms, s);
+}
+
 template <typename T>
 cudaError_t launch_pull(const Layout& L, const Values<T>& V, int rhs, const VecView<T>& v, T* xw, DeviceCtl* ctl,
-                        const ExecConfig& cfg, unsigned long long timeout_ns, int num_sms, cudaStream_t s) {
+                        const ExecConfig& cfg, unsigned long long timeout_ns, int num_sms, cudaStream_t s,
+                        const AdjointArgs<T>* adj) {
   if (L.n == 0) return cudaSuccess;
   ExecArgs<T> a = make_args<T>(L, V, rhs, v, cfg.chunk);
   a.xw = xw;
   a.ctl = ctl;
   a.timeout_ns = timeout_ns;
+  a.sleep_min = cfg.sleep_max ? 16u : 0u;
+  a.sleep_max = cfg.sleep_max;
+  a.ctas_per_sm = cfg.ctas_per_sm;
   size_t smem = 0;
   a.smem_tier = 0;
   if (cfg.smem_tier) {
@@ -493,28 +612,14 @@ cudaError_t launch_pull(const Layout& L, const Values<T>& V, int rhs, const VecV
     if (smem <= 200 * 1024) a.smem_tier = 1;
     else smem = 0;
   }
-  const int block = 256;
-  if (rhs == 1) {
-    if (cfg.exact) return run(k_pull_vec<T, 1, true>, a, block, smem, num_sms, s);
-    switch (cfg.lanes) {
-      case 1: return run(k_pull_vec<T, 1, false>, a, block, smem, num_sms, s);
-      case 2: return run(k_pull_vec<T, 2, false>, a, block, smem, num_sms, s);
-      case 4: return run(k_pull_vec<T, 4, false>, a, block, smem, num_sms, s);
-      case 8: return run(k_pull_vec<T, 8, false>, a, block, smem, num_sms, s);
-      case 16: return run(k_pull_vec<T, 16, false>, a, block, smem, num_sms, s);
-      default: return run(k_pull_vec<T, 32, false>, a, block, smem, num_sms, s);
-    }
+  if (adj) {
+    a.grad = adj->grad;
+    a.xf = adj->xf;
+    a.xf_si = adj->xf_si;
+    a.xf_sk = adj->xf_sk;
+    return launch_pull_impl<T, true>(a, rhs, cfg, smem, num_sms, s);
   }
-  // many right-hand sides: lanes over rhs
-  if (cfg.exact) {
-    if (rhs <= 8) return run(k_pull_multi<T, 8, 1, true>, a, block, smem, num_sms, s);
-    return run(k_pull_multi<T, 32, 2, true>, a, block, smem, num_sms, s);
-  }
-  if (rhs <= 4) return run(k_pull_multi<T, 4, 1, false>, a, block, smem, num_sms, s);
-  if (rhs <= 8) return run(k_pull_multi<T, 8, 1, false>, a, block, smem, num_sms, s);
-  if (rhs <= 16) return run(k_pull_multi<T, 16, 1, false>, a, block, smem, num_sms, s);
-  if (rhs <= 32) return run(k_pull_multi<T, 32, 1, false>, a, block, smem, num_sms, s);
-  return run(k_pull_multi<T, 32, 2, false>, a, block, smem, num_sms, s);
+  return launch_pull_impl<T, false>(a, rhs, cfg, smem, num_sms, s);
 }
 
 template <typename T>
@@ -527,7 +632,10 @@ cudaError_t launch_push(const Layout& L, const Values<T>& V, int rhs, const VecV
   a.counters = counters;
   a.ctl = ctl;
   a.timeout_ns = timeout_ns;
-  const int block = 256;
+  a.sleep_min = cfg.sleep_max ? 16u : 0u;
+  a.sleep_max = cfg.sleep_max;
+  a.ctas_per_sm = cfg.ctas_per_sm;
+  const int block = cfg.block;
   if (rhs == 1) {
     size_t smem = 0;
     a.smem_tier = 0;
@@ -570,9 +678,34 @@ cudaError_t launch_levelset(const Layout& L, const Values<T>& V, int rhs, const 
   auto kernel = cfg.lanes >= 8 ? k_levelset<T, 8> : k_levelset<T, 1>;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
   if (per_sm < 1) per_sm = 1;
-  const int grid = sms * std::min(per_sm, 4);
+  const int grid = sms * std::min(per_sm, cfg.ctas_per_sm > 0 ? cfg.ctas_per_sm : 2);
   void* args[] = {(void*)&a};
   return cudaLaunchCooperativeKernel((void*)kernel, dim3(grid), dim3(block), args, 0, s);
+}
+
+// ------------------------------------------------------------------ gradient w.r.t. values
+// dval[e] = -sum_k lambda[row(e), k] * x[col(e), k] on the stored pattern.
+template <typename T>
+__global__ void k_grad_values(const int* __restrict__ csc_row, const int* __restrict__ csc_col, int nnz, int rhs,
+                              const T* __restrict__ lambda, const T* __restrict__ x, long long si, long long sk,
+                              T* dval) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nnz; e += stride) {
+    const long long r = csc_row[e], c = csc_col[e];
+    T acc = T(0);
+    for (int k = 0; k < rhs; ++k) acc = fma(lambda[r * si + k * sk], x[c * si + k * sk], acc);
+    dval[e] = -acc;
+  }
+}
+
+template <typename T>
+cudaError_t launch_grad_values(const int* csc_row, const int* csc_col, int nnz, int rhs, const T* lambda, const T* x,
+                               long long si, long long sk, T* dval, cudaStream_t s) {
+  if (nnz <= 0) return cudaSuccess;
+  long long grid = (nnz + 255) / 256;
+  if (grid > (1 << 20)) grid = 1 << 20;
+  k_grad_values<T><<<(int)grid, 256, 0, s>>>(csc_row, csc_col, nnz, rhs, lambda, x, si, sk, dval);
+  return cudaGetLastError();
 }
 
 // ------------------------------------------------------------------ reference kernel surface
@@ -670,11 +803,14 @@ cudaError_t launch_ref_executor(const int* col_ptr, const int* row_idx, const T*
 
 #define SPTRSV_INSTANTIATE(T)                                                                                    \
   template cudaError_t launch_pull<T>(const Layout&, const Values<T>&, int, const VecView<T>&, T*, DeviceCtl*,   \
-                                      const ExecConfig&, unsigned long long, int, cudaStream_t);                 \
+                                      const ExecConfig&, unsigned long long, int, cudaStream_t,                  \
+                                      const AdjointArgs<T>*);                                                    \
   template cudaError_t launch_push<T>(const Layout&, const Values<T>&, int, const VecView<T>&, T*, unsigned*,    \
                                       DeviceCtl*, const ExecConfig&, unsigned long long, int, cudaStream_t);     \
   template cudaError_t launch_levelset<T>(const Layout&, const Values<T>&, int, const VecView<T>&, T*,           \
                                           DeviceCtl*, const ExecConfig&, unsigned long long, cudaStream_t);      \
+  template cudaError_t launch_grad_values<T>(const int*, const int*, int, int, const T*, const T*, long long,     \
+                                             long long, T*, cudaStream_t);                                       \
   template cudaError_t launch_ref_executor<T>(const int*, const int*, const T*, int*, T*, int, int, int, int,    \
                                               const T*, T*, DeviceCtl*, unsigned long long, cudaStream_t);
 SPTRSV_INSTANTIATE(double)

@@ -29,7 +29,9 @@ struct ExecConfig {
   int chunk = 1024;       // positions per CTA work unit
   int smem_tier = 1;      // resolve in-chunk dependencies through shared memory
   int exact = 0;          // oracle-order arithmetic (pull only)
-  int block = 256;        // threads per CTA
+  int block = 256;        // threads per CTA (64, 128 or 256)
+  int ctas_per_sm = 0;    // resident CTAs per SM (0: as many as fit)
+  unsigned sleep_max = 0; // backoff cap of global polls in ns (0: spin)
 };
 
 // Solve-time description of one right-hand-side block. Element (i, k) of b
@@ -53,8 +55,10 @@ struct Layout {
   int* dep_ptr = nullptr;    // [n+1]
   int* dep_pos = nullptr;    // [ndep]
   int* dep_src = nullptr;    // [ndep] CSC entry index (for value staging)
+  int* dep_col = nullptr;    // [ndep] column (unknown) of the dependency
   int* diag_src = nullptr;   // [n]
-  // push layout (dependents of each position, diagonal excluded)
+  // push layout (dependents of each position, diagonal excluded), listed in the
+  // order the serial executor applied to the transpose accumulates them
   int* out_ptr = nullptr;    // [n+1]
   int* out_pos = nullptr;    // [ndep]
   int* out_src = nullptr;    // [ndep]
@@ -67,7 +71,9 @@ struct Layout {
 template <typename T>
 struct Values {
   T* dep_val = nullptr;  // [ndep]
+  T* dep_w = nullptr;    // [ndep] dep_val scaled by the reciprocal of its row's diagonal
   T* out_val = nullptr;  // [ndep]
+  T* out_w = nullptr;    // [ndep] out_val scaled by the reciprocal of the owning position's diagonal
   T* diag = nullptr;     // [n]
   T* rcp = nullptr;      // [n] correctly rounded 1/diag
 };
@@ -97,7 +103,7 @@ cudaError_t launch_dep_counts(const int* perm, const int* in_degree, int n, int*
 cudaError_t launch_out_counts(const int* perm, const int* col_ptr, int n, int* counts, cudaStream_t s);
 cudaError_t launch_fill_pull(const int* perm, const int* iperm, const int* csr_ptr, const int* csr_col,
                              const int* csr_src, const int* dep_ptr, int n, int substitution,
-                             int* dep_pos, int* dep_src, int* diag_src, cudaStream_t s);
+                             int* dep_pos, int* dep_src, int* dep_col, int* diag_src, cudaStream_t s);
 cudaError_t launch_fill_push(const int* perm, const int* iperm, const int* col_ptr, const int* row_idx,
                              const int* out_ptr, int n, int substitution, int* out_pos, int* out_src,
                              cudaStream_t s);
@@ -105,10 +111,17 @@ template <typename TV, typename T>
 cudaError_t launch_stage_values(const Layout& L, const TV* val, Values<T>& V, int* flags, cudaStream_t s);
 
 // ---------------------------------------------------------------- execution
+// Transposed (adjoint) solve request: optional fused gradient w.r.t. the values.
+template <typename T>
+struct AdjointArgs {
+  T* grad = nullptr;       // [nnz] CSC order, or null
+  const T* xf = nullptr;   // forward solution (row-indexed, strides below)
+  long long xf_si = 0, xf_sk = 0;
+};
 template <typename T>
 cudaError_t launch_pull(const Layout& L, const Values<T>& V, int rhs, const VecView<T>& v, T* xw,
                         DeviceCtl* ctl, const ExecConfig& cfg, unsigned long long timeout_ns,
-                        int num_sms, cudaStream_t s);
+                        int num_sms, cudaStream_t s, const AdjointArgs<T>* adj = nullptr);
 template <typename T>
 cudaError_t launch_push(const Layout& L, const Values<T>& V, int rhs, const VecView<T>& v, T* left_sum,
                         unsigned* counters, DeviceCtl* ctl, const ExecConfig& cfg,
@@ -118,6 +131,10 @@ cudaError_t launch_levelset(const Layout& L, const Values<T>& V, int rhs, const 
                             DeviceCtl* ctl, const ExecConfig& cfg, unsigned long long timeout_ns,
                             cudaStream_t s);
 size_t pull_smem_bytes(int chunk, int rhs, size_t elem);
+
+template <typename T>
+cudaError_t launch_grad_values(const int* csc_row, const int* csc_col, int nnz, int rhs, const T* lambda,
+                               const T* x, long long si, long long sk, T* dval, cudaStream_t s);
 
 // Kernel-level surface of the reference: in-degree countdown counters owned by
 // the caller, natural column order, one warp per column.

@@ -11,8 +11,14 @@ from ._lib import (DTYPE_F32, DTYPE_F64, LAYOUT_COL_MAJOR, LAYOUT_ROW_MAJOR, OPT
                    SUBSTITUTION_FORWARD, SptrsvError, load)
 from .solver import SyncFreeSolver, analyser, executor, sptrsv_syncfree_cuda
 
+
+def sparse_triangular_solve(solver, values, b):
+    """Differentiable x = op(L)^-1 b (see sptrsv_gb300.autograd)."""
+    from .autograd import sparse_triangular_solve as _f
+    return _f(solver, values, b)
+
 __all__ = [
-    "matgen", "load", "SptrsvError", "SyncFreeSolver", "analyser", "executor", "sptrsv_syncfree_cuda",
+    "matgen", "load", "sparse_triangular_solve", "SptrsvError", "SyncFreeSolver", "analyser", "executor", "sptrsv_syncfree_cuda",
     "SUBSTITUTION_FORWARD", "SUBSTITUTION_BACKWARD", "OPT_WARP_NNZ", "OPT_WARP_RHS", "OPT_WARP_AUTO",
     "LAYOUT_ROW_MAJOR", "LAYOUT_COL_MAJOR", "DTYPE_F64", "DTYPE_F32", "SCHED_AUTO", "SCHED_PUSH",
     "SCHED_PULL", "SCHED_LEVELSET",

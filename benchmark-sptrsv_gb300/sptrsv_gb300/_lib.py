@@ -50,6 +50,9 @@ OPTION_ORDER_BLOCK = 5
 OPTION_TIMEOUT_MS = 6
 OPTION_SYNC_CHECK = 7
 OPTION_PROFILE = 8
+OPTION_BLOCK = 9
+OPTION_BACKOFF_NS = 10
+OPTION_CTAS_PER_SM = 11
 
 
 class SptrsvError(RuntimeError):
@@ -107,6 +110,8 @@ SIGNATURES = {
     "sptrsv_gb300_set_values": (_I, [_VP, _VP, _I, _VP]),
     "sptrsv_gb300_solve": (_I, [_VP, _VP, _I, _I, _I, _VP, _VP, _VP]),
     "sptrsv_gb300_check": (_I, [_VP, _VP]),
+    "sptrsv_gb300_solve_adjoint": (_I, [_VP, _VP, _I, _I, _I, _VP, _VP, _VP, _VP, _VP]),
+    "sptrsv_gb300_grad_values": (_I, [_VP, _I, _I, _I, _VP, _VP, _VP, _VP]),
     "sptrsv_gb300_exec_ms": (_I, [_VP, _PD]),
 }
 

@@ -94,7 +94,8 @@ class SyncFreeSolver:
     def __init__(self, col_ptr, row_idx, n: int | None = None, substitution: int = 0, *, values=None,
                  schedule: int = SCHED_AUTO, lanes: int = 0, chunk: int = 0, order_block: int | None = None,
                  exact: bool = False, smem_tier: bool = True, timeout_ms: int = 1000, sync_check: bool = True,
-                 profile: bool = False, stream=None):
+                 profile: bool = False, block: int = 0, backoff_ns: int | None = None, ctas_per_sm: int = 0,
+                 stream=None):
         torch = _torch()
         self._lib = load()
         self.device = torch.device("cuda", torch.cuda.current_device())
@@ -116,6 +117,10 @@ class SyncFreeSolver:
         self.set_option(_lib.OPTION_TIMEOUT_MS, timeout_ms)
         self.set_option(_lib.OPTION_SYNC_CHECK, int(sync_check))
         self.set_option(_lib.OPTION_PROFILE, int(profile))
+        self.set_option(_lib.OPTION_BLOCK, int(block))
+        if backoff_ns is not None:
+            self.set_option(_lib.OPTION_BACKOFF_NS, int(backoff_ns))
+        self.set_option(_lib.OPTION_CTAS_PER_SM, int(ctas_per_sm))
         self._stream = stream
         self.analyse()
         self.values = None
@@ -190,6 +195,61 @@ class SyncFreeSolver:
                                           _stream_ptr(self._stream))
         check(st, "solve")
         return out.reshape(b.shape) if b.dim() == 1 else out
+
+    def _layout_of(self, t):
+        torch = _torch()
+        t2 = t.reshape(-1, 1) if t.dim() == 1 else t
+        if t2.is_contiguous():
+            return t2, LAYOUT_ROW_MAJOR
+        if t2.t().is_contiguous():
+            return t2, LAYOUT_COL_MAJOR
+        return t2.contiguous(), LAYOUT_ROW_MAJOR
+
+    def solve_adjoint(self, g, x=None, *, values=None, grad_values: bool = False, out=None):
+        """Solve op(L)^T lambda = g on the same analysis (reverse dependency order).
+        With ``grad_values`` (needs the forward solution ``x``), also returns
+        dL[e] = -sum_k lambda[row(e),k] x[col(e),k] over the stored pattern, formed by the
+        same kernel as lambda. Returns (lambda, dval or None)."""
+        torch = _torch()
+        g2, layout = self._layout_of(g)
+        rhs = int(g2.shape[1])
+        dt = DTYPE_F64 if g2.dtype == torch.float64 else DTYPE_F32
+        if out is None:
+            out = (torch.empty_like(g2, memory_format=torch.contiguous_format) if layout == LAYOUT_ROW_MAJOR
+                   else torch.empty((rhs, self.n), dtype=g2.dtype, device=g2.device).t())
+        xp = ctypes.c_void_p(0)
+        dval = None
+        if grad_values:
+            if x is None:
+                raise ValueError("grad_values needs the forward solution x")
+            x2, xl = self._layout_of(x)
+            if xl != layout:
+                x2 = x2.contiguous() if layout == LAYOUT_ROW_MAJOR else x2.t().contiguous().t()
+            xp = _ptr(x2)
+            dval = torch.empty(self.nnz, dtype=g2.dtype, device=g2.device)
+            self._keep = x2
+        vptr = ctypes.c_void_p(0)
+        if values is not None:
+            v = values.to(self.device).contiguous()
+            self.values = v
+            vptr = _ptr(v)
+        check(self._lib.sptrsv_gb300_solve_adjoint(self._h, vptr, dt, rhs, layout, _ptr(g2), _ptr(out), xp,
+                                                   _ptr(dval), _stream_ptr(self._stream)), "solve_adjoint")
+        lam = out.reshape(g.shape) if g.dim() == 1 else out
+        return lam, dval
+
+    def grad_values(self, lam, x):
+        """dL[e] = -sum_k lam[row(e),k] x[col(e),k] (standalone kernel)."""
+        torch = _torch()
+        l2, layout = self._layout_of(lam)
+        x2, xl = self._layout_of(x)
+        if xl != layout:
+            x2 = x2.contiguous() if layout == LAYOUT_ROW_MAJOR else x2.t().contiguous().t()
+        dt = DTYPE_F64 if l2.dtype == torch.float64 else DTYPE_F32
+        dval = torch.empty(self.nnz, dtype=l2.dtype, device=l2.device)
+        check(self._lib.sptrsv_gb300_grad_values(self._h, dt, int(l2.shape[1]), layout, _ptr(l2), _ptr(x2),
+                                                 _ptr(dval), _stream_ptr(self._stream)), "grad_values")
+        return dval
 
     def exec_ms(self) -> float:
         """Device time of the last executor launch (needs profile=True)."""

@@ -83,8 +83,11 @@ typedef enum sptrsv_option {
   SPTRSV_OPTION_TIMEOUT_MS = 6,   /* bound of every device wait, milliseconds */
   SPTRSV_OPTION_SYNC_CHECK = 7,   /* 1 (default): solve calls synchronise and report device errors;
                                      0: fully asynchronous, errors surface in sptrsv_gb300_check */
-  SPTRSV_OPTION_PROFILE = 8       /* 1: record CUDA events around each executor launch
+  SPTRSV_OPTION_PROFILE = 8,      /* 1: record CUDA events around each executor launch
                                      (read with sptrsv_gb300_exec_ms) */
+  SPTRSV_OPTION_BLOCK = 9,        /* threads per CTA of the sync-free executors: 64, 128, 256 (0 = auto) */
+  SPTRSV_OPTION_BACKOFF_NS = 10,  /* cap of the sleep between two polls of a global flag (0 = spin) */
+  SPTRSV_OPTION_CTAS_PER_SM = 11  /* resident CTAs per SM of the executors (0 = as many as fit) */
 } sptrsv_option;
 
 typedef struct sptrsv_info {
@@ -189,6 +192,20 @@ int sptrsv_gb300_set_values(sptrsv_handle_t handle, const void *d_val, int dtype
  * values. b and x must not overlap. */
 int sptrsv_gb300_solve(sptrsv_handle_t handle, const void *d_val, int dtype, int rhs, int layout, const void *d_b,
                        void *d_x, void *stream);
+
+/* Transposed (adjoint) solve op(L)^T Lambda = G on the same analysis, walked
+ * in reverse dependency order (pull executor). With d_x (the forward solution
+ * X, same layout) and d_dval both non-NULL, the same kernel also writes the
+ * gradient of a loss with dLoss/dX = G with respect to every stored value:
+ * d_dval[e] = -sum_k Lambda[row(e),k] * X[col(e),k] (CSC entry order); the
+ * gradient with respect to B is Lambda itself. d_val as in sptrsv_gb300_solve. */
+int sptrsv_gb300_solve_adjoint(sptrsv_handle_t handle, const void *d_val, int dtype, int rhs, int layout,
+                               const void *d_g, void *d_lambda, const void *d_x, void *d_dval, void *stream);
+
+/* Standalone gradient kernel: d_dval[e] = -sum_k Lambda[row(e),k] * X[col(e),k]
+ * over the stored pattern (CSC entry order). */
+int sptrsv_gb300_grad_values(sptrsv_handle_t handle, int dtype, int rhs, int layout, const void *d_lambda,
+                             const void *d_x, void *d_dval, void *stream);
 
 /* Synchronises `stream` and reports (then clears) a device error raised by
  * asynchronous solves since the last check. */
