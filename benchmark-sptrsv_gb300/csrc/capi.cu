@@ -63,7 +63,7 @@ struct sptrsv_gb300_handle_s {
   Values<float> v32;
   bool staged64 = false, staged32 = false;
   // workspace
-  DevBuf xw, left_sum, counters;
+  DevBuf xw, left_sum, counters, r32, d32, stats;
   DeviceCtl* ctl = nullptr;
   int* flags = nullptr;
   int* host_pinned = nullptr;  // 4 ints
@@ -358,7 +358,7 @@ ExecConfig pick_config(const sptrsv_gb300_handle_s* h, int rhs) {
 
 template <typename T>
 int solve_typed(sptrsv_gb300_handle_s* h, const Values<T>& V, int rhs, int layout, const T* b, T* x,
-                cudaStream_t s, const AdjointArgs<T>* adj = nullptr) {
+                cudaStream_t s, const AdjointArgs<T>* adj = nullptr, bool allow_check = true) {
   const int n = h->n;
   VecView<T> v{};
   v.b = b;
@@ -401,7 +401,7 @@ int solve_typed(sptrsv_gb300_handle_s* h, const Values<T>& V, int rhs, int layou
     CUDA_TRY(cudaEventRecord(h->ev_exec[1], s));
     h->ev_recorded = true;
   }
-  if (h->sync_check) return check_device(h, s);
+  if (h->sync_check && allow_check) return check_device(h, s);
   return SPTRSV_OK;
 }
 
@@ -476,6 +476,9 @@ int sptrsv_gb300_destroy(sptrsv_handle_t h) {
   free_buf(h->xw);
   free_buf(h->left_sum);
   free_buf(h->counters);
+  free_buf(h->r32);
+  free_buf(h->d32);
+  free_buf(h->stats);
   if (h->ctl) cudaFree(h->ctl);
   if (h->flags) cudaFree(h->flags);
   if (h->host_pinned) cudaFreeHost(h->host_pinned);
@@ -785,6 +788,76 @@ int sptrsv_gb300_solve(sptrsv_handle_t h, const void* d_val, int dtype, int rhs,
   }
   if (!h->staged32) return SPTRSV_ERR_STATE;
   return solve_typed<float>(h, h->v32, rhs, layout, static_cast<const float*>(d_b), static_cast<float*>(d_x), s);
+}
+
+int sptrsv_gb300_solve_refine(sptrsv_handle_t h, const double* d_val, int rhs, int layout, const double* d_b,
+                              double* d_x, double tol, int max_iter, int* iters, double* est, void* stream) {
+  if (iters) *iters = 0;
+  if (est) *est = NAN;
+  if (!h) return SPTRSV_ERR_INVALID;
+  if (!h->analysed) return SPTRSV_ERR_STATE;
+  if (rhs < 1 || max_iter < 1 || (layout != SPTRSV_LAYOUT_ROW_MAJOR && layout != SPTRSV_LAYOUT_COL_MAJOR))
+    return SPTRSV_ERR_INVALID;
+  if (h->n == 0) return SPTRSV_OK;
+  if (!d_b || !d_x) return SPTRSV_ERR_INVALID;
+  if ((long long)h->n * rhs > INT_MAX) return SPTRSV_ERR_UNSUPPORTED;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int before = h->layout_block;
+  ST_TRY(ensure_layout(h, s));
+  if (d_val) {
+    ST_TRY(stage_values(h, d_val, SPTRSV_DTYPE_F64, s, h->sync_check != 0));
+  } else if (h->layout_block != before) {
+    return SPTRSV_ERR_STATE;
+  }
+  if (!h->staged64 || !h->staged32) return SPTRSV_ERR_STATE;
+  const long long count = (long long)h->n * rhs;
+  ST_TRY(ensure_buf(h, h->r32, sizeof(float) * count, 0, s));
+  ST_TRY(ensure_buf(h, h->d32, sizeof(float) * count, 0, s));
+  ST_TRY(ensure_buf(h, h->stats, 2 * sizeof(unsigned long long), 1, s));
+  const long long si = layout == SPTRSV_LAYOUT_ROW_MAJOR ? rhs : 1;
+  const long long sk = layout == SPTRSV_LAYOUT_ROW_MAJOR ? 1 : h->n;
+  float* r32 = static_cast<float*>(h->r32.p);
+  float* d32 = static_cast<float*>(h->d32.p);
+  auto* stats = static_cast<unsigned long long*>(h->stats.p);
+  const bool checked = tol > 0.0;
+  // X_0 = FP32 solve of (float) B
+  CUDA_TRY(launch_cast_d2f(d_b, r32, count, s));
+  ST_TRY(solve_typed<float>(h, h->v32, rhs, layout, r32, d32, s, nullptr, false));
+  CUDA_TRY(cudaMemsetAsync(stats, 0, 2 * sizeof(unsigned long long), s));
+  CUDA_TRY(launch_update(d_x, d32, count, stats, true, s));
+  double prev = 0.0, xmax = 0.0, estimate = NAN;
+  unsigned long long host_stats[2] = {0, 0};
+  if (checked) {
+    CUDA_TRY(cudaMemcpyAsync(host_stats, stats, sizeof(host_stats), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    std::memcpy(&prev, &host_stats[1], sizeof(double));
+    xmax = prev;
+  }
+  int it = 0;
+  bool converged = false;
+  for (it = 1; it <= max_iter; ++it) {
+    CUDA_TRY(launch_residual(h->layout, h->v64, rhs, d_b, d_x, si, sk, r32, s));
+    ST_TRY(solve_typed<float>(h, h->v32, rhs, layout, r32, d32, s, nullptr, false));
+    CUDA_TRY(cudaMemsetAsync(stats, 0, 2 * sizeof(unsigned long long), s));
+    CUDA_TRY(launch_update(d_x, d32, count, stats, false, s));
+    if (!checked) continue;
+    CUDA_TRY(cudaMemcpyAsync(host_stats, stats, sizeof(host_stats), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    double dmax = 0.0;
+    std::memcpy(&dmax, &host_stats[0], sizeof(double));
+    std::memcpy(&xmax, &host_stats[1], sizeof(double));
+    estimate = (prev > 0.0 && xmax > 0.0) ? dmax * (dmax / prev) / xmax : (dmax == 0.0 ? 0.0 : INFINITY);
+    if (estimate <= tol) {
+      converged = true;
+      break;
+    }
+    prev = dmax;
+  }
+  if (iters) *iters = it > max_iter ? max_iter : it;
+  if (est) *est = estimate;
+  if (h->sync_check || checked) ST_TRY(check_device(h, s));
+  if (checked && !converged) return SPTRSV_ERR_NOT_CONVERGED;
+  return SPTRSV_OK;
 }
 
 int sptrsv_gb300_solve_adjoint(sptrsv_handle_t h, const void* d_val, int dtype, int rhs, int layout, const void* d_g,

@@ -136,6 +136,13 @@ template <typename T>
 cudaError_t launch_grad_values(const int* csc_row, const int* csc_col, int nnz, int rhs, const T* lambda,
                                const T* x, long long si, long long sk, T* dval, cudaStream_t s);
 
+// ---------------------------------------------------------------- mixed precision
+cudaError_t launch_cast_d2f(const double* in, float* out, long long count, cudaStream_t s);
+cudaError_t launch_residual(const Layout& L, const Values<double>& V, int rhs, const double* b, const double* x,
+                            long long si, long long sk, float* r, cudaStream_t s);
+cudaError_t launch_update(double* x, const float* d, long long count, unsigned long long* stats, bool first,
+                          cudaStream_t s);
+
 // Kernel-level surface of the reference: in-degree countdown counters owned by
 // the caller, natural column order, one warp per column.
 template <typename T>

@@ -110,6 +110,7 @@ SIGNATURES = {
     "sptrsv_gb300_set_values": (_I, [_VP, _VP, _I, _VP]),
     "sptrsv_gb300_solve": (_I, [_VP, _VP, _I, _I, _I, _VP, _VP, _VP]),
     "sptrsv_gb300_check": (_I, [_VP, _VP]),
+    "sptrsv_gb300_solve_refine": (_I, [_VP, _VP, _I, _I, _VP, _VP, _D, _I, ctypes.POINTER(_I), _PD, _VP]),
     "sptrsv_gb300_solve_adjoint": (_I, [_VP, _VP, _I, _I, _I, _VP, _VP, _VP, _VP, _VP]),
     "sptrsv_gb300_grad_values": (_I, [_VP, _I, _I, _I, _VP, _VP, _VP, _VP]),
     "sptrsv_gb300_exec_ms": (_I, [_VP, _PD]),

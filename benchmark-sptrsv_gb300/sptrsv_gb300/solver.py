@@ -196,6 +196,30 @@ class SyncFreeSolver:
         check(st, "solve")
         return out.reshape(b.shape) if b.dim() == 1 else out
 
+    def solve_refine(self, b, values=None, *, tol: float = 1e-12, max_iter: int = 10, out=None):
+        """FP32 storage/solve + FP64-residual iterative refinement (b float64). Returns
+        (x, iterations, estimated relative forward error)."""
+        torch = _torch()
+        b2, layout = self._layout_of(b)
+        if b2.dtype != torch.float64:
+            raise TypeError("solve_refine takes float64 right-hand sides")
+        rhs = int(b2.shape[1])
+        if out is None:
+            out = (torch.empty_like(b2, memory_format=torch.contiguous_format) if layout == LAYOUT_ROW_MAJOR
+                   else torch.empty((rhs, self.n), dtype=b2.dtype, device=b2.device).t())
+        vptr = ctypes.c_void_p(0)
+        if values is not None:
+            v = values.to(self.device, torch.float64).contiguous()
+            self.values = v
+            vptr = _ptr(v)
+        it = ctypes.c_int(0)
+        est = ctypes.c_double(0.0)
+        check(self._lib.sptrsv_gb300_solve_refine(self._h, vptr, rhs, layout, _ptr(b2), _ptr(out), float(tol),
+                                                  int(max_iter), ctypes.byref(it), ctypes.byref(est),
+                                                  _stream_ptr(self._stream)), "solve_refine")
+        x = out.reshape(b.shape) if b.dim() == 1 else out
+        return x, int(it.value), float(est.value)
+
     def _layout_of(self, t):
         torch = _torch()
         t2 = t.reshape(-1, 1) if t.dim() == 1 else t

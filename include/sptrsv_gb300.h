@@ -193,6 +193,19 @@ int sptrsv_gb300_set_values(sptrsv_handle_t handle, const void *d_val, int dtype
 int sptrsv_gb300_solve(sptrsv_handle_t handle, const void *d_val, int dtype, int rhs, int layout, const void *d_b,
                        void *d_x, void *stream);
 
+/* Mixed-precision solve: values and x stored and solved in FP32 with FP32
+ * accumulation, accuracy recovered by iterative refinement in which only the
+ * residual R = B - L X (from the FP64 values) and the update X += D run in
+ * FP64. b and x are FP64 (layout as in sptrsv_gb300_solve); d_val is FP64 (or
+ * NULL for the staged FP64 values). Stops when the estimated relative forward
+ * error ||D_k||^2 / (||D_{k-1}|| ||X||) (max norms; D_0 = X_0) is at most
+ * `tol`, after at least one refinement step and at most `max_iter`; tol <= 0
+ * runs exactly max_iter steps without reading anything back (asynchronous,
+ * capturable). Returns SPTRSV_ERR_NOT_CONVERGED when tol > 0 is not met; the
+ * steps taken and the final estimate go to *iters and *est (may be NULL). */
+int sptrsv_gb300_solve_refine(sptrsv_handle_t handle, const double *d_val, int rhs, int layout, const double *d_b,
+                              double *d_x, double tol, int max_iter, int *iters, double *est, void *stream);
+
 /* Transposed (adjoint) solve op(L)^T Lambda = G on the same analysis, walked
  * in reverse dependency order (pull executor). With d_x (the forward solution
  * X, same layout) and d_dval both non-NULL, the same kernel also writes the
