@@ -450,6 +450,19 @@ cudaError_t launch_schedule_keys(const int* rows, const int* depth, int n, int s
   return cudaGetLastError();
 }
 
+__global__ void k_long_keys(const int* __restrict__ rows, const int* __restrict__ in_degree, int n, int threshold,
+                            unsigned* keys) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride)
+    keys[i] = in_degree[rows[i]] - 1 > threshold ? 0u : 1u;
+}
+cudaError_t launch_long_keys(const int* rows, const int* in_degree, int n, int threshold, unsigned* keys,
+                             cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_long_keys<<<grid_for(n), kThreads, 0, s>>>(rows, in_degree, n, threshold, keys);
+  return cudaGetLastError();
+}
+
 __global__ void k_inverse_perm(const int* __restrict__ perm, int n, int* iperm) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += stride)

@@ -1,5 +1,6 @@
 // C ABI: handles, analysis pipeline, solve dispatch, status mapping, and the
 // reference-compatible host entry point.
+#include <algorithm>
 #include <climits>
 #include <cmath>
 #include <cstdio>
@@ -18,6 +19,7 @@ namespace {
 
 int g_verbose = 0;
 int g_bench_repeat = 100;  // BENCH_REPEAT of the reference (common.h:13-15)
+constexpr int kLongDeps = 32;  // dependency lists longer than this are solved by a whole warp
 
 struct DevBuf {
   void* p = nullptr;
@@ -40,6 +42,8 @@ struct sptrsv_gb300_handle_s {
   int block_option = 0;    // 0: automatic
   long long backoff_ns = 256;
   int ctas_per_sm = 0;
+  int staged = 1;
+  int emax_option = 0;
   // analysis
   bool analysed = false;
   int n = 0, nnz = 0, substitution = 0;
@@ -58,6 +62,9 @@ struct sptrsv_gb300_handle_s {
   int* level_ptr_nat = nullptr;
   Layout layout;
   int layout_block = -1;
+  std::vector<int> dep_cnt_host;   // dependencies per position
+  std::vector<int> out_cnt_host;   // dependents per position
+  ChunkTable tab_fwd, tab_adj;
   // staged values
   Values<double> v64;
   Values<float> v32;
@@ -96,10 +103,12 @@ int map_cuda_error(cudaError_t e) {
   return SPTRSV_ERR_CUDA;
 }
 
+// Every array gets 16 spare elements so the executors' bulk copies, widened
+// to 16-byte boundaries, never read past an allocation.
 template <typename T>
 int dev_alloc(sptrsv_gb300_handle_s* h, T** p, size_t count) {
   *p = nullptr;
-  if (count == 0) count = 1;
+  count += 16;
   cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * count);
   if (e != cudaSuccess) return map_cuda_error(e);
   h->device_bytes += sizeof(T) * count;
@@ -116,6 +125,12 @@ int bits_for(long long maxval) {
   int b = 1;
   while (b < 32 && (1LL << b) <= maxval) ++b;
   return b;
+}
+
+void free_table(ChunkTable& t) {
+  if (t.start) cudaFree(t.start);
+  if (t.mode) cudaFree(t.mode);
+  t = ChunkTable();
 }
 
 void free_layout(Layout& L) {
@@ -155,6 +170,8 @@ void free_analysis(sptrsv_gb300_handle_s* h) {
   dev_free(&h->level_item);
   dev_free(&h->level_ptr_nat);
   free_layout(h->layout);
+  free_table(h->tab_fwd);
+  free_table(h->tab_adj);
   free_values(h->v64);
   free_values(h->v32);
   h->staged64 = h->staged32 = false;
@@ -223,6 +240,8 @@ int read_flags(sptrsv_gb300_handle_s* h, cudaStream_t s, int* flags) {
 // Builds the position-space layout for the given order block.
 int build_layout(sptrsv_gb300_handle_s* h, int block, cudaStream_t s) {
   free_layout(h->layout);
+  free_table(h->tab_fwd);
+  free_table(h->tab_adj);
   free_values(h->v64);
   free_values(h->v32);
   h->staged64 = h->staged32 = false;
@@ -258,9 +277,16 @@ int build_layout(sptrsv_gb300_handle_s* h, int block, cudaStream_t s) {
       CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&keys_sorted), sizeof(unsigned) * n, s));
       CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&rows_lv), sizeof(int) * n, s));
       CUDA_TRY(cudaMallocAsync(&temp, radix_sort_temp_bytes(n), s));
-      CUDA_TRY(launch_schedule_keys(rows_nat, h->depth, n, h->substitution, block, 0, keys, s));
-      CUDA_TRY(radix_sort_pairs(keys, rows_nat, keys_sorted, level_order ? L.perm : rows_lv, n,
+      // long dependency lists first inside each level (so chunks of one mode form), then
+      // level order, then (blocked orders) the natural block
+      int* rows_ls = nullptr;
+      CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&rows_ls), sizeof(int) * n, s));
+      CUDA_TRY(launch_long_keys(rows_nat, h->in_degree, n, kLongDeps, keys, s));
+      CUDA_TRY(radix_sort_pairs(keys, rows_nat, keys_sorted, rows_ls, n, 1, temp, s));
+      CUDA_TRY(launch_schedule_keys(rows_ls, h->depth, n, h->substitution, block, 0, keys, s));
+      CUDA_TRY(radix_sort_pairs(keys, rows_ls, keys_sorted, level_order ? L.perm : rows_lv, n,
                                 bits_for(h->nlevels - 1), temp, s));
+      CUDA_TRY(cudaFreeAsync(rows_ls, s));
       if (!level_order) {
         CUDA_TRY(launch_schedule_keys(rows_lv, h->depth, n, h->substitution, block, 1, keys, s));
         CUDA_TRY(radix_sort_pairs(keys, rows_lv, keys_sorted, L.perm, n, bits_for((n - 1) / block), temp, s));
@@ -280,6 +306,15 @@ int build_layout(sptrsv_gb300_handle_s* h, int block, cudaStream_t s) {
                               L.dep_pos, L.dep_src, L.dep_col, L.diag_src, s));
     CUDA_TRY(launch_fill_push(L.perm, L.iperm, h->csc_ptr, h->csc_row, L.out_ptr, n, h->substitution, L.out_pos,
                               L.out_src, s));
+    std::vector<int> ptr((size_t)n + 1);
+    CUDA_TRY(cudaMemcpyAsync(ptr.data(), L.dep_ptr, sizeof(int) * ((size_t)n + 1), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    h->dep_cnt_host.resize(n);
+    for (int p = 0; p < n; ++p) h->dep_cnt_host[p] = ptr[p + 1] - ptr[p];
+    CUDA_TRY(cudaMemcpyAsync(ptr.data(), L.out_ptr, sizeof(int) * ((size_t)n + 1), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    h->out_cnt_host.resize(n);
+    for (int p = 0; p < n; ++p) h->out_cnt_host[p] = ptr[p + 1] - ptr[p];
   }
   if (level_order) {
     L.nlevels = h->nlevels;
@@ -292,6 +327,64 @@ int build_layout(sptrsv_gb300_handle_s* h, int block, cudaStream_t s) {
   CUDA_TRY(cudaStreamSynchronize(s));
   h->layout_block = block;
   return SPTRSV_OK;
+}
+
+// Chunk table over a walk: counts[i] = dependency entries of the i-th unknown
+// walked. A chunk ends at cmax unknowns, at emax entries, or where the mode
+// changes; an unknown with more than emax entries forms a mode-2 chunk alone.
+int build_table(sptrsv_gb300_handle_s* h, ChunkTable& t, const std::vector<int>& counts, bool reversed, int cmax,
+                int emax) {
+  free_table(t);
+  const int n = static_cast<int>(counts.size());
+  auto cnt = [&](int i) { return counts[reversed ? n - 1 - i : i]; };
+  auto mode_of = [&](int c) { return c > emax ? 2 : (c > kLongDeps ? 1 : 0); };
+  std::vector<int> start, mode;
+  start.reserve(n / (cmax > 0 ? cmax : 1) + 16);
+  int i = 0;
+  while (i < n) {
+    const int m0 = mode_of(cnt(i));
+    start.push_back(i);
+    mode.push_back(m0);
+    if (m0 == 2) {
+      ++i;
+      continue;
+    }
+    long long e = 0;
+    const int first = i;
+    while (i < n && i - first < cmax) {
+      const int c = cnt(i);
+      if (mode_of(c) != m0 || e + c > emax) break;
+      e += c;
+      ++i;
+    }
+  }
+  start.push_back(n);
+  t.nchunks = static_cast<int>(mode.size());
+  t.cmax = cmax;
+  t.emax = emax;
+  CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.start), sizeof(int) * start.size()));
+  CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.mode), sizeof(int) * (mode.size() ? mode.size() : 1)));
+  CUDA_TRY(cudaMemcpy(t.start, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice));
+  if (!mode.empty()) CUDA_TRY(cudaMemcpy(t.mode, mode.data(), sizeof(int) * mode.size(), cudaMemcpyHostToDevice));
+  h->device_bytes += sizeof(int) * (start.size() + mode.size());
+  return SPTRSV_OK;
+}
+
+int ensure_table(sptrsv_gb300_handle_s* h, bool adj, int cmax, int emax) {
+  ChunkTable& t = adj ? h->tab_adj : h->tab_fwd;
+  if (t.start && t.cmax == cmax && t.emax == emax) return SPTRSV_OK;
+  return build_table(h, t, adj ? h->out_cnt_host : h->dep_cnt_host, adj, cmax, emax);
+}
+
+int auto_emax(int cmax, size_t elem) {
+  // keep one stage near 90 KB so that two buffers leave room for another CTA
+  const long long budget = 90 * 1024;
+  long long e = budget - (long long)(cmax + 32) * (long long)(8 + elem) - 64;
+  e /= (long long)(4 + elem);
+  long long want = std::max<long long>(4096, 8LL * cmax);
+  if (e > want) e = want;
+  if (e < 64) e = 64;
+  return static_cast<int>(e);
 }
 
 int effective_block(const sptrsv_gb300_handle_s* h) {
@@ -353,6 +446,8 @@ ExecConfig pick_config(const sptrsv_gb300_handle_s* h, int rhs) {
   c.block = h->block_option > 0 ? h->block_option : 256;
   c.sleep_max = static_cast<unsigned>(h->backoff_ns);
   c.ctas_per_sm = h->ctas_per_sm;
+  c.staged = h->staged;
+  c.emax = h->emax_option;
   return c;
 }
 
@@ -393,6 +488,11 @@ int solve_typed(sptrsv_gb300_handle_s* h, const Values<T>& V, int rhs, int layou
                             static_cast<unsigned*>(h->counters.p), h->ctl, c, timeout_ns(h), h->num_sms, s));
   } else if (c.sched == SCHED_LEVELSET) {
     CUDA_TRY(launch_levelset<T>(h->layout, V, rhs, v, static_cast<T*>(h->xw.p), h->ctl, c, timeout_ns(h), s));
+  } else if (rhs == 1 && c.staged) {
+    const int emax = c.emax > 0 ? c.emax : auto_emax(c.chunk, sizeof(T));
+    ST_TRY(ensure_table(h, adj != nullptr, c.chunk, emax));
+    CUDA_TRY(launch_pull_staged<T>(h->layout, V, adj ? h->tab_adj : h->tab_fwd, v, static_cast<T*>(h->xw.p), h->ctl,
+                                   c, timeout_ns(h), h->num_sms, s, adj));
   } else {
     CUDA_TRY(launch_pull<T>(h->layout, V, rhs, v, static_cast<T*>(h->xw.p), h->ctl, c, timeout_ns(h), h->num_sms,
                             s, adj));
@@ -536,6 +636,13 @@ int sptrsv_gb300_set_option(sptrsv_handle_t h, int option, long long value) {
       if (value < 0 || value > 32) return SPTRSV_ERR_INVALID;
       h->ctas_per_sm = static_cast<int>(value);
       return SPTRSV_OK;
+    case SPTRSV_OPTION_STAGED:
+      h->staged = value != 0;
+      return SPTRSV_OK;
+    case SPTRSV_OPTION_STAGE_ENTRIES:
+      if (value < 0 || value > (1 << 16)) return SPTRSV_ERR_INVALID;
+      h->emax_option = static_cast<int>(value);
+      return SPTRSV_OK;
     default:
       return SPTRSV_ERR_INVALID;
   }
@@ -556,6 +663,8 @@ int sptrsv_gb300_get_option(sptrsv_handle_t h, int option, long long* value) {
     case SPTRSV_OPTION_BLOCK: *value = h->block_option; break;
     case SPTRSV_OPTION_BACKOFF_NS: *value = h->backoff_ns; break;
     case SPTRSV_OPTION_CTAS_PER_SM: *value = h->ctas_per_sm; break;
+    case SPTRSV_OPTION_STAGED: *value = h->staged; break;
+    case SPTRSV_OPTION_STAGE_ENTRIES: *value = h->emax_option; break;
     default: return SPTRSV_ERR_INVALID;
   }
   return SPTRSV_OK;

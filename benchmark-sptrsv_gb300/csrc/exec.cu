@@ -20,6 +20,7 @@
 // that sees a failure drains to its barriers and leaves.
 #include <algorithm>
 
+#include "exec_common.cuh"
 #include "internal.h"
 
 namespace sptrsv {
@@ -95,34 +96,10 @@ __device__ __forceinline__ unsigned next_chunk(DeviceCtl* ctl, unsigned nchunks,
   return c;
 }
 
-// The last CTA to leave resets the ticket so the next launch starts at 0.
-__device__ __forceinline__ void leave(DeviceCtl* ctl) {
-  if (threadIdx.x == 0) {
-    __threadfence();
-    const unsigned d = atomicAdd(&ctl->done, 1u);
-    if (d == gridDim.x - 1) {
-      ctl->ticket = 0;
-      ctl->done = 0;
-      __threadfence();
-    }
-  }
-}
-
-// Wait until the word at p is published; returns EMPTY on timeout/failure.
-// Global words back off between polls (sleep_min..sleep_max ns); shared-memory
-// words are polled without sleeping.
 template <typename T, bool SHARED>
 __device__ __forceinline__ typename Flag<T>::Bits wait_flag(const T* p, DeviceCtl* ctl, unsigned long long timeout,
                                                             int where, unsigned sleep_min, unsigned sleep_max) {
-  using F = Flag<T>;
-  typename F::Bits bits = SHARED ? F::load_shared(p) : F::load(p);
-  if (bits != F::EMPTY) return bits;
-  WaitBudget w(timeout, SHARED ? 0u : sleep_min, SHARED ? 0u : sleep_max);
-  do {
-    if (!w.poll(ctl, where)) return F::EMPTY;
-    bits = SHARED ? F::load_shared(p) : F::load(p);
-  } while (bits == F::EMPTY);
-  return bits;
+  return wait_flag_dev<T, SHARED>(p, ctl, timeout, where, sleep_min, sleep_max);
 }
 
 // ------------------------------------------------------------------ pull, one rhs

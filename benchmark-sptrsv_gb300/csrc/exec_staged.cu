@@ -1,0 +1,442 @@
+// Pull executor with TMA-staged chunks (one right-hand side).
+//
+// Work unit: a chunk of consecutive positions from a precomputed chunk table
+// (bounded position count C and dependency count E, one processing mode per
+// chunk). A persistent CTA double-buffers its chunks: while it solves chunk k
+// from shared memory, the bulk-copy engine (cp.async.bulk, 1-D TMA, completion
+// on an mbarrier) streams chunk k+1's slices of the position-space layout --
+// dependency pointers, rows, 1/diag, dependency positions and scaled values --
+// into the other buffer. The only global traffic left on the dependency path
+// is the gather of published x values (value-as-flag words, relaxed loads)
+// and b.
+//
+// Modes: 0 = one thread per unknown (short dependency lists), 1 = one warp per
+// unknown with lanes over its dependencies (long lists), 2 = one warp per
+// unknown reading its list straight from global memory (lists longer than a
+// stage buffer).
+//
+// ADJ solves the transposed system on the same analysis: the chunk table is
+// built over reversed positions and the dependency lists are the push lists.
+#include "exec_common.cuh"
+#include "internal.h"
+
+namespace sptrsv {
+
+namespace {
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// Copies elements [a, b) of src into dst (16-byte aligned smem) through the
+// bulk-copy engine; returns the element offset of `a` inside dst and adds the
+// byte count to *tx. The source range is widened to 16-byte boundaries (the
+// layout arrays are padded so the widened range stays in bounds).
+template <typename E>
+__device__ __forceinline__ int stage_slice(E* dst, const E* src, long long a, long long b, unsigned long long* bar,
+                                           unsigned* tx) {
+  constexpr long long per16 = 16 / sizeof(E);
+  const long long a16 = a & ~(per16 - 1);
+  const long long b16 = (b + per16 - 1) & ~(per16 - 1);
+  const unsigned bytes = static_cast<unsigned>((b16 - a16) * (long long)sizeof(E));
+  if (bytes) {
+    bulk_g2s(dst, src + a16, bytes, bar);
+    *tx += bytes;
+  }
+  return static_cast<int>(a - a16);
+}
+
+template <typename T>
+struct StagedArgs {
+  int n, nchunks, cmax, emax, smem_tier;
+  const int* tab_start;   // [nchunks+1] first original position of each chunk (in walk order)
+  const int* tab_mode;    // [nchunks]
+  const int* perm;
+  const int* lptr;        // dependency pointers (pull lists, or push lists for ADJ)
+  const int* lpos;
+  const T* lval;          // scaled values (or unscaled with EXACT)
+  const T* dscale;        // 1/diag (or diag with EXACT)
+  const T* b;
+  T* x;
+  long long b_si, x_si;
+  T* xw;
+  DeviceCtl* ctl;
+  unsigned long long timeout_ns;
+  unsigned sleep_min, sleep_max;
+  // fused gradient (ADJ only)
+  T* grad;
+  const T* xf;
+  long long xf_si;
+  const int* dep_ptr;
+  const int* dep_src;
+  const int* dep_col;
+  const int* diag_src;
+};
+
+struct StageInfo {
+  int chunk;    // chunk id (>= nchunks: none)
+  int lo, hi;   // original positions [lo, hi)
+  int ebase;    // lptr[lo]
+  int off_ptr, off_perm, off_sc, off_pos, off_val;  // element offsets inside the staged slices
+  int mode;
+};
+
+template <typename T>
+struct StageBufs {
+  int* ptr;
+  int* perm;
+  T* sc;
+  int* pos;
+  T* val;
+};
+
+// Shared-memory carve-up for one stage (all regions 16-byte aligned).
+template <typename T>
+__host__ __device__ inline size_t stage_bytes(int cmax, int emax) {
+  auto up = [](size_t v) { return (v + 15) & ~(size_t)15; };
+  return up(sizeof(int) * (size_t)(cmax + 1 + 8)) + up(sizeof(int) * (size_t)(cmax + 8)) +
+         up(sizeof(T) * (size_t)(cmax + 8)) + up(sizeof(int) * (size_t)(emax + 8)) + up(sizeof(T) * (size_t)(emax + 8));
+}
+template <typename T>
+__device__ inline StageBufs<T> carve(unsigned char* base, int cmax, int emax) {
+  auto up = [](size_t v) { return (v + 15) & ~(size_t)15; };
+  StageBufs<T> s;
+  size_t o = 0;
+  s.ptr = reinterpret_cast<int*>(base + o);
+  o += up(sizeof(int) * (size_t)(cmax + 1 + 8));
+  s.perm = reinterpret_cast<int*>(base + o);
+  o += up(sizeof(int) * (size_t)(cmax + 8));
+  s.sc = reinterpret_cast<T*>(base + o);
+  o += up(sizeof(T) * (size_t)(cmax + 8));
+  s.pos = reinterpret_cast<int*>(base + o);
+  o += up(sizeof(int) * (size_t)(emax + 8));
+  s.val = reinterpret_cast<T*>(base + o);
+  return s;
+}
+
+// Thread 0: claim a chunk and start streaming its slices into stage buffer `sb`.
+template <typename T, bool ADJ>
+__device__ void issue_stage(const StagedArgs<T>& a, StageBufs<T> sb, unsigned long long* bar, StageInfo* info) {
+  const unsigned c = ctl_failed(a.ctl) ? (unsigned)a.nchunks : atomicAdd(&a.ctl->ticket, 1u);
+  info->chunk = static_cast<int>(c);
+  if (c >= (unsigned)a.nchunks) return;
+  const int s0 = a.tab_start[c], s1 = a.tab_start[c + 1];
+  // walk order s0..s1-1; in ADJ the walk runs over reversed positions
+  const int lo = ADJ ? a.n - s1 : s0;
+  const int hi = ADJ ? a.n - s0 : s1;
+  const int mode = a.tab_mode[c];
+  const int e0 = a.lptr[lo], e1 = a.lptr[hi];
+  info->lo = lo;
+  info->hi = hi;
+  info->ebase = e0;
+  info->mode = mode;
+  unsigned tx = 0;
+  fence_proxy_async_smem();
+  // expect_tx must precede the copies' completion: arm with the byte count
+  // computed up front (the widened sizes are deterministic).
+  auto wide = [](long long a_, long long b_, long long per16) {
+    return ((b_ + per16 - 1) & ~(per16 - 1)) - (a_ & ~(per16 - 1));
+  };
+  unsigned expect = 0;
+  expect += (unsigned)(wide(lo, hi + 1, 4) * 4);
+  expect += (unsigned)(wide(lo, hi, 4) * 4);
+  expect += (unsigned)(wide(lo, hi, 16 / sizeof(T)) * sizeof(T));
+  if (mode != 2) {
+    expect += (unsigned)(wide(e0, e1, 4) * 4);
+    expect += (unsigned)(wide(e0, e1, 16 / sizeof(T)) * sizeof(T));
+  }
+  mbar_arrive_expect_tx(bar, expect);
+  info->off_ptr = stage_slice<int>(sb.ptr, a.lptr, lo, hi + 1, bar, &tx);
+  info->off_perm = stage_slice<int>(sb.perm, a.perm, lo, hi, bar, &tx);
+  info->off_sc = stage_slice<T>(sb.sc, a.dscale, lo, hi, bar, &tx);
+  if (mode != 2) {
+    info->off_pos = stage_slice<int>(sb.pos, a.lpos, e0, e1, bar, &tx);
+    info->off_val = stage_slice<T>(sb.val, a.lval, e0, e1, bar, &tx);
+  } else {
+    info->off_pos = info->off_val = 0;
+  }
+}
+
+template <typename T, bool EXACT, bool ADJ>
+__global__ void __launch_bounds__(256) k_pull_staged(StagedArgs<T> a) {
+  using F = Flag<T>;
+  using Bits = typename F::Bits;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ unsigned long long s_bar[2];
+  __shared__ StageInfo s_info[2];
+  __shared__ int s_fail;
+  const size_t sbytes = stage_bytes<T>(a.cmax, a.emax);
+  StageBufs<T> bufs[2] = {carve<T>(smem_raw, a.cmax, a.emax), carve<T>(smem_raw + sbytes, a.cmax, a.emax)};
+  T* s_x = reinterpret_cast<T*>(smem_raw + 2 * sbytes);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  if (threadIdx.x == 0) {
+    mbar_init(&s_bar[0], 1);
+    mbar_init(&s_bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    s_fail = 0;
+    issue_stage<T, ADJ>(a, bufs[0], &s_bar[0], &s_info[0]);
+  }
+  __syncthreads();
+  unsigned parity[2] = {0u, 0u};
+  int st = 0;
+  for (;;) {
+    const StageInfo info = s_info[st];
+    if (info.chunk >= a.nchunks) break;
+    // Prefetch the next chunk into the other buffer (its previous contents were
+    // consumed before the barrier that ended the last iteration).
+    if (threadIdx.x == 0) issue_stage<T, ADJ>(a, bufs[st ^ 1], &s_bar[st ^ 1], &s_info[st ^ 1]);
+    // Wait for this chunk's slices (bounded).
+    if (!mbar_test(&s_bar[st], parity[st])) {
+      WaitBudget w(a.timeout_ns);
+      while (!mbar_test(&s_bar[st], parity[st])) {
+        if (!w.poll(a.ctl, info.lo)) { s_fail = 1; break; }
+      }
+    }
+    parity[st] ^= 1u;
+    const int len = info.hi - info.lo;
+    if (a.smem_tier)
+      for (int i = threadIdx.x; i < len; i += blockDim.x) *reinterpret_cast<Bits*>(&s_x[i]) = F::EMPTY;
+    __syncthreads();
+    bool fail = s_fail != 0;
+    const StageBufs<T> sb = bufs[st];
+    const int* sptr = sb.ptr + info.off_ptr;
+    const int* sperm = sb.perm + info.off_perm;
+    const T* ssc = sb.sc + info.off_sc;
+    const int* spos = sb.pos + info.off_pos;
+    const T* sval = sb.val + info.off_val;
+    const int lo = info.lo, hi = info.hi;
+    // position p (original) -> local index li = p - lo; walk index i -> p
+    auto pos_of = [&](int i) { return ADJ ? hi - 1 - i : lo + i; };
+    auto is_local = [&](int q) { return ADJ ? (q < hi) : (q >= lo); };
+    if (!fail && (EXACT || info.mode == 0)) {
+      constexpr int U = 8;
+      const bool from_smem = info.mode != 2;
+      const int* vpos = from_smem ? spos : a.lpos;
+      const T* vval = from_smem ? sval : a.lval;
+      for (int i = threadIdx.x; i < len && !fail; i += blockDim.x) {
+        const int p = pos_of(i);
+        const int li = p - lo;
+        const int row = sperm[li];
+        const int ea = from_smem ? sptr[li] - info.ebase : sptr[li];
+        const int eb = from_smem ? sptr[li + 1] - info.ebase : sptr[li + 1];
+        const T bi = a.b[(long long)row * a.b_si];
+        const T sc = ssc[li];
+        T acc = EXACT ? T(0) : bi * sc;
+        for (int e = ea; e < eb && !fail; e += U) {
+          int q[U];
+          T w[U];
+          Bits bits[U];
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            q[u] = e + u < eb ? vpos[e + u] : -1;
+            w[u] = e + u < eb ? vval[e + u] : T(0);
+          }
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            bits[u] = F::EMPTY;
+            if (q[u] >= 0) bits[u] = (a.smem_tier && is_local(q[u])) ? F::load_shared(&s_x[q[u] - lo]) : F::load(&a.xw[q[u]]);
+          }
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            if (q[u] < 0 || fail) continue;
+            if (bits[u] == F::EMPTY) {
+              bits[u] = (a.smem_tier && is_local(q[u]))
+                            ? wait_flag_dev<T, true>(&s_x[q[u] - lo], a.ctl, a.timeout_ns, p, 0, 0)
+                            : wait_flag_dev<T, false>(&a.xw[q[u]], a.ctl, a.timeout_ns, p, a.sleep_min, a.sleep_max);
+              if (bits[u] == F::EMPTY) { fail = true; continue; }
+            }
+            acc = EXACT ? exact_mul_add<T>(acc, w[u], F::value(bits[u])) : fma(-w[u], F::value(bits[u]), acc);
+          }
+        }
+        if (fail) break;
+        const T xi = EXACT ? exact_finish<T>(bi, acc, sc) : acc;
+        if (a.smem_tier) F::store_shared(&s_x[li], xi);
+        F::store(&a.xw[p], xi);
+        a.x[(long long)row * a.x_si] = xi;
+        if (ADJ && a.grad) {
+          for (int e = a.dep_ptr[p]; e < a.dep_ptr[p + 1]; ++e)
+            a.grad[a.dep_src[e]] = -xi * a.xf[(long long)a.dep_col[e] * a.xf_si];
+          a.grad[a.diag_src[p]] = -xi * a.xf[(long long)row * a.xf_si];
+        }
+      }
+    } else if (!fail) {
+      // one warp per unknown; lanes over its dependency list
+      constexpr int U = 2;
+      const bool from_smem = info.mode == 1;
+      for (int i = warp; i < len && !fail; i += nwarps) {
+        const int p = pos_of(i);
+        const int li = p - lo;
+        const int row = sperm[li];
+        const int ea = from_smem ? sptr[li] - info.ebase : sptr[li];
+        const int eb = from_smem ? sptr[li + 1] - info.ebase : sptr[li + 1];
+        const int* vpos = from_smem ? spos : a.lpos;
+        const T* vval = from_smem ? sval : a.lval;
+        const T bi = a.b[(long long)row * a.b_si];
+        const T sc = ssc[li];
+        T acc = (lane == 0 && !EXACT) ? bi * sc : T(0);
+        for (int e = ea + lane; e < eb && !fail; e += 32 * U) {
+          int q[U];
+          T w[U];
+          Bits bits[U];
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            const int ee = e + u * 32;
+            q[u] = ee < eb ? vpos[ee] : -1;
+            w[u] = ee < eb ? vval[ee] : T(0);
+          }
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            bits[u] = F::EMPTY;
+            if (q[u] >= 0) bits[u] = (a.smem_tier && is_local(q[u])) ? F::load_shared(&s_x[q[u] - lo]) : F::load(&a.xw[q[u]]);
+          }
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            if (q[u] < 0 || fail) continue;
+            if (bits[u] == F::EMPTY) {
+              bits[u] = (a.smem_tier && is_local(q[u]))
+                            ? wait_flag_dev<T, true>(&s_x[q[u] - lo], a.ctl, a.timeout_ns, p, 0, 0)
+                            : wait_flag_dev<T, false>(&a.xw[q[u]], a.ctl, a.timeout_ns, p, a.sleep_min, a.sleep_max);
+              if (bits[u] == F::EMPTY) { fail = true; continue; }
+            }
+            acc = fma(-w[u], F::value(bits[u]), acc);
+          }
+        }
+        fail = __any_sync(0xffffffffu, fail);
+        if (fail) break;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        const T xi = acc;
+        if (lane == 0) {
+          if (a.smem_tier) F::store_shared(&s_x[li], xi);
+          F::store(&a.xw[p], xi);
+          a.x[(long long)row * a.x_si] = xi;
+        }
+        if (ADJ && a.grad) {
+          for (int e = a.dep_ptr[p] + lane; e < a.dep_ptr[p + 1]; e += 32)
+            a.grad[a.dep_src[e]] = -xi * a.xf[(long long)a.dep_col[e] * a.xf_si];
+          if (lane == 0) a.grad[a.diag_src[p]] = -xi * a.xf[(long long)row * a.xf_si];
+        }
+      }
+    }
+    if (__syncthreads_or(fail)) {
+      // Let the prefetch already in flight land before the CTA leaves.
+      if (threadIdx.x == 0 && s_info[st ^ 1].chunk < a.nchunks) {
+        WaitBudget w(a.timeout_ns);
+        while (!mbar_test(&s_bar[st ^ 1], parity[st ^ 1])) {
+          if (!w.poll(a.ctl, -1)) break;
+        }
+      }
+      break;
+    }
+    st ^= 1;
+  }
+  __syncthreads();
+  leave(a.ctl);
+}
+
+template <typename T, bool EXACT, bool ADJ>
+cudaError_t run_staged(const StagedArgs<T>& a, int block, int ctas_per_sm, int num_sms, cudaStream_t s) {
+  const size_t smem = 2 * stage_bytes<T>(a.cmax, a.emax) + (a.smem_tier ? sizeof(T) * (size_t)a.cmax : 0);
+  auto kernel = k_pull_staged<T, EXACT, ADJ>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  if (ctas_per_sm > 0 && per_sm > ctas_per_sm) per_sm = ctas_per_sm;
+  long long grid = (long long)num_sms * per_sm;
+  if (grid > a.nchunks) grid = a.nchunks;
+  if (grid < 1) grid = 1;
+  kernel<<<(int)grid, block, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t staged_smem_bytes(int cmax, int emax, size_t elem, bool smem_tier) {
+  return 2 * (elem == 8 ? stage_bytes<double>(cmax, emax) : stage_bytes<float>(cmax, emax)) +
+         (smem_tier ? elem * (size_t)cmax : 0);
+}
+
+template <typename T>
+cudaError_t launch_pull_staged(const Layout& L, const Values<T>& V, const ChunkTable& tab, const VecView<T>& v, T* xw,
+                               DeviceCtl* ctl, const ExecConfig& cfg, unsigned long long timeout_ns, int num_sms,
+                               cudaStream_t s, const AdjointArgs<T>* adj) {
+  if (L.n == 0) return cudaSuccess;
+  StagedArgs<T> a{};
+  a.n = L.n;
+  a.nchunks = tab.nchunks;
+  a.cmax = tab.cmax;
+  a.emax = tab.emax;
+  a.smem_tier = cfg.smem_tier;
+  a.tab_start = tab.start;
+  a.tab_mode = tab.mode;
+  a.perm = L.perm;
+  const bool is_adj = adj != nullptr;
+  a.lptr = is_adj ? L.out_ptr : L.dep_ptr;
+  a.lpos = is_adj ? L.out_pos : L.dep_pos;
+  a.lval = is_adj ? (cfg.exact ? V.out_val : V.out_w) : (cfg.exact ? V.dep_val : V.dep_w);
+  a.dscale = cfg.exact ? V.diag : V.rcp;
+  a.b = v.b;
+  a.x = v.x;
+  a.b_si = v.b_si;
+  a.x_si = v.x_si;
+  a.xw = xw;
+  a.ctl = ctl;
+  a.timeout_ns = timeout_ns;
+  a.sleep_min = cfg.sleep_max ? 16u : 0u;
+  a.sleep_max = cfg.sleep_max;
+  if (is_adj) {
+    a.grad = adj->grad;
+    a.xf = adj->xf;
+    a.xf_si = adj->xf_si;
+    a.dep_ptr = L.dep_ptr;
+    a.dep_src = L.dep_src;
+    a.dep_col = L.dep_col;
+    a.diag_src = L.diag_src;
+  }
+  const int block = cfg.block;
+  if (cfg.exact) {
+    return is_adj ? run_staged<T, true, true>(a, block, cfg.ctas_per_sm, num_sms, s)
+                  : run_staged<T, true, false>(a, block, cfg.ctas_per_sm, num_sms, s);
+  }
+  return is_adj ? run_staged<T, false, true>(a, block, cfg.ctas_per_sm, num_sms, s)
+                : run_staged<T, false, false>(a, block, cfg.ctas_per_sm, num_sms, s);
+}
+
+template cudaError_t launch_pull_staged<double>(const Layout&, const Values<double>&, const ChunkTable&,
+                                                const VecView<double>&, double*, DeviceCtl*, const ExecConfig&,
+                                                unsigned long long, int, cudaStream_t, const AdjointArgs<double>*);
+template cudaError_t launch_pull_staged<float>(const Layout&, const Values<float>&, const ChunkTable&,
+                                               const VecView<float>&, float*, DeviceCtl*, const ExecConfig&,
+                                               unsigned long long, int, cudaStream_t, const AdjointArgs<float>*);
+
+}  // namespace sptrsv

@@ -32,6 +32,19 @@ struct ExecConfig {
   int block = 256;        // threads per CTA (64, 128 or 256)
   int ctas_per_sm = 0;    // resident CTAs per SM (0: as many as fit)
   unsigned sleep_max = 0; // backoff cap of global polls in ns (0: spin)
+  int staged = 1;         // one right-hand side: TMA-staged chunk executor
+  int emax = 0;           // staged: dependency entries per chunk (0: automatic)
+};
+
+// Work units of the staged executor: chunk k covers walk indices
+// [start[k], start[k+1]) (positions for a forward walk, reversed positions for
+// the adjoint walk), holds at most cmax unknowns and emax dependency entries,
+// and is processed in one mode (0 thread per unknown, 1 warp per unknown,
+// 2 warp per unknown reading its list from global memory).
+struct ChunkTable {
+  int nchunks = 0, cmax = 0, emax = 0;
+  int* start = nullptr;   // device [nchunks+1]
+  int* mode = nullptr;    // device [nchunks]
 };
 
 // Solve-time description of one right-hand-side block. Element (i, k) of b
@@ -99,6 +112,9 @@ cudaError_t launch_levels(const int* col_ptr, const int* row_idx, const int* in_
 cudaError_t launch_schedule_keys(const int* rows, const int* depth, int n, int substitution, int block,
                                  int mode, unsigned* keys, cudaStream_t s);
 cudaError_t launch_inverse_perm(const int* perm, int n, int* iperm, cudaStream_t s);
+// key = 0 for rows with more than `threshold` dependencies, 1 otherwise
+cudaError_t launch_long_keys(const int* rows, const int* in_degree, int n, int threshold, unsigned* keys,
+                             cudaStream_t s);
 cudaError_t launch_dep_counts(const int* perm, const int* in_degree, int n, int* counts, cudaStream_t s);
 cudaError_t launch_out_counts(const int* perm, const int* col_ptr, int n, int* counts, cudaStream_t s);
 cudaError_t launch_fill_pull(const int* perm, const int* iperm, const int* csr_ptr, const int* csr_col,
@@ -131,6 +147,11 @@ cudaError_t launch_levelset(const Layout& L, const Values<T>& V, int rhs, const 
                             DeviceCtl* ctl, const ExecConfig& cfg, unsigned long long timeout_ns,
                             cudaStream_t s);
 size_t pull_smem_bytes(int chunk, int rhs, size_t elem);
+size_t staged_smem_bytes(int cmax, int emax, size_t elem, bool smem_tier);
+template <typename T>
+cudaError_t launch_pull_staged(const Layout& L, const Values<T>& V, const ChunkTable& tab, const VecView<T>& v, T* xw,
+                               DeviceCtl* ctl, const ExecConfig& cfg, unsigned long long timeout_ns, int num_sms,
+                               cudaStream_t s, const AdjointArgs<T>* adj);
 
 template <typename T>
 cudaError_t launch_grad_values(const int* csc_row, const int* csc_col, int nnz, int rhs, const T* lambda,

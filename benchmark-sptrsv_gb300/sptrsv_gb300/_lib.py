@@ -53,6 +53,8 @@ OPTION_PROFILE = 8
 OPTION_BLOCK = 9
 OPTION_BACKOFF_NS = 10
 OPTION_CTAS_PER_SM = 11
+OPTION_STAGED = 12
+OPTION_STAGE_ENTRIES = 13
 
 
 class SptrsvError(RuntimeError):

@@ -87,7 +87,10 @@ typedef enum sptrsv_option {
                                      (read with sptrsv_gb300_exec_ms) */
   SPTRSV_OPTION_BLOCK = 9,        /* threads per CTA of the sync-free executors: 64, 128, 256 (0 = auto) */
   SPTRSV_OPTION_BACKOFF_NS = 10,  /* cap of the sleep between two polls of a global flag (0 = spin) */
-  SPTRSV_OPTION_CTAS_PER_SM = 11  /* resident CTAs per SM of the executors (0 = as many as fit) */
+  SPTRSV_OPTION_CTAS_PER_SM = 11, /* resident CTAs per SM of the executors (0 = as many as fit) */
+  SPTRSV_OPTION_STAGED = 12,      /* 1 (default): one-rhs pull solves stream each chunk's layout slices
+                                     into shared memory with bulk copies (TMA), double-buffered */
+  SPTRSV_OPTION_STAGE_ENTRIES = 13 /* staged executor: dependency entries per chunk buffer (0 = auto) */
 } sptrsv_option;
 
 typedef struct sptrsv_info {

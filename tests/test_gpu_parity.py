@@ -45,6 +45,11 @@ CONFIGS = [
     dict(schedule=2, lanes=2, order_block=1),
     dict(schedule=2, lanes=8, order_block=10**9, chunk=64),
     dict(schedule=2, lanes=32, smem_tier=False),
+    dict(schedule=2, staged=False, lanes=1),
+    dict(schedule=2, staged=False, lanes=4, order_block=10**9),
+    dict(schedule=2, chunk=32, stage_entries=64),
+    dict(schedule=2, chunk=7, stage_entries=16, order_block=10**9, smem_tier=False),
+    dict(schedule=2, chunk=4096, block=64, ctas_per_sm=1, backoff_ns=0),
     dict(schedule=3, lanes=1),
     dict(schedule=3, lanes=8),
 ]
@@ -63,10 +68,12 @@ def test_fp64_matches_oracle(cuda, name, cfg):
 
 
 @pytest.mark.parametrize("name", golden_names())
-@pytest.mark.parametrize("order_block", [1, 256, 10**9])
-def test_exact_pull_is_bit_identical(cuda, name, order_block):
+@pytest.mark.parametrize("order_block,staged,entries", [(1, True, 0), (256, True, 0), (10**9, True, 0),
+                                                        (256, False, 0), (10**9, True, 16)])
+def test_exact_pull_is_bit_identical(cuda, name, order_block, staged, entries):
     g = load_golden(name)
-    s = make_solver(cuda, g, schedule=2, exact=True, order_block=order_block)
+    s = make_solver(cuda, g, schedule=2, exact=True, order_block=order_block, staged=staged,
+                    stage_entries=entries, chunk=64 if entries else 0)
     x = s.solve(b_tensor(cuda, g)).cpu().numpy().ravel()
     assert np.array_equal(x.view(np.uint64), g["x64"].view(np.uint64))
     x32 = s.solve(b_tensor(cuda, g, np.float32)).cpu().numpy().ravel()

@@ -42,7 +42,8 @@ def test_refine_column_major_1m_like(cuda, oracle_port, rhs):
     s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, values=m.val)
     b_cm = cuda.from_numpy(np.ascontiguousarray(B.T)).cuda().t()
     x, iters, est = s.solve_refine(b_cm)
-    assert x.stride() == (1, m.n)
+    if rhs > 1:
+        assert x.stride() == (1, m.n)
     assert relerr(x.cpu().numpy(), ref) <= TOL_FWD
     # fixed-step mode (no read-back) gives the same answer after the same number of steps
     x2, it2, _ = s.solve_refine(b_cm, tol=0.0, max_iter=iters)
