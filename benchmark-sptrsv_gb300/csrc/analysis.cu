@@ -19,6 +19,10 @@ inline int grid_for(long long count, int threads = kThreads, int cap = 1 << 20) 
 }
 }  // namespace
 
+__device__ __forceinline__ int dir_of(const SysDesc& d, long long c) {
+  return d.dir ? static_cast<int>(d.dir[c]) : d.substitution;
+}
+
 // ------------------------------------------------------------ validation
 __global__ void k_validate_ptr(const int* __restrict__ col_ptr, int n, int nnz, int* flags) {
   const long long stride = (long long)gridDim.x * blockDim.x;
@@ -34,9 +38,10 @@ __global__ void k_validate_ptr(const int* __restrict__ col_ptr, int n, int nnz, 
 
 // One thread per column. Requires monotone, in-range column pointers.
 __global__ void k_validate_rows(const int* __restrict__ col_ptr, const int* __restrict__ row_idx, int n,
-                                int substitution, int* flags) {
+                                SysDesc sd, int* flags) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += stride) {
+    const int substitution = dir_of(sd, c);
     const int beg = col_ptr[c], end = col_ptr[c + 1];
     int f = 0;
     if (beg == end) {
@@ -67,10 +72,86 @@ cudaError_t launch_validate_ptr(const int* col_ptr, int n, int nnz, int* flags, 
   k_validate_ptr<<<grid_for((long long)n + 1), kThreads, 0, s>>>(col_ptr, n, nnz, flags);
   return cudaGetLastError();
 }
-cudaError_t launch_validate_rows(const int* col_ptr, const int* row_idx, int n, int substitution,
-                                 int* flags, cudaStream_t s) {
+cudaError_t launch_validate_rows(const int* col_ptr, const int* row_idx, int n, const SysDesc& sd, int* flags,
+                                 cudaStream_t s) {
   if (n == 0) return cudaSuccess;
-  k_validate_rows<<<grid_for(n), kThreads, 0, s>>>(col_ptr, row_idx, n, substitution, flags);
+  k_validate_rows<<<grid_for(n), kThreads, 0, s>>>(col_ptr, row_idx, n, sd, flags);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ batches
+__device__ __forceinline__ int upper_bound_sys(const int* off, int count, long long v) {
+  // largest s with off[s] <= v
+  int lo = 0, hi = count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= v) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void k_batch_cols(const int* __restrict__ col_ptr_cat, int count, const int* __restrict__ sys_off,
+                             const int* __restrict__ sys_eoff, const int* __restrict__ sys_sub, int n, int nnz,
+                             int* col_ptr, unsigned char* dir, int* sys_of, int* flags) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  if (blockIdx.x == 0 && threadIdx.x == 0) col_ptr[n] = nnz;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += stride) {
+    const int sy = upper_bound_sys(sys_off, count, c);
+    const long long local = c - sys_off[sy];
+    const int len = (sy + 1 < count ? sys_off[sy + 1] : n) - sys_off[sy];
+    const int* cp = col_ptr_cat + sys_off[sy] + sy;
+    const int enz = (sy + 1 < count ? sys_eoff[sy + 1] : nnz) - sys_eoff[sy];
+    if (local == 0 && (cp[0] != 0 || cp[len] != enz)) atomicOr(flags, SF_BAD_PTR);
+    col_ptr[c] = sys_eoff[sy] + cp[local];
+    dir[c] = static_cast<unsigned char>(sys_sub[sy]);
+    sys_of[c] = sy;
+  }
+}
+__global__ void k_batch_rows(const int* __restrict__ row_idx_cat, int count, const int* __restrict__ sys_off,
+                             const int* __restrict__ sys_eoff, int n, int nnz, int* row_idx, int* flags) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nnz; e += stride) {
+    const int sy = upper_bound_sys(sys_eoff, count, e);
+    const int local = row_idx_cat[e];
+    const int len = (sy + 1 < count ? sys_off[sy + 1] : n) - sys_off[sy];
+    if (local < 0 || local >= len) atomicOr(flags, SF_ROW_RANGE);
+    row_idx[e] = sys_off[sy] + local;
+  }
+}
+cudaError_t launch_batch_merge(const int* col_ptr_cat, const int* row_idx_cat, int count, const int* sys_off,
+                               const int* sys_eoff, const int* sys_sub, int n, int nnz, int* col_ptr, int* row_idx,
+                               unsigned char* dir, int* sys_of, int* flags, cudaStream_t s) {
+  k_batch_cols<<<grid_for(n > 0 ? n : 1), kThreads, 0, s>>>(col_ptr_cat, count, sys_off, sys_eoff, sys_sub, n, nnz,
+                                                            col_ptr, dir, sys_of, flags);
+  if (nnz > 0)
+    k_batch_rows<<<grid_for(nnz), kThreads, 0, s>>>(row_idx_cat, count, sys_off, sys_eoff, n, nnz, row_idx, flags);
+  return cudaGetLastError();
+}
+
+__device__ __forceinline__ void nat_of(const SysDesc& sd, int n, long long r, long long* off, long long* nat) {
+  if (!sd.sys_of) {
+    *off = 0;
+    *nat = sd.substitution == 0 ? r : n - 1 - r;
+    return;
+  }
+  const int sy = sd.sys_of[r];
+  *off = sd.sys_off[sy];
+  const long long local = r - *off;
+  *nat = sd.dir[r] == 0 ? local : sd.sys_n[sy] - 1 - local;
+}
+
+__global__ void k_nat_rows(SysDesc sd, int n, int* rows_nat) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n; r += stride) {
+    long long off, nat;
+    nat_of(sd, n, r, &off, &nat);
+    rows_nat[off + nat] = static_cast<int>(r);
+  }
+}
+cudaError_t launch_nat_rows(const SysDesc& sd, int n, int* rows_nat, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_nat_rows<<<grid_for(n), kThreads, 0, s>>>(sd, n, rows_nat);
   return cudaGetLastError();
 }
 
@@ -430,23 +511,28 @@ cudaError_t launch_levels(const int* col_ptr, const int* row_idx, const int* in_
 // ------------------------------------------------------------ schedule
 // mode 0: key = depth (level order); mode 1: key = natural position / block
 // (second, stable pass of the blocked level order).
-__global__ void k_schedule_keys(const int* __restrict__ rows, const int* __restrict__ depth, int n,
-                                int substitution, int block, int mode, unsigned* keys) {
+// mode 0: key = depth (level order); mode 1: key = (natural position inside its
+// system / block) * count + system (second, stable pass of the blocked level
+// order; batches interleave their systems block by block).
+__global__ void k_schedule_keys(const int* __restrict__ rows, const int* __restrict__ depth, int n, SysDesc sd,
+                                int block, int mode, unsigned* keys) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
     const int r = rows[i];
     if (mode == 0) {
       keys[i] = static_cast<unsigned>(depth[r]);
     } else {
-      const int nat = substitution == 0 ? r : n - 1 - r;
-      keys[i] = static_cast<unsigned>(nat / block);
+      long long off, nat;
+      nat_of(sd, n, r, &off, &nat);
+      const long long sy = sd.sys_of ? sd.sys_of[r] : 0;
+      keys[i] = static_cast<unsigned>((nat / block) * sd.count + sy);
     }
   }
 }
-cudaError_t launch_schedule_keys(const int* rows, const int* depth, int n, int substitution, int block, int mode,
+cudaError_t launch_schedule_keys(const int* rows, const int* depth, int n, const SysDesc& sd, int block, int mode,
                                  unsigned* keys, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  k_schedule_keys<<<grid_for(n), kThreads, 0, s>>>(rows, depth, n, substitution, block, mode, keys);
+  k_schedule_keys<<<grid_for(n), kThreads, 0, s>>>(rows, depth, n, sd, block, mode, keys);
   return cudaGetLastError();
 }
 
@@ -504,10 +590,11 @@ cudaError_t launch_out_counts(const int* perm, const int* col_ptr, int n, int* c
 __global__ void k_fill_pull(const int* __restrict__ perm, const int* __restrict__ iperm,
                             const int* __restrict__ csr_ptr, const int* __restrict__ csr_col,
                             const int* __restrict__ csr_src, const int* __restrict__ dep_ptr, int n,
-                            int substitution, int* dep_pos, int* dep_src, int* dep_col, int* diag_src) {
+                            SysDesc sd, int* dep_pos, int* dep_src, int* dep_col, int* diag_src) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += stride) {
     const int r = perm[p];
+    const int substitution = dir_of(sd, r);
     const int beg = csr_ptr[r], end = csr_ptr[r + 1];
     int out = dep_ptr[p];
     if (substitution == 0) {
@@ -528,10 +615,10 @@ __global__ void k_fill_pull(const int* __restrict__ perm, const int* __restrict_
   }
 }
 cudaError_t launch_fill_pull(const int* perm, const int* iperm, const int* csr_ptr, const int* csr_col,
-                             const int* csr_src, const int* dep_ptr, int n, int substitution, int* dep_pos,
+                             const int* csr_src, const int* dep_ptr, int n, const SysDesc& sd, int* dep_pos,
                              int* dep_src, int* dep_col, int* diag_src, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  k_fill_pull<<<grid_for(n), kThreads, 0, s>>>(perm, iperm, csr_ptr, csr_col, csr_src, dep_ptr, n, substitution,
+  k_fill_pull<<<grid_for(n), kThreads, 0, s>>>(perm, iperm, csr_ptr, csr_col, csr_src, dep_ptr, n, sd,
                                                 dep_pos, dep_src, dep_col, diag_src);
   return cudaGetLastError();
 }
@@ -542,10 +629,11 @@ cudaError_t launch_fill_pull(const int* perm, const int* iperm, const int* csr_p
 // upper one. The push executor is order-agnostic; the adjoint solve relies on it.
 __global__ void k_fill_push(const int* __restrict__ perm, const int* __restrict__ iperm,
                             const int* __restrict__ col_ptr, const int* __restrict__ row_idx,
-                            const int* __restrict__ out_ptr, int n, int substitution, int* out_pos, int* out_src) {
+                            const int* __restrict__ out_ptr, int n, SysDesc sd, int* out_pos, int* out_src) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += stride) {
     const int c = perm[p];
+    const int substitution = dir_of(sd, c);
     int out = out_ptr[p];
     if (substitution == 0) {
       for (int e = col_ptr[c + 1] - 1; e > col_ptr[c]; --e, ++out) {
@@ -561,10 +649,10 @@ __global__ void k_fill_push(const int* __restrict__ perm, const int* __restrict_
   }
 }
 cudaError_t launch_fill_push(const int* perm, const int* iperm, const int* col_ptr, const int* row_idx,
-                             const int* out_ptr, int n, int substitution, int* out_pos, int* out_src,
+                             const int* out_ptr, int n, const SysDesc& sd, int* out_pos, int* out_src,
                              cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  k_fill_push<<<grid_for(n), kThreads, 0, s>>>(perm, iperm, col_ptr, row_idx, out_ptr, n, substitution, out_pos,
+  k_fill_push<<<grid_for(n), kThreads, 0, s>>>(perm, iperm, col_ptr, row_idx, out_ptr, n, sd, out_pos,
                                                 out_src);
   return cudaGetLastError();
 }

@@ -44,12 +44,20 @@ struct sptrsv_gb300_handle_s {
   int ctas_per_sm = 0;
   int staged = 1;
   int emax_option = 0;
+  int stages_option = 2;
   // analysis
   bool analysed = false;
   int n = 0, nnz = 0, substitution = 0;
   int nlevels = 0, pmin = 0, pavg = 0, pmax = 0, max_in_degree = 0;
   double analysis_ms = 0.0;
   std::vector<int> level_sizes_host;
+  // batch (several independent triangles in one index space)
+  int batch_count = 1;
+  std::vector<int> sys_off_host, sys_n_host, sys_sub_host;
+  unsigned char* sys_dir = nullptr;
+  int* sys_of = nullptr;
+  int* sys_off = nullptr;
+  int* sys_n = nullptr;
   int* csc_ptr = nullptr;   // owned copy of the structure
   int* csc_row = nullptr;
   int* csc_col = nullptr;   // column of every CSC entry
@@ -159,6 +167,14 @@ void free_values(Values<T>& V) {
 }
 
 void free_analysis(sptrsv_gb300_handle_s* h) {
+  dev_free(&h->sys_dir);
+  dev_free(&h->sys_of);
+  dev_free(&h->sys_off);
+  dev_free(&h->sys_n);
+  h->batch_count = 1;
+  h->sys_off_host.clear();
+  h->sys_n_host.clear();
+  h->sys_sub_host.clear();
   dev_free(&h->csc_ptr);
   dev_free(&h->csc_row);
   dev_free(&h->csc_col);
@@ -194,6 +210,17 @@ int ensure_buf(sptrsv_gb300_handle_s* h, DevBuf& b, size_t bytes, int fill_zero,
   h->device_bytes += bytes;
   if (fill_zero) CUDA_TRY(cudaMemsetAsync(b.p, 0, bytes, s));
   return SPTRSV_OK;
+}
+
+SysDesc sys_desc(const sptrsv_gb300_handle_s* h) {
+  SysDesc d;
+  d.count = h->batch_count;
+  d.substitution = h->substitution;
+  d.dir = h->sys_dir;
+  d.sys_of = h->sys_of;
+  d.sys_off = h->sys_off;
+  d.sys_n = h->sys_n;
+  return d;
 }
 
 unsigned long long timeout_ns(const sptrsv_gb300_handle_s* h) {
@@ -266,7 +293,8 @@ int build_layout(sptrsv_gb300_handle_s* h, int block, cudaStream_t s) {
     // natural order rows
     int* rows_nat = nullptr;
     CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&rows_nat), sizeof(int) * n, s));
-    CUDA_TRY(h->substitution == 0 ? launch_iota(rows_nat, n, 0, 1, s) : launch_iota(rows_nat, n, n - 1, -1, s));
+    const SysDesc sd = sys_desc(h);
+    CUDA_TRY(launch_nat_rows(sd, n, rows_nat, s));
     if (block <= 1) {
       CUDA_TRY(cudaMemcpyAsync(L.perm, rows_nat, sizeof(int) * n, cudaMemcpyDeviceToDevice, s));
     } else {
@@ -283,13 +311,18 @@ int build_layout(sptrsv_gb300_handle_s* h, int block, cudaStream_t s) {
       CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&rows_ls), sizeof(int) * n, s));
       CUDA_TRY(launch_long_keys(rows_nat, h->in_degree, n, kLongDeps, keys, s));
       CUDA_TRY(radix_sort_pairs(keys, rows_nat, keys_sorted, rows_ls, n, 1, temp, s));
-      CUDA_TRY(launch_schedule_keys(rows_ls, h->depth, n, h->substitution, block, 0, keys, s));
+      CUDA_TRY(launch_schedule_keys(rows_ls, h->depth, n, sd, block, 0, keys, s));
       CUDA_TRY(radix_sort_pairs(keys, rows_ls, keys_sorted, level_order ? L.perm : rows_lv, n,
                                 bits_for(h->nlevels - 1), temp, s));
       CUDA_TRY(cudaFreeAsync(rows_ls, s));
       if (!level_order) {
-        CUDA_TRY(launch_schedule_keys(rows_lv, h->depth, n, h->substitution, block, 1, keys, s));
-        CUDA_TRY(radix_sort_pairs(keys, rows_lv, keys_sorted, L.perm, n, bits_for((n - 1) / block), temp, s));
+        CUDA_TRY(launch_schedule_keys(rows_lv, h->depth, n, sd, block, 1, keys, s));
+        int max_sys = 0;
+        for (int v : h->sys_n_host) max_sys = std::max(max_sys, v);
+        if (h->sys_n_host.empty()) max_sys = n;
+        const long long max_key = (long long)((max_sys - 1) / block + 1) * h->batch_count;
+        if (max_key > 0xFFFFFFFFLL) return SPTRSV_ERR_UNSUPPORTED;
+        CUDA_TRY(radix_sort_pairs(keys, rows_lv, keys_sorted, L.perm, n, bits_for(max_key - 1), temp, s));
       }
       CUDA_TRY(cudaFreeAsync(keys, s));
       CUDA_TRY(cudaFreeAsync(keys_sorted, s));
@@ -302,9 +335,9 @@ int build_layout(sptrsv_gb300_handle_s* h, int block, cudaStream_t s) {
     CUDA_TRY(exclusive_scan_int(L.dep_ptr, L.dep_ptr, n, true, s));
     CUDA_TRY(launch_out_counts(L.perm, h->csc_ptr, n, L.out_ptr, s));
     CUDA_TRY(exclusive_scan_int(L.out_ptr, L.out_ptr, n, true, s));
-    CUDA_TRY(launch_fill_pull(L.perm, L.iperm, h->csr_ptr, h->csr_col, h->csr_src, L.dep_ptr, n, h->substitution,
+    CUDA_TRY(launch_fill_pull(L.perm, L.iperm, h->csr_ptr, h->csr_col, h->csr_src, L.dep_ptr, n, sd,
                               L.dep_pos, L.dep_src, L.dep_col, L.diag_src, s));
-    CUDA_TRY(launch_fill_push(L.perm, L.iperm, h->csc_ptr, h->csc_row, L.out_ptr, n, h->substitution, L.out_pos,
+    CUDA_TRY(launch_fill_push(L.perm, L.iperm, h->csc_ptr, h->csc_row, L.out_ptr, n, sd, L.out_pos,
                               L.out_src, s));
     std::vector<int> ptr((size_t)n + 1);
     CUDA_TRY(cudaMemcpyAsync(ptr.data(), L.dep_ptr, sizeof(int) * ((size_t)n + 1), cudaMemcpyDeviceToHost, s));
@@ -376,9 +409,9 @@ int ensure_table(sptrsv_gb300_handle_s* h, bool adj, int cmax, int emax) {
   return build_table(h, t, adj ? h->out_cnt_host : h->dep_cnt_host, adj, cmax, emax);
 }
 
-int auto_emax(int cmax, size_t elem) {
-  // keep one stage near 90 KB so that two buffers leave room for another CTA
-  const long long budget = 90 * 1024;
+int auto_emax(int cmax, size_t elem, int stages) {
+  // keep the ring of stage buffers within ~180 KB of shared memory
+  const long long budget = (180 * 1024) / (stages < 2 ? 2 : stages);
   long long e = budget - (long long)(cmax + 32) * (long long)(8 + elem) - 64;
   e /= (long long)(4 + elem);
   long long want = std::max<long long>(4096, 8LL * cmax);
@@ -448,6 +481,7 @@ ExecConfig pick_config(const sptrsv_gb300_handle_s* h, int rhs) {
   c.ctas_per_sm = h->ctas_per_sm;
   c.staged = h->staged;
   c.emax = h->emax_option;
+  c.stages = h->stages_option;
   return c;
 }
 
@@ -489,7 +523,7 @@ int solve_typed(sptrsv_gb300_handle_s* h, const Values<T>& V, int rhs, int layou
   } else if (c.sched == SCHED_LEVELSET) {
     CUDA_TRY(launch_levelset<T>(h->layout, V, rhs, v, static_cast<T*>(h->xw.p), h->ctl, c, timeout_ns(h), s));
   } else if (rhs == 1 && c.staged) {
-    const int emax = c.emax > 0 ? c.emax : auto_emax(c.chunk, sizeof(T));
+    const int emax = c.emax > 0 ? c.emax : auto_emax(c.chunk, sizeof(T), c.stages);
     ST_TRY(ensure_table(h, adj != nullptr, c.chunk, emax));
     CUDA_TRY(launch_pull_staged<T>(h->layout, V, adj ? h->tab_adj : h->tab_fwd, v, static_cast<T*>(h->xw.p), h->ctl,
                                    c, timeout_ns(h), h->num_sms, s, adj));
@@ -643,6 +677,10 @@ int sptrsv_gb300_set_option(sptrsv_handle_t h, int option, long long value) {
       if (value < 0 || value > (1 << 16)) return SPTRSV_ERR_INVALID;
       h->emax_option = static_cast<int>(value);
       return SPTRSV_OK;
+    case SPTRSV_OPTION_STAGES:
+      if (value < 2 || value > 4) return SPTRSV_ERR_INVALID;
+      h->stages_option = static_cast<int>(value);
+      return SPTRSV_OK;
     default:
       return SPTRSV_ERR_INVALID;
   }
@@ -665,23 +703,21 @@ int sptrsv_gb300_get_option(sptrsv_handle_t h, int option, long long* value) {
     case SPTRSV_OPTION_CTAS_PER_SM: *value = h->ctas_per_sm; break;
     case SPTRSV_OPTION_STAGED: *value = h->staged; break;
     case SPTRSV_OPTION_STAGE_ENTRIES: *value = h->emax_option; break;
+    case SPTRSV_OPTION_STAGES: *value = h->stages_option; break;
     default: return SPTRSV_ERR_INVALID;
   }
   return SPTRSV_OK;
 }
 
-int sptrsv_gb300_analyse(sptrsv_handle_t h, int m, int n, int nnz, const int* d_colPtr, const int* d_rowIdx,
-                         int substitution, void* stream) {
-  if (!h) return SPTRSV_ERR_INVALID;
-  if (m != n) return SPTRSV_ERR_NOT_SQUARE;
-  if (n < 0 || nnz < 0 || (substitution != 0 && substitution != 1)) return SPTRSV_ERR_INVALID;
-  if (nnz < n) return SPTRSV_ERR_BAD_STRUCTURE;  // a diagonal per column at least
-  if (n > 0 && (!d_colPtr || (nnz > 0 && !d_rowIdx))) return SPTRSV_ERR_INVALID;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  free_analysis(h);
-  h->n = n;
-  h->nnz = nnz;
-  h->substitution = substitution;
+}  // extern "C"
+
+namespace {
+// The analysis pipeline on a CSC structure already described by h->n, nnz,
+// substitution and (for batches) the system arrays.
+int analyse_core(sptrsv_handle_t h, const int* d_colPtr, const int* d_rowIdx, cudaStream_t s) {
+  const int n = h->n, nnz = h->nnz, substitution = h->substitution;
+  (void)substitution;
+  const SysDesc sd0 = sys_desc(h);
   cudaEvent_t e0, e1;
   CUDA_TRY(cudaEventCreate(&e0));
   CUDA_TRY(cudaEventCreate(&e1));
@@ -693,7 +729,7 @@ int sptrsv_gb300_analyse(sptrsv_handle_t h, int m, int n, int nnz, const int* d_
   int f = 0;
   ST_TRY(read_flags(h, s, &f));
   if (f) return SPTRSV_ERR_BAD_STRUCTURE;
-  CUDA_TRY(launch_validate_rows(d_colPtr, d_rowIdx, n, substitution, h->flags, s));
+  CUDA_TRY(launch_validate_rows(d_colPtr, d_rowIdx, n, sd0, h->flags, s));
   ST_TRY(read_flags(h, s, &f));
   if (f) return SPTRSV_ERR_BAD_STRUCTURE;
 
@@ -792,7 +828,7 @@ int sptrsv_gb300_analyse(sptrsv_handle_t h, int m, int n, int nnz, const int* d_
     CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&iota), sizeof(int) * n, s));
     CUDA_TRY(cudaMallocAsync(&temp, radix_sort_temp_bytes(n), s));
     CUDA_TRY(launch_iota(iota, n, 0, 1, s));
-    CUDA_TRY(launch_schedule_keys(iota, h->depth, n, 0, 1, 0, keys, s));
+    CUDA_TRY(launch_schedule_keys(iota, h->depth, n, SysDesc(), 1, 0, keys, s));
     CUDA_TRY(radix_sort_pairs(keys, iota, keys_sorted, h->level_item, n, bits_for(nl - 1), temp, s));
     CUDA_TRY(cudaFreeAsync(keys, s));
     CUDA_TRY(cudaFreeAsync(keys_sorted, s));
@@ -818,6 +854,88 @@ int sptrsv_gb300_analyse(sptrsv_handle_t h, int m, int n, int nnz, const int* d_
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return SPTRSV_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int sptrsv_gb300_analyse(sptrsv_handle_t h, int m, int n, int nnz, const int* d_colPtr, const int* d_rowIdx,
+                         int substitution, void* stream) {
+  if (!h) return SPTRSV_ERR_INVALID;
+  if (m != n) return SPTRSV_ERR_NOT_SQUARE;
+  if (n < 0 || nnz < 0 || (substitution != 0 && substitution != 1)) return SPTRSV_ERR_INVALID;
+  if (nnz < n) return SPTRSV_ERR_BAD_STRUCTURE;  // a diagonal per column at least
+  if (n > 0 && (!d_colPtr || (nnz > 0 && !d_rowIdx))) return SPTRSV_ERR_INVALID;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  free_analysis(h);
+  h->n = n;
+  h->nnz = nnz;
+  h->substitution = substitution;
+  return analyse_core(h, d_colPtr, d_rowIdx, s);
+}
+
+int sptrsv_gb300_analyse_batch(sptrsv_handle_t h, int count, const int* h_n, const int* h_nnz,
+                               const int* h_substitution, const int* d_colPtr, const int* d_rowIdx, void* stream) {
+  if (!h || count < 1 || !h_n || !h_nnz || !h_substitution) return SPTRSV_ERR_INVALID;
+  long long total_n = 0, total_nnz = 0;
+  for (int i = 0; i < count; ++i) {
+    if (h_n[i] < 0 || h_nnz[i] < h_n[i] || (h_substitution[i] != 0 && h_substitution[i] != 1))
+      return h_n[i] >= 0 && h_nnz[i] < h_n[i] ? SPTRSV_ERR_BAD_STRUCTURE : SPTRSV_ERR_INVALID;
+    total_n += h_n[i];
+    total_nnz += h_nnz[i];
+  }
+  if (total_n > INT_MAX || total_nnz > INT_MAX) return SPTRSV_ERR_UNSUPPORTED;
+  if (total_n > 0 && (!d_colPtr || (total_nnz > 0 && !d_rowIdx))) return SPTRSV_ERR_INVALID;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  free_analysis(h);
+  const int n = static_cast<int>(total_n), nnz = static_cast<int>(total_nnz);
+  h->n = n;
+  h->nnz = nnz;
+  h->substitution = h_substitution[0];
+  h->batch_count = count;
+  std::vector<int> off(count), eoff(count);
+  long long ro = 0, eo = 0;
+  for (int i = 0; i < count; ++i) {
+    off[i] = static_cast<int>(ro);
+    eoff[i] = static_cast<int>(eo);
+    ro += h_n[i];
+    eo += h_nnz[i];
+  }
+  h->sys_off_host = off;
+  h->sys_n_host.assign(h_n, h_n + count);
+  h->sys_sub_host.assign(h_substitution, h_substitution + count);
+  ST_TRY(dev_alloc(h, &h->sys_dir, n));
+  ST_TRY(dev_alloc(h, &h->sys_of, n));
+  ST_TRY(dev_alloc(h, &h->sys_off, count));
+  ST_TRY(dev_alloc(h, &h->sys_n, count));
+  int *d_eoff = nullptr, *d_sub = nullptr, *g_ptr = nullptr, *g_row = nullptr;
+  CUDA_TRY(cudaMemcpyAsync(h->sys_off, off.data(), sizeof(int) * count, cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(h->sys_n, h_n, sizeof(int) * count, cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&d_eoff), sizeof(int) * count, s));
+  CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&d_sub), sizeof(int) * count, s));
+  CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&g_ptr), sizeof(int) * ((size_t)n + 1), s));
+  CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&g_row), sizeof(int) * ((size_t)nnz + 1), s));
+  CUDA_TRY(cudaMemcpyAsync(d_eoff, eoff.data(), sizeof(int) * count, cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(d_sub, h_substitution, sizeof(int) * count, cudaMemcpyHostToDevice, s));
+  // per-system pointers must start at 0 and end at their nnz: checked by the merged validation
+  CUDA_TRY(cudaMemsetAsync(h->flags, 0, sizeof(int), s));
+  CUDA_TRY(launch_batch_merge(d_colPtr, d_rowIdx, count, h->sys_off, d_eoff, d_sub, n, nnz, g_ptr, g_row, h->sys_dir,
+                              h->sys_of, h->flags, s));
+  int mf = 0;
+  ST_TRY(read_flags(h, s, &mf));
+  const int st = mf ? SPTRSV_ERR_BAD_STRUCTURE : analyse_core(h, g_ptr, g_row, s);
+  cudaFreeAsync(d_eoff, s);
+  cudaFreeAsync(d_sub, s);
+  cudaFreeAsync(g_ptr, s);
+  cudaFreeAsync(g_row, s);
+  cudaStreamSynchronize(s);
+  return st;
+}
+
+int sptrsv_gb300_batch_count(sptrsv_handle_t h, int* count) {
+  if (!h || !count) return SPTRSV_ERR_INVALID;
+  *count = h->batch_count;
+  return h->analysed ? SPTRSV_OK : SPTRSV_ERR_STATE;
 }
 
 int sptrsv_gb300_get_info(sptrsv_handle_t h, sptrsv_info* info) {

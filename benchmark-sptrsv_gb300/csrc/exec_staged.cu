@@ -74,7 +74,7 @@ __device__ __forceinline__ int stage_slice(E* dst, const E* src, long long a, lo
 
 template <typename T>
 struct StagedArgs {
-  int n, nchunks, cmax, emax, smem_tier;
+  int n, nchunks, cmax, emax, smem_tier, stages;
   const int* tab_start;   // [nchunks+1] first original position of each chunk (in walk order)
   const int* tab_mode;    // [nchunks]
   const int* perm;
@@ -140,12 +140,17 @@ __device__ inline StageBufs<T> carve(unsigned char* base, int cmax, int emax) {
   return s;
 }
 
-// Thread 0: claim a chunk and start streaming its slices into stage buffer `sb`.
+// Producer lane: claim a chunk and start streaming its slices into stage
+// buffer `sb`; the copies complete on `bar` (armed with their byte count).
+// A chunk id >= nchunks marks the end of the work.
 template <typename T, bool ADJ>
 __device__ void issue_stage(const StagedArgs<T>& a, StageBufs<T> sb, unsigned long long* bar, StageInfo* info) {
   const unsigned c = ctl_failed(a.ctl) ? (unsigned)a.nchunks : atomicAdd(&a.ctl->ticket, 1u);
   info->chunk = static_cast<int>(c);
-  if (c >= (unsigned)a.nchunks) return;
+  if (c >= (unsigned)a.nchunks) {
+    mbar_arrive_expect_tx(bar, 0);
+    return;
+  }
   const int s0 = a.tab_start[c], s1 = a.tab_start[c + 1];
   // walk order s0..s1-1; in ADJ the walk runs over reversed positions
   const int lo = ADJ ? a.n - s1 : s0;
@@ -156,10 +161,6 @@ __device__ void issue_stage(const StagedArgs<T>& a, StageBufs<T> sb, unsigned lo
   info->hi = hi;
   info->ebase = e0;
   info->mode = mode;
-  unsigned tx = 0;
-  fence_proxy_async_smem();
-  // expect_tx must precede the copies' completion: arm with the byte count
-  // computed up front (the widened sizes are deterministic).
   auto wide = [](long long a_, long long b_, long long per16) {
     return ((b_ + per16 - 1) & ~(per16 - 1)) - (a_ & ~(per16 - 1));
   };
@@ -171,7 +172,9 @@ __device__ void issue_stage(const StagedArgs<T>& a, StageBufs<T> sb, unsigned lo
     expect += (unsigned)(wide(e0, e1, 4) * 4);
     expect += (unsigned)(wide(e0, e1, 16 / sizeof(T)) * sizeof(T));
   }
+  fence_proxy_async_smem();
   mbar_arrive_expect_tx(bar, expect);
+  unsigned tx = 0;
   info->off_ptr = stage_slice<int>(sb.ptr, a.lptr, lo, hi + 1, bar, &tx);
   info->off_perm = stage_slice<int>(sb.perm, a.perm, lo, hi, bar, &tx);
   info->off_sc = stage_slice<T>(sb.sc, a.dscale, lo, hi, bar, &tx);
@@ -183,178 +186,234 @@ __device__ void issue_stage(const StagedArgs<T>& a, StageBufs<T> sb, unsigned lo
   }
 }
 
+// Bounded wait on an mbarrier phase; false once the budget runs out or
+// another thread failed.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, DeviceCtl* ctl,
+                                          unsigned long long timeout, int where) {
+  if (mbar_test(bar, parity)) return true;
+  WaitBudget w(timeout);
+  while (!mbar_test(bar, parity)) {
+    if (!w.poll(ctl, where)) return false;
+  }
+  return true;
+}
+
+constexpr int kMaxStages = 4;
+
+// Warp-specialised pipeline. Warp 0 is the producer: it claims chunks and
+// streams them into a ring of `a.stages` buffers (full[s] completes when a
+// chunk's bytes have landed; empty[s] when every consumer warp is done with
+// it). Warps 1.. are consumers: they take the ring in order, solve the chunk's
+// unknowns from shared memory, and release the buffer. There is no CTA-wide
+// barrier between chunks.
 template <typename T, bool EXACT, bool ADJ>
 __global__ void __launch_bounds__(256) k_pull_staged(StagedArgs<T> a) {
   using F = Flag<T>;
   using Bits = typename F::Bits;
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  __shared__ unsigned long long s_bar[2];
-  __shared__ StageInfo s_info[2];
-  __shared__ int s_fail;
+  __shared__ unsigned long long s_full[kMaxStages], s_empty[kMaxStages];
+  __shared__ StageInfo s_info[kMaxStages];
+  const int S = a.stages;
   const size_t sbytes = stage_bytes<T>(a.cmax, a.emax);
-  StageBufs<T> bufs[2] = {carve<T>(smem_raw, a.cmax, a.emax), carve<T>(smem_raw + sbytes, a.cmax, a.emax)};
-  T* s_x = reinterpret_cast<T*>(smem_raw + 2 * sbytes);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nconsumer_warps = (blockDim.x >> 5) - 1;
+  const int nconsumers = nconsumer_warps * 32;
+  T* s_xbase = reinterpret_cast<T*>(smem_raw + (size_t)S * sbytes);
   if (threadIdx.x == 0) {
-    mbar_init(&s_bar[0], 1);
-    mbar_init(&s_bar[1], 1);
+    for (int i = 0; i < S; ++i) {
+      mbar_init(&s_full[i], 1);
+      mbar_init(&s_empty[i], nconsumer_warps);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    s_fail = 0;
-    issue_stage<T, ADJ>(a, bufs[0], &s_bar[0], &s_info[0]);
   }
   __syncthreads();
-  unsigned parity[2] = {0u, 0u};
-  int st = 0;
-  for (;;) {
-    const StageInfo info = s_info[st];
-    if (info.chunk >= a.nchunks) break;
-    // Prefetch the next chunk into the other buffer (its previous contents were
-    // consumed before the barrier that ended the last iteration).
-    if (threadIdx.x == 0) issue_stage<T, ADJ>(a, bufs[st ^ 1], &s_bar[st ^ 1], &s_info[st ^ 1]);
-    // Wait for this chunk's slices (bounded).
-    if (!mbar_test(&s_bar[st], parity[st])) {
-      WaitBudget w(a.timeout_ns);
-      while (!mbar_test(&s_bar[st], parity[st])) {
-        if (!w.poll(a.ctl, info.lo)) { s_fail = 1; break; }
+
+  if (warp == 0) {
+    // ---------------- producer
+    bool in_flight[kMaxStages] = {false, false, false, false};
+    unsigned issued_parity[kMaxStages] = {0u, 0u, 0u, 0u};
+    for (int r = 0;; ++r) {
+      const int st = r % S;
+      const unsigned round = static_cast<unsigned>(r / S);
+      // wait until every consumer warp released this buffer (first round: free)
+      bool ok = true;
+      if (lane == 0) ok = mbar_wait(&s_empty[st], (round & 1u) ^ 1u, a.ctl, a.timeout_ns, -1);
+      ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+      if (!ok) break;
+      in_flight[st] = false;
+      if (a.smem_tier) {
+        T* sx = s_xbase + (size_t)st * a.cmax;
+        for (int i = lane; i < a.cmax; i += 32) *reinterpret_cast<Bits*>(&sx[i]) = F::EMPTY;
       }
+      __syncwarp();
+      int chunk = 0;
+      if (lane == 0) {
+        StageBufs<T> sb = carve<T>(smem_raw + (size_t)st * sbytes, a.cmax, a.emax);
+        issue_stage<T, ADJ>(a, sb, &s_full[st], &s_info[st]);
+        chunk = s_info[st].chunk;
+      }
+      chunk = __shfl_sync(0xffffffffu, chunk, 0);
+      if (chunk >= a.nchunks) break;
+      in_flight[st] = true;
+      issued_parity[st] = round & 1u;
     }
-    parity[st] ^= 1u;
-    const int len = info.hi - info.lo;
-    if (a.smem_tier)
-      for (int i = threadIdx.x; i < len; i += blockDim.x) *reinterpret_cast<Bits*>(&s_x[i]) = F::EMPTY;
-    __syncthreads();
-    bool fail = s_fail != 0;
-    const StageBufs<T> sb = bufs[st];
-    const int* sptr = sb.ptr + info.off_ptr;
-    const int* sperm = sb.perm + info.off_perm;
-    const T* ssc = sb.sc + info.off_sc;
-    const int* spos = sb.pos + info.off_pos;
-    const T* sval = sb.val + info.off_val;
-    const int lo = info.lo, hi = info.hi;
-    // position p (original) -> local index li = p - lo; walk index i -> p
-    auto pos_of = [&](int i) { return ADJ ? hi - 1 - i : lo + i; };
-    auto is_local = [&](int q) { return ADJ ? (q < hi) : (q >= lo); };
-    if (!fail && (EXACT || info.mode == 0)) {
-      constexpr int U = 8;
-      const bool from_smem = info.mode != 2;
-      const int* vpos = from_smem ? spos : a.lpos;
-      const T* vval = from_smem ? sval : a.lval;
-      for (int i = threadIdx.x; i < len && !fail; i += blockDim.x) {
-        const int p = pos_of(i);
-        const int li = p - lo;
-        const int row = sperm[li];
-        const int ea = from_smem ? sptr[li] - info.ebase : sptr[li];
-        const int eb = from_smem ? sptr[li + 1] - info.ebase : sptr[li + 1];
-        const T bi = a.b[(long long)row * a.b_si];
-        const T sc = ssc[li];
-        T acc = EXACT ? T(0) : bi * sc;
-        for (int e = ea; e < eb && !fail; e += U) {
-          int q[U];
-          T w[U];
-          Bits bits[U];
-#pragma unroll
-          for (int u = 0; u < U; ++u) {
-            q[u] = e + u < eb ? vpos[e + u] : -1;
-            w[u] = e + u < eb ? vval[e + u] : T(0);
-          }
-#pragma unroll
-          for (int u = 0; u < U; ++u) {
-            bits[u] = F::EMPTY;
-            if (q[u] >= 0) bits[u] = (a.smem_tier && is_local(q[u])) ? F::load_shared(&s_x[q[u] - lo]) : F::load(&a.xw[q[u]]);
-          }
-#pragma unroll
-          for (int u = 0; u < U; ++u) {
-            if (q[u] < 0 || fail) continue;
-            if (bits[u] == F::EMPTY) {
-              bits[u] = (a.smem_tier && is_local(q[u]))
-                            ? wait_flag_dev<T, true>(&s_x[q[u] - lo], a.ctl, a.timeout_ns, p, 0, 0)
-                            : wait_flag_dev<T, false>(&a.xw[q[u]], a.ctl, a.timeout_ns, p, a.sleep_min, a.sleep_max);
-              if (bits[u] == F::EMPTY) { fail = true; continue; }
-            }
-            acc = EXACT ? exact_mul_add<T>(acc, w[u], F::value(bits[u])) : fma(-w[u], F::value(bits[u]), acc);
-          }
-        }
-        if (fail) break;
-        const T xi = EXACT ? exact_finish<T>(bi, acc, sc) : acc;
-        if (a.smem_tier) F::store_shared(&s_x[li], xi);
-        F::store(&a.xw[p], xi);
-        a.x[(long long)row * a.x_si] = xi;
-        if (ADJ && a.grad) {
-          for (int e = a.dep_ptr[p]; e < a.dep_ptr[p + 1]; ++e)
-            a.grad[a.dep_src[e]] = -xi * a.xf[(long long)a.dep_col[e] * a.xf_si];
-          a.grad[a.diag_src[p]] = -xi * a.xf[(long long)row * a.xf_si];
-        }
-      }
-    } else if (!fail) {
-      // one warp per unknown; lanes over its dependency list
-      constexpr int U = 2;
-      const bool from_smem = info.mode == 1;
-      for (int i = warp; i < len && !fail; i += nwarps) {
-        const int p = pos_of(i);
-        const int li = p - lo;
-        const int row = sperm[li];
-        const int ea = from_smem ? sptr[li] - info.ebase : sptr[li];
-        const int eb = from_smem ? sptr[li + 1] - info.ebase : sptr[li + 1];
-        const int* vpos = from_smem ? spos : a.lpos;
-        const T* vval = from_smem ? sval : a.lval;
-        const T bi = a.b[(long long)row * a.b_si];
-        const T sc = ssc[li];
-        T acc = (lane == 0 && !EXACT) ? bi * sc : T(0);
-        for (int e = ea + lane; e < eb && !fail; e += 32 * U) {
-          int q[U];
-          T w[U];
-          Bits bits[U];
-#pragma unroll
-          for (int u = 0; u < U; ++u) {
-            const int ee = e + u * 32;
-            q[u] = ee < eb ? vpos[ee] : -1;
-            w[u] = ee < eb ? vval[ee] : T(0);
-          }
-#pragma unroll
-          for (int u = 0; u < U; ++u) {
-            bits[u] = F::EMPTY;
-            if (q[u] >= 0) bits[u] = (a.smem_tier && is_local(q[u])) ? F::load_shared(&s_x[q[u] - lo]) : F::load(&a.xw[q[u]]);
-          }
-#pragma unroll
-          for (int u = 0; u < U; ++u) {
-            if (q[u] < 0 || fail) continue;
-            if (bits[u] == F::EMPTY) {
-              bits[u] = (a.smem_tier && is_local(q[u]))
-                            ? wait_flag_dev<T, true>(&s_x[q[u] - lo], a.ctl, a.timeout_ns, p, 0, 0)
-                            : wait_flag_dev<T, false>(&a.xw[q[u]], a.ctl, a.timeout_ns, p, a.sleep_min, a.sleep_max);
-              if (bits[u] == F::EMPTY) { fail = true; continue; }
-            }
-            acc = fma(-w[u], F::value(bits[u]), acc);
-          }
-        }
-        fail = __any_sync(0xffffffffu, fail);
-        if (fail) break;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        const T xi = acc;
-        if (lane == 0) {
-          if (a.smem_tier) F::store_shared(&s_x[li], xi);
-          F::store(&a.xw[p], xi);
-          a.x[(long long)row * a.x_si] = xi;
-        }
-        if (ADJ && a.grad) {
-          for (int e = a.dep_ptr[p] + lane; e < a.dep_ptr[p + 1]; e += 32)
-            a.grad[a.dep_src[e]] = -xi * a.xf[(long long)a.dep_col[e] * a.xf_si];
-          if (lane == 0) a.grad[a.diag_src[p]] = -xi * a.xf[(long long)row * a.xf_si];
-        }
-      }
-    }
-    if (__syncthreads_or(fail)) {
-      // Let the prefetch already in flight land before the CTA leaves.
-      if (threadIdx.x == 0 && s_info[st ^ 1].chunk < a.nchunks) {
+    if (lane == 0) {
+      // copies issued but possibly never consumed (a consumer failed) must land
+      // before the CTA leaves; in a normal run these phases are already complete
+      for (int i = 0; i < S; ++i) {
+        if (!in_flight[i]) continue;
         WaitBudget w(a.timeout_ns);
-        while (!mbar_test(&s_bar[st ^ 1], parity[st ^ 1])) {
+        while (!mbar_test(&s_full[i], issued_parity[i])) {
           if (!w.poll(a.ctl, -1)) break;
         }
       }
-      break;
     }
-    st ^= 1;
+  } else {
+    // ---------------- consumers
+    const int ct = threadIdx.x - 32;     // consumer thread index
+    const int cw = warp - 1;             // consumer warp index
+    bool fail = false;
+    for (int r = 0;; ++r) {
+      const int st = r % S;
+      const unsigned round = static_cast<unsigned>(r / S);
+      if (!mbar_wait(&s_full[st], round & 1u, a.ctl, a.timeout_ns, -1)) fail = true;
+      fail = __any_sync(0xffffffffu, fail);
+      if (fail) break;
+      const StageInfo info = s_info[st];
+      if (info.chunk >= a.nchunks) break;
+      const StageBufs<T> sb = carve<T>(smem_raw + (size_t)st * sbytes, a.cmax, a.emax);
+      T* s_x = s_xbase + (size_t)st * a.cmax;
+      const int* sptr = sb.ptr + info.off_ptr;
+      const int* sperm = sb.perm + info.off_perm;
+      const T* ssc = sb.sc + info.off_sc;
+      const int* spos = sb.pos + info.off_pos;
+      const T* sval = sb.val + info.off_val;
+      const int lo = info.lo, hi = info.hi;
+      const int len = hi - lo;
+      auto pos_of = [&](int i) { return ADJ ? hi - 1 - i : lo + i; };
+      auto is_local = [&](int q) { return ADJ ? (q < hi) : (q >= lo); };
+      if (EXACT || info.mode == 0) {
+        constexpr int U = 8;
+        const bool from_smem = info.mode != 2;
+        const int* vpos = from_smem ? spos : a.lpos;
+        const T* vval = from_smem ? sval : a.lval;
+        for (int i = ct; i < len && !fail; i += nconsumers) {
+          const int p = pos_of(i);
+          const int li = p - lo;
+          const int row = sperm[li];
+          const int ea = from_smem ? sptr[li] - info.ebase : sptr[li];
+          const int eb = from_smem ? sptr[li + 1] - info.ebase : sptr[li + 1];
+          const T bi = a.b[(long long)row * a.b_si];
+          const T sc = ssc[li];
+          T acc = EXACT ? T(0) : bi * sc;
+          for (int e = ea; e < eb && !fail; e += U) {
+            int q[U];
+            T w[U];
+            Bits bits[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+              q[u] = e + u < eb ? vpos[e + u] : -1;
+              w[u] = e + u < eb ? vval[e + u] : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+              bits[u] = F::EMPTY;
+              if (q[u] >= 0)
+                bits[u] = (a.smem_tier && is_local(q[u])) ? F::load_shared(&s_x[q[u] - lo]) : F::load(&a.xw[q[u]]);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+              if (q[u] < 0 || fail) continue;
+              if (bits[u] == F::EMPTY) {
+                bits[u] = (a.smem_tier && is_local(q[u]))
+                              ? wait_flag_dev<T, true>(&s_x[q[u] - lo], a.ctl, a.timeout_ns, p, 0, 0)
+                              : wait_flag_dev<T, false>(&a.xw[q[u]], a.ctl, a.timeout_ns, p, a.sleep_min, a.sleep_max);
+                if (bits[u] == F::EMPTY) { fail = true; continue; }
+              }
+              acc = EXACT ? exact_mul_add<T>(acc, w[u], F::value(bits[u])) : fma(-w[u], F::value(bits[u]), acc);
+            }
+          }
+          if (fail) break;
+          const T xi = EXACT ? exact_finish<T>(bi, acc, sc) : acc;
+          if (a.smem_tier) F::store_shared(&s_x[li], xi);
+          F::store(&a.xw[p], xi);
+          a.x[(long long)row * a.x_si] = xi;
+          if (ADJ && a.grad) {
+            for (int e = a.dep_ptr[p]; e < a.dep_ptr[p + 1]; ++e)
+              a.grad[a.dep_src[e]] = -xi * a.xf[(long long)a.dep_col[e] * a.xf_si];
+            a.grad[a.diag_src[p]] = -xi * a.xf[(long long)row * a.xf_si];
+          }
+        }
+      } else {
+        // one warp per unknown; lanes over its dependency list
+        constexpr int U = 2;
+        const bool from_smem = info.mode == 1;
+        for (int i = cw; i < len && !fail; i += nconsumer_warps) {
+          const int p = pos_of(i);
+          const int li = p - lo;
+          const int row = sperm[li];
+          const int ea = from_smem ? sptr[li] - info.ebase : sptr[li];
+          const int eb = from_smem ? sptr[li + 1] - info.ebase : sptr[li + 1];
+          const int* vpos = from_smem ? spos : a.lpos;
+          const T* vval = from_smem ? sval : a.lval;
+          const T bi = a.b[(long long)row * a.b_si];
+          const T sc = ssc[li];
+          T acc = lane == 0 ? bi * sc : T(0);
+          for (int e = ea + lane; e < eb && !fail; e += 32 * U) {
+            int q[U];
+            T w[U];
+            Bits bits[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+              const int ee = e + u * 32;
+              q[u] = ee < eb ? vpos[ee] : -1;
+              w[u] = ee < eb ? vval[ee] : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+              bits[u] = F::EMPTY;
+              if (q[u] >= 0)
+                bits[u] = (a.smem_tier && is_local(q[u])) ? F::load_shared(&s_x[q[u] - lo]) : F::load(&a.xw[q[u]]);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+              if (q[u] < 0 || fail) continue;
+              if (bits[u] == F::EMPTY) {
+                bits[u] = (a.smem_tier && is_local(q[u]))
+                              ? wait_flag_dev<T, true>(&s_x[q[u] - lo], a.ctl, a.timeout_ns, p, 0, 0)
+                              : wait_flag_dev<T, false>(&a.xw[q[u]], a.ctl, a.timeout_ns, p, a.sleep_min, a.sleep_max);
+                if (bits[u] == F::EMPTY) { fail = true; continue; }
+              }
+              acc = fma(-w[u], F::value(bits[u]), acc);
+            }
+          }
+          fail = __any_sync(0xffffffffu, fail);
+          if (fail) break;
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+          const T xi = acc;
+          if (lane == 0) {
+            if (a.smem_tier) F::store_shared(&s_x[li], xi);
+            F::store(&a.xw[p], xi);
+            a.x[(long long)row * a.x_si] = xi;
+          }
+          if (ADJ && a.grad) {
+            for (int e = a.dep_ptr[p] + lane; e < a.dep_ptr[p + 1]; e += 32)
+              a.grad[a.dep_src[e]] = -xi * a.xf[(long long)a.dep_col[e] * a.xf_si];
+            if (lane == 0) a.grad[a.diag_src[p]] = -xi * a.xf[(long long)row * a.xf_si];
+          }
+        }
+      }
+      fail = __any_sync(0xffffffffu, fail);
+      if (fail) break;
+      // release the buffer (one arrival per consumer warp)
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&s_empty[st])) : "memory");
+    }
+    if (fail && lane == 0) {
+      // make the producer stop: record a failure if none is recorded yet
+      atomicCAS(&a.ctl->code, DEV_OK, DEV_TIMEOUT);
+    }
   }
   __syncthreads();
   leave(a.ctl);
@@ -362,7 +421,7 @@ __global__ void __launch_bounds__(256) k_pull_staged(StagedArgs<T> a) {
 
 template <typename T, bool EXACT, bool ADJ>
 cudaError_t run_staged(const StagedArgs<T>& a, int block, int ctas_per_sm, int num_sms, cudaStream_t s) {
-  const size_t smem = 2 * stage_bytes<T>(a.cmax, a.emax) + (a.smem_tier ? sizeof(T) * (size_t)a.cmax : 0);
+  const size_t smem = (size_t)a.stages * (stage_bytes<T>(a.cmax, a.emax) + (a.smem_tier ? sizeof(T) * (size_t)a.cmax : 0));
   auto kernel = k_pull_staged<T, EXACT, ADJ>;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -381,9 +440,9 @@ cudaError_t run_staged(const StagedArgs<T>& a, int block, int ctas_per_sm, int n
 
 }  // namespace
 
-size_t staged_smem_bytes(int cmax, int emax, size_t elem, bool smem_tier) {
-  return 2 * (elem == 8 ? stage_bytes<double>(cmax, emax) : stage_bytes<float>(cmax, emax)) +
-         (smem_tier ? elem * (size_t)cmax : 0);
+size_t staged_smem_bytes(int cmax, int emax, size_t elem, bool smem_tier, int stages) {
+  return (size_t)stages * ((elem == 8 ? stage_bytes<double>(cmax, emax) : stage_bytes<float>(cmax, emax)) +
+                           (smem_tier ? elem * (size_t)cmax : 0));
 }
 
 template <typename T>
@@ -397,6 +456,7 @@ cudaError_t launch_pull_staged(const Layout& L, const Values<T>& V, const ChunkT
   a.cmax = tab.cmax;
   a.emax = tab.emax;
   a.smem_tier = cfg.smem_tier;
+  a.stages = cfg.stages < 2 ? 2 : (cfg.stages > kMaxStages ? kMaxStages : cfg.stages);
   a.tab_start = tab.start;
   a.tab_mode = tab.mode;
   a.perm = L.perm;

@@ -34,6 +34,7 @@ struct ExecConfig {
   unsigned sleep_max = 0; // backoff cap of global polls in ns (0: spin)
   int staged = 1;         // one right-hand side: TMA-staged chunk executor
   int emax = 0;           // staged: dependency entries per chunk (0: automatic)
+  int stages = 2;         // staged: chunk buffers in the producer/consumer ring
 };
 
 // Work units of the staged executor: chunk k covers walk indices
@@ -91,10 +92,30 @@ struct Values {
   T* rcp = nullptr;      // [n] correctly rounded 1/diag
 };
 
+// Independent triangles sharing one index space (a batch): unknown c belongs
+// to system sys_of[c], whose unknowns are [sys_off[s], sys_off[s] + sys_n[s])
+// and which is solved forward (dir 0, lower) or backward (dir 1, upper). A
+// single system has count 1, null arrays and a uniform `substitution`.
+struct SysDesc {
+  int count = 1;
+  int substitution = 0;
+  const unsigned char* dir = nullptr;
+  const int* sys_of = nullptr;
+  const int* sys_off = nullptr;
+  const int* sys_n = nullptr;
+};
+
 // ---------------------------------------------------------------- analysis
 cudaError_t launch_validate_ptr(const int* col_ptr, int n, int nnz, int* flags, cudaStream_t s);
-cudaError_t launch_validate_rows(const int* col_ptr, const int* row_idx, int n, int substitution,
-                                 int* flags, cudaStream_t s);
+cudaError_t launch_validate_rows(const int* col_ptr, const int* row_idx, int n, const SysDesc& sd, int* flags,
+                                 cudaStream_t s);
+// batch: merge per-system CSC arrays (local indices, concatenated) into one
+// block-diagonal CSC and fill the per-unknown system/direction arrays
+cudaError_t launch_batch_merge(const int* col_ptr_cat, const int* row_idx_cat, int count, const int* sys_off,
+                               const int* sys_eoff, const int* sys_sub, int n, int nnz, int* col_ptr, int* row_idx,
+                               unsigned char* dir, int* sys_of, int* flags, cudaStream_t s);
+// natural execution order: forward systems ascending, backward systems descending
+cudaError_t launch_nat_rows(const SysDesc& sd, int n, int* rows_nat, cudaStream_t s);
 cudaError_t launch_in_degree(const int* row_idx, int m, int nnz, int* in_degree, cudaStream_t s);
 // exclusive scan of `count` ints; out may alias in; out[count] receives the total when with_total.
 cudaError_t exclusive_scan_int(const int* in, int* out, int count, bool with_total, cudaStream_t s);
@@ -109,7 +130,7 @@ cudaError_t launch_gather_int(const int* src, const int* idx, int* out, int coun
 cudaError_t launch_levels(const int* col_ptr, const int* row_idx, const int* in_degree, int n,
                           int* cnt_scratch, int* front_a, int* front_b, int* depth, int* level_sizes,
                           DeviceCtl* ctl, unsigned long long timeout_ns, cudaStream_t s);
-cudaError_t launch_schedule_keys(const int* rows, const int* depth, int n, int substitution, int block,
+cudaError_t launch_schedule_keys(const int* rows, const int* depth, int n, const SysDesc& sd, int block,
                                  int mode, unsigned* keys, cudaStream_t s);
 cudaError_t launch_inverse_perm(const int* perm, int n, int* iperm, cudaStream_t s);
 // key = 0 for rows with more than `threshold` dependencies, 1 otherwise
@@ -118,10 +139,10 @@ cudaError_t launch_long_keys(const int* rows, const int* in_degree, int n, int t
 cudaError_t launch_dep_counts(const int* perm, const int* in_degree, int n, int* counts, cudaStream_t s);
 cudaError_t launch_out_counts(const int* perm, const int* col_ptr, int n, int* counts, cudaStream_t s);
 cudaError_t launch_fill_pull(const int* perm, const int* iperm, const int* csr_ptr, const int* csr_col,
-                             const int* csr_src, const int* dep_ptr, int n, int substitution,
+                             const int* csr_src, const int* dep_ptr, int n, const SysDesc& sd,
                              int* dep_pos, int* dep_src, int* dep_col, int* diag_src, cudaStream_t s);
 cudaError_t launch_fill_push(const int* perm, const int* iperm, const int* col_ptr, const int* row_idx,
-                             const int* out_ptr, int n, int substitution, int* out_pos, int* out_src,
+                             const int* out_ptr, int n, const SysDesc& sd, int* out_pos, int* out_src,
                              cudaStream_t s);
 template <typename TV, typename T>
 cudaError_t launch_stage_values(const Layout& L, const TV* val, Values<T>& V, int* flags, cudaStream_t s);
@@ -147,7 +168,7 @@ cudaError_t launch_levelset(const Layout& L, const Values<T>& V, int rhs, const 
                             DeviceCtl* ctl, const ExecConfig& cfg, unsigned long long timeout_ns,
                             cudaStream_t s);
 size_t pull_smem_bytes(int chunk, int rhs, size_t elem);
-size_t staged_smem_bytes(int cmax, int emax, size_t elem, bool smem_tier);
+size_t staged_smem_bytes(int cmax, int emax, size_t elem, bool smem_tier, int stages);
 template <typename T>
 cudaError_t launch_pull_staged(const Layout& L, const Values<T>& V, const ChunkTable& tab, const VecView<T>& v, T* xw,
                                DeviceCtl* ctl, const ExecConfig& cfg, unsigned long long timeout_ns, int num_sms,

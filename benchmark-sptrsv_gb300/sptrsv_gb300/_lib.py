@@ -55,6 +55,7 @@ OPTION_BACKOFF_NS = 10
 OPTION_CTAS_PER_SM = 11
 OPTION_STAGED = 12
 OPTION_STAGE_ENTRIES = 13
+OPTION_STAGES = 14
 
 
 class SptrsvError(RuntimeError):
@@ -107,6 +108,8 @@ SIGNATURES = {
     "sptrsv_gb300_get_option": (_I, [_VP, _I, ctypes.POINTER(_LL)]),
     "sptrsv_gb300_analyse": (_I, [_VP, _I, _I, _I, _VP, _VP, _I, _VP]),
     "sptrsv_gb300_get_info": (_I, [_VP, ctypes.POINTER(Info)]),
+    "sptrsv_gb300_analyse_batch": (_I, [_VP, _I, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "sptrsv_gb300_batch_count": (_I, [_VP, ctypes.POINTER(_I)]),
     "sptrsv_gb300_levels": (_I, [_VP, _VP, _VP, _VP]),
     "sptrsv_gb300_csr": (_I, [_VP, _VP, _VP, _VP, _VP]),
     "sptrsv_gb300_set_values": (_I, [_VP, _VP, _I, _VP]),

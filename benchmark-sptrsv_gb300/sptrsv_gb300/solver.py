@@ -95,7 +95,7 @@ class SyncFreeSolver:
                  schedule: int = SCHED_AUTO, lanes: int = 0, chunk: int = 0, order_block: int | None = None,
                  exact: bool = False, smem_tier: bool = True, timeout_ms: int = 1000, sync_check: bool = True,
                  profile: bool = False, block: int = 0, backoff_ns: int | None = None, ctas_per_sm: int = 0,
-                 staged: bool = True, stage_entries: int = 0, stream=None):
+                 staged: bool = True, stage_entries: int = 0, stages: int = 2, stream=None):
         torch = _torch()
         self._lib = load()
         self.device = torch.device("cuda", torch.cuda.current_device())
@@ -123,6 +123,7 @@ class SyncFreeSolver:
         self.set_option(_lib.OPTION_CTAS_PER_SM, int(ctas_per_sm))
         self.set_option(_lib.OPTION_STAGED, int(staged))
         self.set_option(_lib.OPTION_STAGE_ENTRIES, int(stage_entries))
+        self.set_option(_lib.OPTION_STAGES, int(stages))
         self._stream = stream
         self.analyse()
         self.values = None

@@ -90,7 +90,8 @@ typedef enum sptrsv_option {
   SPTRSV_OPTION_CTAS_PER_SM = 11, /* resident CTAs per SM of the executors (0 = as many as fit) */
   SPTRSV_OPTION_STAGED = 12,      /* 1 (default): one-rhs pull solves stream each chunk's layout slices
                                      into shared memory with bulk copies (TMA), double-buffered */
-  SPTRSV_OPTION_STAGE_ENTRIES = 13 /* staged executor: dependency entries per chunk buffer (0 = auto) */
+  SPTRSV_OPTION_STAGE_ENTRIES = 13, /* staged executor: dependency entries per chunk buffer (0 = auto) */
+  SPTRSV_OPTION_STAGES = 14       /* staged executor: chunk buffers in the producer/consumer ring (2-4) */
 } sptrsv_option;
 
 typedef struct sptrsv_info {
@@ -175,6 +176,20 @@ int sptrsv_gb300_get_option(sptrsv_handle_t handle, int option, long long *value
 int sptrsv_gb300_analyse(sptrsv_handle_t handle, int m, int n, int nnz, const int *d_colPtr, const int *d_rowIdx,
                          int substitution, void *stream);
 int sptrsv_gb300_get_info(sptrsv_handle_t handle, sptrsv_info *info);
+
+/* Batch analysis: `count` independent square triangles, each lower (forward)
+ * or upper (backward) per h_substitution[s], analysed into ONE handle that
+ * solves all of them in one persistent launch. h_n, h_nnz, h_substitution are
+ * host arrays; d_colPtr concatenates the per-system column pointer arrays
+ * (n_s+1 entries each, local 0-based), d_rowIdx the per-system row indices
+ * (local). Afterwards the handle behaves as one system of sum(n_s) unknowns:
+ * values are the per-system value arrays concatenated, and b / x are
+ * sum(n_s) x rhs blocks (system s occupies rows off_s .. off_s+n_s-1).
+ * The schedule interleaves the systems block by block (or by level with
+ * SPTRSV_OPTION_ORDER_BLOCK >= sum(n_s)). */
+int sptrsv_gb300_analyse_batch(sptrsv_handle_t handle, int count, const int *h_n, const int *h_nnz,
+                               const int *h_substitution, const int *d_colPtr, const int *d_rowIdx, void *stream);
+int sptrsv_gb300_batch_count(sptrsv_handle_t handle, int *count);
 
 /* Copies level sets out (device pointers; level_ptr[nlevels+1] with the
  * row counts of findlevel, level_item[n] the rows of each level in ascending

@@ -50,6 +50,8 @@ CONFIGS = [
     dict(schedule=2, chunk=32, stage_entries=64),
     dict(schedule=2, chunk=7, stage_entries=16, order_block=10**9, smem_tier=False),
     dict(schedule=2, chunk=4096, block=64, ctas_per_sm=1, backoff_ns=0),
+    dict(schedule=2, chunk=100, stages=3, order_block=10**9),
+    dict(schedule=2, chunk=33, stages=4, stage_entries=48, block=128),
     dict(schedule=3, lanes=1),
     dict(schedule=3, lanes=8),
 ]
