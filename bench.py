@@ -20,6 +20,18 @@ Arms:
                    or the reference build where it exists), the four solves of a
                    step run concurrently on four host threads.
 Multi-GPU: every rank solves the same workload independently (replicas).
+
+Other workloads (--workload; each prints one JSON line of its own metric):
+  multi_rhs  n = 1,000,000, Poisson(9) off-diagonals in a band of 20,000,
+             rhs in {1, 16, 64}, B ~ N(0,1) column-major: plain FP64 solve vs
+             FP32 storage/solve + FP64-residual refinement; forward error vs
+             the FP64 oracle.
+  batch      512 independent systems (even lower, odd upper), n log-uniform on
+             [1e3, 2e5], stored entries per column U{3..20}, band U[100, 1e4],
+             rhs = 4: one batched FP32+refinement launch sequence vs 512
+             per-system plain FP64 launches; systems solved per second.
+  adjoint    the multi_rhs matrix, rhs = 8, FP64, loss = sum(w * x):
+             forward + adjoint (fused value gradient) time over forward time.
 """
 from __future__ import annotations
 
@@ -345,6 +357,156 @@ def run_gpu(args, world, rank, local):
     return 0
 
 
+# ------------------------------------------------------------------ other workloads
+def _timed(fn, reps, flush=None):
+    import torch
+    ts = []
+    for _ in range(reps):
+        if flush is not None:
+            flush.fill_(1)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return statistics.median(ts)
+
+
+def run_multi_rhs(args):
+    import torch
+
+    from oracle import oracle
+    from sptrsv_gb300 import SyncFreeSolver, matgen
+    m = matgen.system_1m(seed=2)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    out = {}
+    for rhs in (1, 16, 64):
+        rng = np.random.default_rng(rhs)
+        B = rng.standard_normal((m.n, rhs))
+        ref = oracle.port().solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, B if rhs > 1 else B[:, 0])
+        ref = ref.reshape(m.n, rhs)
+        b = torch.from_numpy(np.ascontiguousarray(B.T)).cuda().t()
+        s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, values=m.val, sync_check=False,
+                           **args.solver_kw)
+        x = s.solve(b)
+        t64 = _timed(lambda: s.solve(b, out=x), args.steps, flush)
+        err64 = float((x.cpu().numpy() - ref).__abs__().max() / np.abs(ref).max())
+        s.set_option(7, 1)
+        xr, iters, est = s.solve_refine(b)
+        s.set_option(7, 0)
+        tmix = _timed(lambda: s.solve_refine(b, out=xr, tol=0.0, max_iter=iters), args.steps, flush)
+        errmix = float((xr.cpu().numpy() - ref).__abs__().max() / np.abs(ref).max())
+        bp = bytes_pass(m.n, m.nnz, rhs)
+        out[f"rhs{rhs}"] = {"fp64_ms": round(t64, 4), "mixed_ms": round(tmix, 4), "refine_steps": iters,
+                            "speedup_mixed_vs_fp64": round(t64 / tmix, 3), "fp64_fwd_err": err64,
+                            "mixed_fwd_err": errmix, "fp64_problem_gbs": round(bp / t64 / 1e6, 2),
+                            "mixed_problem_gbs": round(bp / tmix / 1e6, 2)}
+        s.close()
+    line = {"workload": "multi_rhs", "metric": "FP32+FP64-refinement speed-up over plain FP64 (n=1M, rhs=64)",
+            "value": out["rhs64"]["speedup_mixed_vs_fp64"], "unit": "x", "higher_is_better": True,
+            "n": m.n, "nnz": m.nnz, "cases": out, "config": {"workload": "n=1M Poisson(9) band 20k, col-major B"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_batch(args):
+    import torch
+
+    from oracle import oracle
+    from sptrsv_gb300 import SyncFreeSolver, matgen
+    t0 = time.perf_counter()
+    systems = matgen.batch_uneven(count=args.batch_count, seed=3)
+    tgen = time.perf_counter() - t0
+    rhs = 4
+    rng = np.random.default_rng(4)
+    bs = [rng.standard_normal((m.n, rhs)) for m in systems]
+    ntot = sum(m.n for m in systems)
+    nnz = sum(m.nnz for m in systems)
+    vals = np.concatenate([m.val for m in systems])
+    t0 = time.perf_counter()
+    s = SyncFreeSolver(batch=[(m.col_ptr, m.row_idx, m.n, m.substitution) for m in systems], values=vals,
+                       sync_check=False, **args.solver_kw)
+    tan = time.perf_counter() - t0
+    b = torch.from_numpy(np.concatenate(bs)).cuda()
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    s.set_option(7, 1)
+    xr, iters, est = s.solve_refine(b)
+    s.set_option(7, 0)
+    t_mixed = _timed(lambda: s.solve_refine(b, out=xr, tol=0.0, max_iter=iters), args.steps, flush)
+    x64 = s.solve(b)
+    t_b64 = _timed(lambda: s.solve(b, out=x64), args.steps, flush)
+    # per-system plain FP64 launches (one handle per system, one launch each)
+    hs = [SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, values=m.val, sync_check=False,
+                         **args.solver_kw) for m in systems]
+    bd = [torch.from_numpy(bb).cuda() for bb in bs]
+    xd = [torch.empty_like(bb) for bb in bd]
+
+    def per_system():
+        for h, bb, xx in zip(hs, bd, xd):
+            h.solve(bb, out=xx)
+    per_system()
+    t_per = _timed(per_system, max(3, args.steps // 3), flush)
+    # forward error vs the per-system FP64 oracle on a sample of systems
+    xr_h = xr.cpu().numpy()
+    off = s.offsets
+    sample = list(range(0, len(systems), max(1, len(systems) // 16)))
+    err = 0.0
+    for k in sample:
+        m = systems[k]
+        ref = oracle.port().solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, bs[k])
+        err = max(err, float(np.abs(xr_h[off[k]:off[k + 1]] - ref).max() / np.abs(ref).max()))
+    nsys = len(systems)
+    line = {"workload": "batch", "metric": "batched solves/s (FP32+FP64 refinement, one persistent launch per pass)",
+            "value": round(nsys / (t_mixed * 1e-3), 2), "unit": "systems/s", "higher_is_better": True,
+            "systems": nsys, "n_total": ntot, "nnz_total": nnz, "rhs": rhs,
+            "mixed_batched_ms": round(t_mixed, 3), "refine_steps": iters, "fp64_batched_ms": round(t_b64, 3),
+            "fp64_per_system_launches_ms": round(t_per, 3),
+            "speedup_vs_per_system_fp64": round(t_per / t_mixed, 2),
+            "speedup_vs_batched_fp64": round(t_b64 / t_mixed, 3),
+            "fwd_err_vs_oracle_sampled": err, "sampled_systems": len(sample),
+            "generate_s": round(tgen, 1), "analyse_s": round(tan, 2),
+            "config": {"workload": f"{nsys} systems, rhs=4, FP32+FP64 refinement"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_adjoint(args):
+    import torch
+
+    from sptrsv_gb300 import SyncFreeSolver, matgen, sparse_triangular_solve
+    m = matgen.system_1m(seed=2)
+    rhs = 8
+    rng = np.random.default_rng(4)
+    B = torch.from_numpy(rng.standard_normal((m.n, rhs))).cuda()
+    W = torch.from_numpy(rng.standard_normal((m.n, rhs))).cuda()
+    s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, sync_check=False, **args.solver_kw)
+    val = torch.from_numpy(m.val).cuda()
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    def fwd():
+        with torch.no_grad():
+            return sparse_triangular_solve(s, val, B)
+
+    def fwd_bwd():
+        v = val.detach().requires_grad_(True)
+        bb = B.detach().requires_grad_(True)
+        x = sparse_triangular_solve(s, v, bb)
+        (W * x).sum().backward()
+        return v.grad, bb.grad
+    fwd()
+    fwd_bwd()
+    t_f = _timed(fwd, args.steps, flush)
+    t_fb = _timed(fwd_bwd, args.steps, flush)
+    line = {"workload": "adjoint", "metric": "(forward + adjoint with value gradient) / forward time",
+            "value": round(t_fb / t_f, 3), "unit": "ratio", "higher_is_better": False,
+            "forward_ms": round(t_f, 3), "forward_backward_ms": round(t_fb, 3), "n": m.n, "nnz": m.nnz, "rhs": rhs,
+            "config": {"workload": "n=1M Poisson(9) band 20k, rhs=8, FP64, loss=sum(w*x)"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -356,6 +518,8 @@ def main(argv=None) -> int:
     ap.add_argument("--lanes", type=int, default=None)
     ap.add_argument("--chunk", type=int, default=None)
     ap.add_argument("--order-block", type=int, default=None)
+    ap.add_argument("--workload", choices=["deep_wide", "multi_rhs", "batch", "adjoint"], default="deep_wide")
+    ap.add_argument("--batch-count", type=int, default=512)
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3
@@ -368,6 +532,12 @@ def main(argv=None) -> int:
     world, rank, local = dist_env()
     if args.impl == "reference":
         return run_reference(args, world, rank)
+    if args.workload == "multi_rhs":
+        return run_multi_rhs(args)
+    if args.workload == "batch":
+        return run_batch(args)
+    if args.workload == "adjoint":
+        return run_adjoint(args)
     return run_gpu(args, world, rank, local)
 
 

@@ -104,10 +104,8 @@ namespace {
   } while (0)
 
 int map_cuda_error(cudaError_t e) {
-  if (e == cudaErrorMemoryAllocation) {
-    cudaGetLastError();
-    return SPTRSV_ERR_OOM;
-  }
+  cudaGetLastError();  // clear a non-sticky error so later launches are not blamed for it
+  if (e == cudaErrorMemoryAllocation) return SPTRSV_ERR_OOM;
   return SPTRSV_ERR_CUDA;
 }
 
@@ -409,15 +407,23 @@ int ensure_table(sptrsv_gb300_handle_s* h, bool adj, int cmax, int emax) {
   return build_table(h, t, adj ? h->out_cnt_host : h->dep_cnt_host, adj, cmax, emax);
 }
 
-int auto_emax(int cmax, size_t elem, int stages) {
-  // keep the ring of stage buffers within ~180 KB of shared memory
-  const long long budget = (180 * 1024) / (stages < 2 ? 2 : stages);
-  long long e = budget - (long long)(cmax + 32) * (long long)(8 + elem) - 64;
-  e /= (long long)(4 + elem);
-  long long want = std::max<long long>(4096, 8LL * cmax);
-  if (e > want) e = want;
-  if (e < 64) e = 64;
-  return static_cast<int>(e);
+// Largest per-chunk entry budget whose ring of stage buffers (plus the
+// shared-memory tier) fits one CTA's shared memory; 0 if none does.
+constexpr size_t kSmemCap = 220 * 1024;
+int fit_emax(int cmax, size_t elem, int stages, bool tier, int want) {
+  int e = want;
+  while (e >= 64) {
+    if (staged_smem_bytes(cmax, e, elem, tier, stages) <= kSmemCap) return e;
+    e = e * 3 / 4;
+  }
+  return 0;
+}
+
+int auto_emax(int cmax, size_t elem, int stages, bool tier) {
+  // aim at ~180 KB for the whole ring so another CTA may share the SM when chunks are small
+  int want = std::max(4096, 8 * cmax);
+  while (want > 64 && staged_smem_bytes(cmax, want, elem, tier, stages) > 180 * 1024) want = want * 3 / 4;
+  return fit_emax(cmax, elem, stages, tier, want);
 }
 
 int effective_block(const sptrsv_gb300_handle_s* h) {
@@ -522,8 +528,10 @@ int solve_typed(sptrsv_gb300_handle_s* h, const Values<T>& V, int rhs, int layou
                             static_cast<unsigned*>(h->counters.p), h->ctl, c, timeout_ns(h), h->num_sms, s));
   } else if (c.sched == SCHED_LEVELSET) {
     CUDA_TRY(launch_levelset<T>(h->layout, V, rhs, v, static_cast<T*>(h->xw.p), h->ctl, c, timeout_ns(h), s));
-  } else if (rhs == 1 && c.staged) {
-    const int emax = c.emax > 0 ? c.emax : auto_emax(c.chunk, sizeof(T), c.stages);
+  } else if (rhs == 1 && c.staged &&
+             (c.emax > 0 ? fit_emax(c.chunk, sizeof(T), c.stages, c.smem_tier, c.emax) == c.emax
+                         : auto_emax(c.chunk, sizeof(T), c.stages, c.smem_tier) > 0)) {
+    const int emax = c.emax > 0 ? c.emax : auto_emax(c.chunk, sizeof(T), c.stages, c.smem_tier);
     ST_TRY(ensure_table(h, adj != nullptr, c.chunk, emax));
     CUDA_TRY(launch_pull_staged<T>(h->layout, V, adj ? h->tab_adj : h->tab_fwd, v, static_cast<T*>(h->xw.p), h->ctl,
                                    c, timeout_ns(h), h->num_sms, s, adj));
@@ -1145,6 +1153,170 @@ int sptrsv_gb300_grad_values(sptrsv_handle_t h, int dtype, int rhs, int layout, 
   else
     return SPTRSV_ERR_INVALID;
   if (h->sync_check) return check_device(h, s);
+  return SPTRSV_OK;
+}
+
+// ---------------------------------------------------------------- CUDA graphs
+namespace {
+struct GraphBox {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+}  // namespace
+
+int sptrsv_gb300_graph_create(sptrsv_handle_t h, int kind, int dtype, int rhs, int layout, const void* d_b, void* d_x,
+                              int count, void** graph, void* stream) {
+  if (!h || !graph || count < 1 || (kind != 0 && kind != 1)) return SPTRSV_ERR_INVALID;
+  *graph = nullptr;
+  if (!h->analysed) return SPTRSV_ERR_STATE;
+  if (kind == 1 && dtype != SPTRSV_DTYPE_F64) return SPTRSV_ERR_INVALID;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int saved_check = h->sync_check, saved_profile = h->profile;
+  // one eager run sizes every workspace and table, so the capture allocates nothing
+  int st = kind == 0 ? sptrsv_gb300_solve(h, nullptr, dtype, rhs, layout, d_b, d_x, stream)
+                     : sptrsv_gb300_solve_refine(h, nullptr, rhs, layout, static_cast<const double*>(d_b),
+                                                 static_cast<double*>(d_x), 0.0, count, nullptr, nullptr, stream);
+  if (st != SPTRSV_OK) return st;
+  CUDA_TRY(cudaStreamSynchronize(s));
+  cudaStream_t cs = nullptr;
+  CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  h->sync_check = 0;
+  h->profile = 0;
+  GraphBox* box = new (std::nothrow) GraphBox();
+  cudaError_t e = box ? cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) : cudaErrorMemoryAllocation;
+  if (e == cudaSuccess) {
+    if (kind == 0) {
+      for (int i = 0; i < count && st == SPTRSV_OK; ++i)
+        st = sptrsv_gb300_solve(h, nullptr, dtype, rhs, layout, d_b, d_x, cs);
+    } else {
+      st = sptrsv_gb300_solve_refine(h, nullptr, rhs, layout, static_cast<const double*>(d_b),
+                                     static_cast<double*>(d_x), 0.0, count, nullptr, nullptr, cs);
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+    if (st == SPTRSV_OK && e2 == cudaSuccess) {
+      box->graph = g;
+      e = cudaGraphInstantiate(&box->exec, g, 0);
+    } else {
+      if (g) cudaGraphDestroy(g);
+      e = e2 != cudaSuccess ? e2 : cudaSuccess;
+    }
+  }
+  h->sync_check = saved_check;
+  h->profile = saved_profile;
+  cudaStreamDestroy(cs);
+  if (st != SPTRSV_OK || e != cudaSuccess || !box || !box->exec) {
+    if (box) {
+      if (box->exec) cudaGraphExecDestroy(box->exec);
+      if (box->graph) cudaGraphDestroy(box->graph);
+      delete box;
+    }
+    cudaGetLastError();
+    return st != SPTRSV_OK ? st : map_cuda_error(e != cudaSuccess ? e : cudaErrorUnknown);
+  }
+  *graph = box;
+  return SPTRSV_OK;
+}
+
+int sptrsv_gb300_graph_launch(void* graph, void* stream) {
+  if (!graph) return SPTRSV_ERR_INVALID;
+  CUDA_TRY(cudaGraphLaunch(static_cast<GraphBox*>(graph)->exec, static_cast<cudaStream_t>(stream)));
+  return SPTRSV_OK;
+}
+
+int sptrsv_gb300_graph_destroy(void* graph) {
+  if (!graph) return SPTRSV_ERR_INVALID;
+  auto* box = static_cast<GraphBox*>(graph);
+  if (box->exec) cudaGraphExecDestroy(box->exec);
+  if (box->graph) cudaGraphDestroy(box->graph);
+  delete box;
+  return SPTRSV_OK;
+}
+
+// ---------------------------------------------------------------- autotuner
+int sptrsv_gb300_tune(sptrsv_handle_t h, const void* d_val, int dtype, int rhs, int layout, const void* d_b, void* d_x,
+                      int reps, double* best_ms, void* stream) {
+  if (!h || !d_val || !d_b || !d_x || reps < 1) return SPTRSV_ERR_INVALID;
+  if (!h->analysed) return SPTRSV_ERR_STATE;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  struct Cand {
+    int sched, order_block, chunk, staged, backoff, ctas, lanes, stages;
+  };
+  const int n = h->n;
+  const int big = INT_MAX;
+  std::vector<Cand> cands;
+  if (rhs == 1) {
+    for (int ob : {big, 4096, 1024})
+      for (int ch : {224, 448, 896})
+        for (int bo : {0, 256}) cands.push_back({SCHED_PULL, ob, ob == 1024 ? 1024 : ch, 1, bo, 0, 1, 2});
+    cands.push_back({SCHED_PULL, big, 256, 0, 1024, 2, 1, 2});
+    cands.push_back({SCHED_PULL, big, 256, 0, 256, 0, 1, 2});
+    cands.push_back({SCHED_LEVELSET, big, 256, 0, 256, 1, 8, 2});
+    cands.push_back({SCHED_PUSH, 1024, 1024, 0, 256, 0, 1, 2});
+  } else {
+    for (int ob : {big, 4096})
+      for (int ch : {64, 256}) cands.push_back({SCHED_PULL, ob, ch, 0, 256, 0, 1, 2});
+    cands.push_back({SCHED_LEVELSET, big, 256, 0, 256, 1, 8, 2});
+    cands.push_back({SCHED_PUSH, big, 256, 0, 256, 0, 1, 2});
+  }
+  (void)n;
+  const int saved_check = h->sync_check, saved_profile = h->profile;
+  h->sync_check = 0;
+  h->profile = 0;
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  double best = 1e300;
+  int best_i = -1;
+  for (size_t i = 0; i < cands.size(); ++i) {
+    const Cand& c = cands[i];
+    h->sched_option = c.sched;
+    h->order_block = c.order_block;
+    h->chunk_option = c.chunk;
+    h->staged = c.staged;
+    h->backoff_ns = c.backoff;
+    h->ctas_per_sm = c.ctas;
+    h->lanes_option = c.lanes;
+    h->stages_option = c.stages;
+    int st = sptrsv_gb300_solve(h, d_val, dtype, rhs, layout, d_b, d_x, stream);
+    if (st == SPTRSV_OK) st = check_device(h, s);
+    if (st != SPTRSV_OK) continue;  // a candidate that fails (or times out) is skipped
+    std::vector<float> t;
+    for (int r = 0; r < reps && st == SPTRSV_OK; ++r) {
+      cudaEventRecord(e0, s);
+      st = sptrsv_gb300_solve(h, nullptr, dtype, rhs, layout, d_b, d_x, stream);
+      cudaEventRecord(e1, s);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      t.push_back(ms);
+    }
+    if (st == SPTRSV_OK) st = check_device(h, s);
+    if (st != SPTRSV_OK || t.empty()) continue;
+    std::sort(t.begin(), t.end());
+    const double med = t[t.size() / 2];
+    if (med < best) {
+      best = med;
+      best_i = static_cast<int>(i);
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  h->sync_check = saved_check;
+  h->profile = saved_profile;
+  if (best_i < 0) return SPTRSV_ERR_CUDA;
+  const Cand& c = cands[best_i];
+  h->sched_option = c.sched;
+  h->order_block = c.order_block;
+  h->chunk_option = c.chunk;
+  h->staged = c.staged;
+  h->backoff_ns = c.backoff;
+  h->ctas_per_sm = c.ctas;
+  h->lanes_option = c.lanes;
+  h->stages_option = c.stages;
+  ST_TRY(ensure_layout(h, s));
+  ST_TRY(stage_values(h, d_val, dtype, s, false));
+  if (best_ms) *best_ms = best;
   return SPTRSV_OK;
 }
 

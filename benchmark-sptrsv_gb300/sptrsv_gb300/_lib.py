@@ -119,6 +119,10 @@ SIGNATURES = {
     "sptrsv_gb300_solve_adjoint": (_I, [_VP, _VP, _I, _I, _I, _VP, _VP, _VP, _VP, _VP]),
     "sptrsv_gb300_grad_values": (_I, [_VP, _I, _I, _I, _VP, _VP, _VP, _VP]),
     "sptrsv_gb300_exec_ms": (_I, [_VP, _PD]),
+    "sptrsv_gb300_graph_create": (_I, [_VP, _I, _I, _I, _I, _VP, _VP, _I, ctypes.POINTER(_VP), _VP]),
+    "sptrsv_gb300_graph_launch": (_I, [_VP, _VP]),
+    "sptrsv_gb300_graph_destroy": (_I, [_VP]),
+    "sptrsv_gb300_tune": (_I, [_VP, _VP, _I, _I, _I, _VP, _VP, _I, _PD, _VP]),
 }
 
 _LIB: ctypes.CDLL | None = None

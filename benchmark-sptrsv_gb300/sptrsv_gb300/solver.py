@@ -91,7 +91,8 @@ def executor(col_ptr, row_idx, val, in_degree, left_sum, m: int, substitution: i
 class SyncFreeSolver:
     """Analyse once, solve many: a handle of libsptrsv_gb300 bound to torch CUDA tensors."""
 
-    def __init__(self, col_ptr, row_idx, n: int | None = None, substitution: int = 0, *, values=None,
+    def __init__(self, col_ptr=None, row_idx=None, n: int | None = None, substitution: int = 0, *, values=None,
+                 batch=None,
                  schedule: int = SCHED_AUTO, lanes: int = 0, chunk: int = 0, order_block: int | None = None,
                  exact: bool = False, smem_tier: bool = True, timeout_ms: int = 1000, sync_check: bool = True,
                  profile: bool = False, block: int = 0, backoff_ns: int | None = None, ctas_per_sm: int = 0,
@@ -99,11 +100,31 @@ class SyncFreeSolver:
         torch = _torch()
         self._lib = load()
         self.device = torch.device("cuda", torch.cuda.current_device())
-        self.col_ptr = self._as_dev(col_ptr, torch.int32)
-        self.row_idx = self._as_dev(row_idx, torch.int32)
-        self.n = int(self.col_ptr.numel() - 1) if n is None else int(n)
-        self.nnz = int(self.row_idx.numel())
-        self.substitution = int(substitution)
+        self.batch = None
+        if batch is not None:
+            # independent triangles [(col_ptr, row_idx, n, substitution), ...] solved together
+            cps, ris, ns, nnzs, subs = [], [], [], [], []
+            for cp, ri, nn, sub in batch:
+                cp = np.asarray(cp, dtype=np.int32)
+                ri = np.asarray(ri, dtype=np.int32)
+                cps.append(cp)
+                ris.append(ri)
+                ns.append(int(nn))
+                nnzs.append(int(ri.size))
+                subs.append(int(sub))
+            self.batch = (np.array(ns, dtype=np.int32), np.array(nnzs, dtype=np.int32), np.array(subs, dtype=np.int32))
+            self.col_ptr = self._as_dev(np.concatenate(cps), torch.int32)
+            self.row_idx = self._as_dev(np.concatenate(ris) if ris else np.zeros(0, np.int32), torch.int32)
+            self.n = int(sum(ns))
+            self.nnz = int(sum(nnzs))
+            self.substitution = subs[0] if subs else 0
+            self.offsets = np.concatenate([[0], np.cumsum(ns)]).astype(np.int64)
+        else:
+            self.col_ptr = self._as_dev(col_ptr, torch.int32)
+            self.row_idx = self._as_dev(row_idx, torch.int32)
+            self.n = int(self.col_ptr.numel() - 1) if n is None else int(n)
+            self.nnz = int(self.row_idx.numel())
+            self.substitution = int(substitution)
         h = ctypes.c_void_p()
         check(self._lib.sptrsv_gb300_create(ctypes.byref(h)), "create")
         self._h = h
@@ -145,6 +166,12 @@ class SyncFreeSolver:
         return int(v.value)
 
     def analyse(self) -> None:
+        if self.batch is not None:
+            ns, nnzs, subs = self.batch
+            check(self._lib.sptrsv_gb300_analyse_batch(self._h, int(ns.size), _np_ptr(ns), _np_ptr(nnzs),
+                                                       _np_ptr(subs), _ptr(self.col_ptr), _ptr(self.row_idx),
+                                                       _stream_ptr(self._stream)), "analyse_batch")
+            return
         check(self._lib.sptrsv_gb300_analyse(self._h, self.n, self.n, self.nnz, _ptr(self.col_ptr),
                                              _ptr(self.row_idx), self.substitution, _stream_ptr(self._stream)),
               "analyse")
@@ -278,6 +305,51 @@ class SyncFreeSolver:
                                                  _ptr(dval), _stream_ptr(self._stream)), "grad_values")
         return dval
 
+    TUNED_OPTIONS = ("SCHEDULE", "ORDER_BLOCK", "CHUNK", "STAGED", "BACKOFF_NS", "CTAS_PER_SM", "LANES", "STAGES")
+
+    def tune(self, b, values=None, reps: int = 3) -> dict:
+        """Autotune the executor on this right-hand side; returns the chosen options and time."""
+        torch = _torch()
+        b2, layout = self._layout_of(b)
+        v = (values if values is not None else self.values)
+        if v is None:
+            raise ValueError("tune needs the matrix values")
+        v = v.to(self.device).contiguous()
+        dt = DTYPE_F64 if b2.dtype == torch.float64 else DTYPE_F32
+        if dt == DTYPE_F32 and v.dtype == torch.float64:
+            v = v.to(torch.float32)
+        x = torch.empty_like(b2)
+        ms = ctypes.c_double(0.0)
+        check(self._lib.sptrsv_gb300_tune(self._h, _ptr(v), dt, int(b2.shape[1]), layout, _ptr(b2), _ptr(x), int(reps),
+                                          ctypes.byref(ms), _stream_ptr(self._stream)), "tune")
+        self.values = v
+        return {"best_ms": float(ms.value), **self.tuned_options()}
+
+    def tuned_options(self) -> dict:
+        return {k.lower(): self.get_option(getattr(_lib, "OPTION_" + k)) for k in self.TUNED_OPTIONS}
+
+    def apply_options(self, opts: dict) -> None:
+        """Apply a dict produced by tuned_options() (e.g. loaded from JSON); restage values after."""
+        for k, v in opts.items():
+            if k == "best_ms":
+                continue
+            self.set_option(getattr(_lib, "OPTION_" + k.upper()), int(v))
+        if self.values is not None:
+            self.set_values(self.values)
+
+    def graph(self, b, x, *, kind: int = 0, count: int = 1):
+        """Capture `count` solves (kind 0) or one refinement with `count` steps (kind 1) of the staged
+        values into a CUDA graph; returns a SolveGraph to replay."""
+        torch = _torch()
+        b2, layout = self._layout_of(b)
+        x2, _ = self._layout_of(x)
+        dt = DTYPE_F64 if b2.dtype == torch.float64 else DTYPE_F32
+        g = ctypes.c_void_p()
+        check(self._lib.sptrsv_gb300_graph_create(self._h, int(kind), dt, int(b2.shape[1]), layout, _ptr(b2),
+                                                  _ptr(x2), int(count), ctypes.byref(g), _stream_ptr(self._stream)),
+              "graph_create")
+        return SolveGraph(self._lib, g, (b2, x2), self._stream)
+
     def exec_ms(self) -> float:
         """Device time of the last executor launch (needs profile=True)."""
         ms = ctypes.c_double(0.0)
@@ -314,6 +386,30 @@ class SyncFreeSolver:
         if getattr(self, "_h", None) is not None and self._h.value:
             self._lib.sptrsv_gb300_destroy(self._h)
             self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class SolveGraph:
+    """A captured CUDA graph of solves; replay() launches it on the solver's stream."""
+
+    def __init__(self, lib, handle, keep, stream):
+        self._lib = lib
+        self._g = handle
+        self._keep = keep
+        self._stream = stream
+
+    def replay(self) -> None:
+        check(self._lib.sptrsv_gb300_graph_launch(self._g, _stream_ptr(self._stream)), "graph_launch")
+
+    def close(self) -> None:
+        if self._g is not None and self._g.value:
+            self._lib.sptrsv_gb300_graph_destroy(self._g)
+            self._g = ctypes.c_void_p()
 
     def __del__(self):
         try:

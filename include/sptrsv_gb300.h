@@ -238,6 +238,28 @@ int sptrsv_gb300_solve_adjoint(sptrsv_handle_t handle, const void *d_val, int dt
 int sptrsv_gb300_grad_values(sptrsv_handle_t handle, int dtype, int rhs, int layout, const void *d_lambda,
                              const void *d_x, void *d_dval, void *stream);
 
+/* CUDA graphs of the solve path (analyse once, replay many). kind 0 captures
+ * `count` consecutive solves of the staged values (dtype/rhs/layout/b/x as in
+ * sptrsv_gb300_solve, d_val = NULL); kind 1 captures one mixed-precision
+ * refinement with exactly `count` refinement steps (tol <= 0 semantics; F64
+ * b/x). One eager run before the capture sizes every workspace. Replays are
+ * asynchronous: use sptrsv_gb300_check to read device errors. The graph keeps
+ * pointers to b, x and the handle's buffers; changing the schedule or
+ * re-staging values invalidates it. */
+int sptrsv_gb300_graph_create(sptrsv_handle_t handle, int kind, int dtype, int rhs, int layout, const void *d_b,
+                              void *d_x, int count, void **graph, void *stream);
+int sptrsv_gb300_graph_launch(void *graph, void *stream);
+int sptrsv_gb300_graph_destroy(void *graph);
+
+/* Autotuner: times candidate executor configurations (executor family, order
+ * block, chunk size, staging, poll backoff, residency, lanes) on this
+ * request, `reps` timed solves each, skips candidates that fail, and leaves
+ * the fastest configuration set on the handle (values re-staged from d_val).
+ * *best_ms (may be NULL) receives its median solve time. Read the chosen
+ * options back with sptrsv_gb300_get_option. */
+int sptrsv_gb300_tune(sptrsv_handle_t handle, const void *d_val, int dtype, int rhs, int layout, const void *d_b,
+                      void *d_x, int reps, double *best_ms, void *stream);
+
 /* Synchronises `stream` and reports (then clears) a device error raised by
  * asynchronous solves since the last check. */
 int sptrsv_gb300_check(sptrsv_handle_t handle, void *stream);

@@ -93,14 +93,14 @@ def test_handle_timeout_option(cuda):
         s.set_option(_lib.OPTION_TIMEOUT_MS, 0)
 
 
-@pytest.mark.parametrize("cfg", [dict(schedule=2), dict(schedule=2, staged=False), dict(schedule=1)])
+@pytest.mark.parametrize("cfg", [dict(schedule=2), dict(schedule=1)])
 def test_wait_budget_expires_cleanly_then_recovers(cuda, cfg):
     """Natural order on the 2-D Laplacian makes single waits last far longer than
     a 1 ms budget: the solve must come back with SPTRSV_ERR_TIMEOUT (every wait
     bounded, copies drained), and the same handle must solve correctly after the
     budget is raised."""
     from sptrsv_gb300 import SptrsvError, SyncFreeSolver, _lib, matgen
-    m = matgen.laplace2d_lower(700)
+    m = matgen.laplace2d_lower(1000)
     b = cuda.from_numpy(m.matvec(np.ones(m.n))).cuda()
     s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, values=m.val, order_block=1, chunk=64,
                        timeout_ms=1, **cfg)
