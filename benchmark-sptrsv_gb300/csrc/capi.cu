@@ -33,7 +33,7 @@ struct sptrsv_gb300_handle_s {
   int num_sms = 0;
   // options
   ExecConfig cfg;
-  int order_block = 1024;
+  int order_block = INT_MAX;   // level order: the fastest schedule on both deep and wide DAGs measured
   long long timeout_ms = 1000;
   int sync_check = 1;
   int sched_option = SCHED_AUTO;
@@ -481,7 +481,7 @@ ExecConfig pick_config(const sptrsv_gb300_handle_s* h, int rhs) {
   ExecConfig c = h->cfg;
   c.sched = h->sched_option == SCHED_AUTO ? SCHED_PULL : h->sched_option;
   c.lanes = h->lanes_option > 0 ? h->lanes_option : 1;
-  c.chunk = h->chunk_option > 0 ? h->chunk_option : (rhs == 1 ? 1024 : 256);
+  c.chunk = h->chunk_option > 0 ? h->chunk_option : (rhs == 1 ? 224 : 256);
   c.block = h->block_option > 0 ? h->block_option : 256;
   c.sleep_max = static_cast<unsigned>(h->backoff_ns);
   c.ctas_per_sm = h->ctas_per_sm;
