@@ -57,6 +57,8 @@ OPTION_STAGED = 12
 OPTION_STAGE_ENTRIES = 13
 OPTION_STAGES = 14
 
+NOALLOC_MAX_N = 262144  # SPTRSV_NOALLOC_MAX_N
+
 
 class SptrsvError(RuntimeError):
     """A non-zero sptrsv_status returned by the library."""
@@ -123,6 +125,7 @@ SIGNATURES = {
     "sptrsv_gb300_graph_launch": (_I, [_VP, _VP]),
     "sptrsv_gb300_graph_destroy": (_I, [_VP]),
     "sptrsv_gb300_tune": (_I, [_VP, _VP, _I, _I, _I, _VP, _VP, _I, _PD, _VP]),
+    "sptrsv_gb300_solve_noalloc": (_I, [_VP, _VP, _VP, _I, _I, _I, _VP, _VP, _VP]),
 }
 
 _LIB: ctypes.CDLL | None = None

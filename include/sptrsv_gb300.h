@@ -260,6 +260,28 @@ int sptrsv_gb300_graph_destroy(void *graph);
 int sptrsv_gb300_tune(sptrsv_handle_t handle, const void *d_val, int dtype, int rhs, int layout, const void *d_b,
                       void *d_x, int reps, double *best_ms, void *stream);
 
+/* ---------------------------------------------------------------------------
+ * Allocation-free solve. No counterpart in the reference: it exists for
+ * callers that may not allocate device memory themselves — code running
+ * under a host framework that owns the whole device-memory budget (every
+ * byte must come from its allocator or pool) and latency-critical loops that
+ * cannot accept the device-wide synchronisation a cudaMalloc/cudaFree can
+ * imply. One forward or backward FP64 solve with one right-hand side on a
+ * CSC triangle (device pointers, reference conventions), using the
+ * kernel-level analyser and executor with all scratch (counters, partial
+ * sums, control words) in a fixed device array inside the library, sized for
+ * at most SPTRSV_NOALLOC_MAX_N unknowns (about 3 MB, held by every GPU that
+ * loads the library until the process exits). Larger n returns
+ * SPTRSV_ERR_UNSUPPORTED. The first call on a device looks up the array's
+ * address (once per device); make it before any stream capture. All calls
+ * share the array and each clears it before use, so calls whose GPU work
+ * overlaps race: serialise them. Synchronises `stream`; returns
+ * SPTRSV_ERR_TIMEOUT if a bounded device wait ran out. Allocates nothing.
+ * ------------------------------------------------------------------------- */
+#define SPTRSV_NOALLOC_MAX_N 262144
+int sptrsv_gb300_solve_noalloc(const int *d_colPtr, const int *d_rowIdx, const double *d_val, int n, int nnz,
+                               int substitution, const double *d_b, double *d_x, void *stream);
+
 /* Synchronises `stream` and reports (then clears) a device error raised by
  * asynchronous solves since the last check. */
 int sptrsv_gb300_check(sptrsv_handle_t handle, void *stream);
