@@ -146,36 +146,13 @@ __global__ void __launch_bounds__(256) k_pull_vec(ExecArgs<T> a) {
       const T bi = a.b[(long long)row * a.b_si];
       T acc = T(0);
       if (!EXACT && lane == 0) acc = bi * a.rcp[p];
-      for (int eb = e0 + lane; eb < e1 && !fail; eb += G * U) {
-        int q[U];
-        T w[U];
-        Bits bits[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int e = eb + u * G;
-          q[u] = e < e1 ? lpos[e] : -1;
-          w[u] = e < e1 ? vals[e] : T(0);
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          bits[u] = F::EMPTY;
-          if (q[u] >= 0) {
-            const int qr = ADJ ? last - q[u] : q[u];
-            bits[u] = (a.smem_tier && qr >= base) ? F::load_shared(&s_x[qr - base]) : F::load(&a.xw[q[u]]);
-          }
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          if (q[u] < 0 || fail) continue;
-          if (bits[u] == F::EMPTY) {
-            const int qr = ADJ ? last - q[u] : q[u];
-            bits[u] = (a.smem_tier && qr >= base) ? wait_flag<T, true>(&s_x[qr - base], a.ctl, a.timeout_ns, p, a.sleep_min, a.sleep_max)
-                                                  : wait_flag<T, false>(&a.xw[q[u]], a.ctl, a.timeout_ns, p, a.sleep_min, a.sleep_max);
-            if (bits[u] == F::EMPTY) { fail = true; continue; }
-          }
-          acc = EXACT ? mul_add<T>(acc, w[u], F::value(bits[u]), true) : fma(-w[u], F::value(bits[u]), acc);
-        }
-      }
+      auto slot = [&](int q) {
+        const int qr = ADJ ? last - q : q;
+        return (a.smem_tier && qr >= base) ? qr - base : -1;
+      };
+      if (!gather_deps<T, EXACT, U, G>(lpos, vals, e0 + lane, e1, a.xw, s_x, slot, a.ctl, a.timeout_ns, p,
+                                       a.sleep_min, a.sleep_max, acc))
+        fail = true;
       if (G > 1) {
         fail = __any_sync(gmask, fail);
 #pragma unroll
@@ -238,23 +215,69 @@ __global__ void __launch_bounds__(256) k_pull_multi(ExecArgs<T> a) {
           const int k = kt + lane + j * G;
           acc[j] = (!EXACT && k < rhs) ? a.b[(long long)row * a.b_si + (long long)k * a.b_sk] * rc : T(0);
         }
-        for (int e = e0; e < e1 && !fail; ++e) {
-          const int q = lpos[e];
-          const int qr = ADJ ? last - q : q;
-          const T v = vals[e];
-          const bool local = a.smem_tier && qr >= base;
+        // dependencies in batches of UD: all flag loads of a batch (every dependency x every
+        // right-hand side this lane covers) are issued together and re-polled together
+        constexpr int UD = 4;
+        for (int eb = e0; eb < e1 && !fail; eb += UD) {
+          int q[UD], sl[UD];
+          T v[UD];
+          typename F::Bits bits[UD][RPL];
+          unsigned todo = 0u;
 #pragma unroll
-          for (int j = 0; j < RPL; ++j) {
-            const int k = kt + lane + j * G;
-            if (k < rhs && !fail) {
-              typename F::Bits bits;
-              if (local)
-                bits = wait_flag<T, true>(&s_x[(long long)(qr - base) * rhs + k], a.ctl, a.timeout_ns, p, a.sleep_min, a.sleep_max);
-              else
-                bits = wait_flag<T, false>(&a.xw[(long long)q * rhs + k], a.ctl, a.timeout_ns, p, a.sleep_min, a.sleep_max);
-              if (bits == F::EMPTY) fail = true;
-              else acc[j] = EXACT ? mul_add<T>(acc[j], v, F::value(bits), true) : fma(-v, F::value(bits), acc[j]);
+          for (int u = 0; u < UD; ++u) {
+            q[u] = eb + u < e1 ? lpos[eb + u] : -1;
+            v[u] = eb + u < e1 ? vals[eb + u] : T(0);
+            const int qr = ADJ ? last - q[u] : q[u];
+            sl[u] = (q[u] >= 0 && a.smem_tier && qr >= base) ? qr - base : -1;
+          }
+#pragma unroll
+          for (int u = 0; u < UD; ++u)
+#pragma unroll
+            for (int j = 0; j < RPL; ++j) {
+              const int k = kt + lane + j * G;
+              bits[u][j] = F::EMPTY;
+              if (q[u] >= 0 && k < rhs) {
+                bits[u][j] = sl[u] >= 0 ? F::load_shared(&s_x[(long long)sl[u] * rhs + k])
+                                        : F::load(&a.xw[(long long)q[u] * rhs + k]);
+                todo |= 1u << (u * RPL + j);
+              }
             }
+          WaitBudget wb(a.timeout_ns);
+          unsigned nap = a.sleep_min;
+          for (;;) {
+            bool global_pending = false;
+#pragma unroll
+            for (int j = 0; j < RPL; ++j) {
+              bool prefix = true;
+#pragma unroll
+              for (int u = 0; u < UD; ++u) {
+                const unsigned bit = 1u << (u * RPL + j);
+                if (!(todo & bit)) continue;
+                if (bits[u][j] != F::EMPTY && (!EXACT || prefix)) {
+                  acc[j] = EXACT ? mul_add<T>(acc[j], v[u], F::value(bits[u][j]), true)
+                                 : fma(-v[u], F::value(bits[u][j]), acc[j]);
+                  todo &= ~bit;
+                } else {
+                  prefix = false;
+                  if (bits[u][j] == F::EMPTY && sl[u] < 0) global_pending = true;
+                }
+              }
+            }
+            if (!todo) break;
+            if (global_pending && a.sleep_max) {
+              __nanosleep(nap);
+              nap = nap * 2u < a.sleep_max ? nap * 2u : a.sleep_max;
+            }
+            if (!wb.poll(a.ctl, p)) { fail = true; break; }
+#pragma unroll
+            for (int u = 0; u < UD; ++u)
+#pragma unroll
+              for (int j = 0; j < RPL; ++j) {
+                const int k = kt + lane + j * G;
+                if ((todo & (1u << (u * RPL + j))) && bits[u][j] == F::EMPTY)
+                  bits[u][j] = sl[u] >= 0 ? F::load_shared(&s_x[(long long)sl[u] * rhs + k])
+                                          : F::load(&a.xw[(long long)q[u] * rhs + k]);
+              }
           }
         }
         fail = __any_sync(gmask, fail);

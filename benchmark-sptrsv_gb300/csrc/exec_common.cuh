@@ -57,4 +57,72 @@ __device__ __forceinline__ float exact_finish<float>(float bi, float acc, float 
   return __fdiv_rn(__fsub_rn(bi, acc), diag);
 }
 
+// Accumulates the dependencies e = e_first, e_first + STRIDE, ... < e_end of
+// one unknown into acc: acc -= w_e * x_q (any order), or with EXACT the serial
+// executor's product-then-sum in list order. The index/value loads and the
+// flag loads of U dependencies are issued together; every dependency still
+// unpublished is re-polled together on each retry, so once the last one is
+// published the wait ends within one poll round trip, whatever the list
+// length. local_slot(q) gives the shared-memory slot of an in-chunk
+// dependency, or -1 for one read from global memory (which backs off between
+// polls, sleep_min..sleep_max ns). Returns false on timeout / failure.
+template <typename T, bool EXACT, int U, int STRIDE, class LocalSlot>
+__device__ __forceinline__ bool gather_deps(const int* __restrict__ pos, const T* __restrict__ val, int e_first,
+                                            int e_end, const T* xw, const T* s_x, LocalSlot local_slot,
+                                            DeviceCtl* ctl, unsigned long long timeout, int where,
+                                            unsigned sleep_min, unsigned sleep_max, T& acc) {
+  using F = Flag<T>;
+  using Bits = typename F::Bits;
+  for (int e = e_first; e < e_end; e += U * STRIDE) {
+    int q[U], ls[U];
+    T w[U];
+    Bits bits[U];
+    unsigned todo = 0u;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int ee = e + u * STRIDE;
+      q[u] = ee < e_end ? pos[ee] : -1;
+      w[u] = ee < e_end ? val[ee] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      ls[u] = -1;
+      bits[u] = F::EMPTY;
+      if (q[u] >= 0) {
+        ls[u] = local_slot(q[u]);
+        bits[u] = ls[u] >= 0 ? F::load_shared(&s_x[ls[u]]) : F::load(&xw[q[u]]);
+        todo |= 1u << u;
+      }
+    }
+    WaitBudget wb(timeout);
+    unsigned nap = sleep_min;
+    for (;;) {
+      bool prefix = true;
+      unsigned global_pending = 0u;
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (!(todo & (1u << u))) continue;
+        if (bits[u] != F::EMPTY && (!EXACT || prefix)) {
+          acc = EXACT ? exact_mul_add<T>(acc, w[u], F::value(bits[u])) : fma(-w[u], F::value(bits[u]), acc);
+          todo &= ~(1u << u);
+        } else {
+          prefix = false;
+          if (bits[u] == F::EMPTY && ls[u] < 0) global_pending |= 1u << u;
+        }
+      }
+      if (!todo) break;
+      if (global_pending && sleep_max) {
+        __nanosleep(nap);
+        nap = nap * 2u < sleep_max ? nap * 2u : sleep_max;
+      }
+      if (!wb.poll(ctl, where)) return false;
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        if ((todo & (1u << u)) && bits[u] == F::EMPTY)
+          bits[u] = ls[u] >= 0 ? F::load_shared(&s_x[ls[u]]) : F::load(&xw[q[u]]);
+    }
+  }
+  return true;
+}
+
 }  // namespace sptrsv

@@ -292,8 +292,9 @@ __global__ void __launch_bounds__(256) k_pull_staged(StagedArgs<T> a) {
       const int len = hi - lo;
       auto pos_of = [&](int i) { return ADJ ? hi - 1 - i : lo + i; };
       auto is_local = [&](int q) { return ADJ ? (q < hi) : (q >= lo); };
+      const bool tier = a.smem_tier != 0;
+      auto slot = [&](int q) { return (tier && (ADJ ? q < hi : q >= lo)) ? q - lo : -1; };
       if (EXACT || info.mode == 0) {
-        constexpr int U = 8;
         const bool from_smem = info.mode != 2;
         const int* vpos = from_smem ? spos : a.lpos;
         const T* vval = from_smem ? sval : a.lval;
@@ -306,34 +307,11 @@ __global__ void __launch_bounds__(256) k_pull_staged(StagedArgs<T> a) {
           const T bi = a.b[(long long)row * a.b_si];
           const T sc = ssc[li];
           T acc = EXACT ? T(0) : bi * sc;
-          for (int e = ea; e < eb && !fail; e += U) {
-            int q[U];
-            T w[U];
-            Bits bits[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-              q[u] = e + u < eb ? vpos[e + u] : -1;
-              w[u] = e + u < eb ? vval[e + u] : T(0);
-            }
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-              bits[u] = F::EMPTY;
-              if (q[u] >= 0)
-                bits[u] = (a.smem_tier && is_local(q[u])) ? F::load_shared(&s_x[q[u] - lo]) : F::load(&a.xw[q[u]]);
-            }
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-              if (q[u] < 0 || fail) continue;
-              if (bits[u] == F::EMPTY) {
-                bits[u] = (a.smem_tier && is_local(q[u]))
-                              ? wait_flag_dev<T, true>(&s_x[q[u] - lo], a.ctl, a.timeout_ns, p, 0, 0)
-                              : wait_flag_dev<T, false>(&a.xw[q[u]], a.ctl, a.timeout_ns, p, a.sleep_min, a.sleep_max);
-                if (bits[u] == F::EMPTY) { fail = true; continue; }
-              }
-              acc = EXACT ? exact_mul_add<T>(acc, w[u], F::value(bits[u])) : fma(-w[u], F::value(bits[u]), acc);
-            }
+          if (!gather_deps<T, EXACT, 8, 1>(vpos, vval, ea, eb, a.xw, s_x, slot, a.ctl, a.timeout_ns, p, a.sleep_min,
+                                           a.sleep_max, acc)) {
+            fail = true;
+            break;
           }
-          if (fail) break;
           const T xi = EXACT ? exact_finish<T>(bi, acc, sc) : acc;
           if (a.smem_tier) F::store_shared(&s_x[li], xi);
           F::store(&a.xw[p], xi);
@@ -346,7 +324,6 @@ __global__ void __launch_bounds__(256) k_pull_staged(StagedArgs<T> a) {
         }
       } else {
         // one warp per unknown; lanes over its dependency list
-        constexpr int U = 2;
         const bool from_smem = info.mode == 1;
         for (int i = cw; i < len && !fail; i += nconsumer_warps) {
           const int p = pos_of(i);
@@ -359,34 +336,9 @@ __global__ void __launch_bounds__(256) k_pull_staged(StagedArgs<T> a) {
           const T bi = a.b[(long long)row * a.b_si];
           const T sc = ssc[li];
           T acc = lane == 0 ? bi * sc : T(0);
-          for (int e = ea + lane; e < eb && !fail; e += 32 * U) {
-            int q[U];
-            T w[U];
-            Bits bits[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-              const int ee = e + u * 32;
-              q[u] = ee < eb ? vpos[ee] : -1;
-              w[u] = ee < eb ? vval[ee] : T(0);
-            }
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-              bits[u] = F::EMPTY;
-              if (q[u] >= 0)
-                bits[u] = (a.smem_tier && is_local(q[u])) ? F::load_shared(&s_x[q[u] - lo]) : F::load(&a.xw[q[u]]);
-            }
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-              if (q[u] < 0 || fail) continue;
-              if (bits[u] == F::EMPTY) {
-                bits[u] = (a.smem_tier && is_local(q[u]))
-                              ? wait_flag_dev<T, true>(&s_x[q[u] - lo], a.ctl, a.timeout_ns, p, 0, 0)
-                              : wait_flag_dev<T, false>(&a.xw[q[u]], a.ctl, a.timeout_ns, p, a.sleep_min, a.sleep_max);
-                if (bits[u] == F::EMPTY) { fail = true; continue; }
-              }
-              acc = fma(-w[u], F::value(bits[u]), acc);
-            }
-          }
+          if (!gather_deps<T, false, 2, 32>(vpos, vval, ea + lane, eb, a.xw, s_x, slot, a.ctl, a.timeout_ns, p,
+                                            a.sleep_min, a.sleep_max, acc))
+            fail = true;
           fail = __any_sync(0xffffffffu, fail);
           if (fail) break;
 #pragma unroll
