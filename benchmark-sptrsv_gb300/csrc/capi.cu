@@ -481,8 +481,11 @@ ExecConfig pick_config(const sptrsv_gb300_handle_s* h, int rhs) {
   ExecConfig c = h->cfg;
   c.sched = h->sched_option == SCHED_AUTO ? SCHED_PULL : h->sched_option;
   c.lanes = h->lanes_option > 0 ? h->lanes_option : 1;
-  c.chunk = h->chunk_option > 0 ? h->chunk_option : (rhs == 1 ? 224 : 256);
   c.block = h->block_option > 0 ? h->block_option : 256;
+  // one-rhs: one unknown per consumer thread per chunk; many rhs: one unknown per
+  // lane group (the group width the multi-rhs executors pick for this rhs)
+  const int group = rhs <= 4 ? 4 : rhs <= 8 ? 8 : rhs <= 16 ? 16 : 32;
+  c.chunk = h->chunk_option > 0 ? h->chunk_option : (rhs == 1 ? 224 : std::max(1, c.block / group));
   c.sleep_max = static_cast<unsigned>(h->backoff_ns);
   c.ctas_per_sm = h->ctas_per_sm;
   c.staged = h->staged;
@@ -1254,10 +1257,12 @@ int sptrsv_gb300_tune(sptrsv_handle_t h, const void* d_val, int dtype, int rhs, 
     cands.push_back({SCHED_LEVELSET, big, 256, 0, 256, 1, 8, 2});
     cands.push_back({SCHED_PUSH, 1024, 1024, 0, 256, 0, 1, 2});
   } else {
-    for (int ob : {big, 4096})
-      for (int ch : {64, 256}) cands.push_back({SCHED_PULL, ob, ch, 0, 256, 0, 1, 2});
+    // chunk 0 = one unknown per lane group; larger chunks trade tickets for locality
+    for (int ch : {0, 32})
+      for (int bo : {64, 512})
+        for (int ctas : {0, 2}) cands.push_back({SCHED_PULL, big, ch, 0, bo, ctas, 1, 2});
     cands.push_back({SCHED_LEVELSET, big, 256, 0, 256, 1, 8, 2});
-    cands.push_back({SCHED_PUSH, big, 256, 0, 256, 0, 1, 2});
+    cands.push_back({SCHED_PUSH, big, 0, 0, 256, 0, 1, 2});
   }
   (void)n;
   const int saved_check = h->sync_check, saved_profile = h->profile;
