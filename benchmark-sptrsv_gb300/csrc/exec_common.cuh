@@ -96,6 +96,7 @@ __device__ __forceinline__ bool gather_deps(const int* __restrict__ pos, const T
     }
     WaitBudget wb(timeout);
     unsigned nap = sleep_min;
+    unsigned local_spins = 0u;
     for (;;) {
       bool prefix = true;
       unsigned global_pending = 0u;
@@ -115,7 +116,9 @@ __device__ __forceinline__ bool gather_deps(const int* __restrict__ pos, const T
         __nanosleep(nap);
         nap = nap * 2u < sleep_max ? nap * 2u : sleep_max;
       }
-      if (!wb.poll(ctl, where)) return false;
+      // spins on shared memory only skip the (global-memory) status and timer
+      // checks most of the time, so an in-chunk hop stays a few dozen cycles
+      if ((global_pending || (++local_spins & 255u) == 0u) && !wb.poll(ctl, where)) return false;
 #pragma unroll
       for (int u = 0; u < U; ++u)
         if ((todo & (1u << u)) && bits[u] == F::EMPTY)
