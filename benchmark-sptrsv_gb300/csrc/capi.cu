@@ -45,6 +45,8 @@ struct sptrsv_gb300_handle_s {
   int staged = 1;
   int emax_option = 0;
   int stages_option = 2;
+  int fused_grad = 0;
+  int wsync = 0;
   // analysis
   bool analysed = false;
   int n = 0, nnz = 0, substitution = 0;
@@ -491,6 +493,7 @@ ExecConfig pick_config(const sptrsv_gb300_handle_s* h, int rhs) {
   c.staged = h->staged;
   c.emax = h->emax_option;
   c.stages = h->stages_option;
+  c.wsync = h->wsync;
   return c;
 }
 
@@ -692,6 +695,12 @@ int sptrsv_gb300_set_option(sptrsv_handle_t h, int option, long long value) {
       if (value < 2 || value > 4) return SPTRSV_ERR_INVALID;
       h->stages_option = static_cast<int>(value);
       return SPTRSV_OK;
+    case SPTRSV_OPTION_FUSED_GRAD:
+      h->fused_grad = value != 0;
+      return SPTRSV_OK;
+    case SPTRSV_OPTION_WARP_SYNC:
+      h->wsync = value != 0;
+      return SPTRSV_OK;
     default:
       return SPTRSV_ERR_INVALID;
   }
@@ -715,6 +724,8 @@ int sptrsv_gb300_get_option(sptrsv_handle_t h, int option, long long* value) {
     case SPTRSV_OPTION_STAGED: *value = h->staged; break;
     case SPTRSV_OPTION_STAGE_ENTRIES: *value = h->emax_option; break;
     case SPTRSV_OPTION_STAGES: *value = h->stages_option; break;
+    case SPTRSV_OPTION_FUSED_GRAD: *value = h->fused_grad; break;
+    case SPTRSV_OPTION_WARP_SYNC: *value = h->wsync; break;
     default: return SPTRSV_ERR_INVALID;
   }
   return SPTRSV_OK;
@@ -1117,6 +1128,15 @@ int sptrsv_gb300_solve_adjoint(sptrsv_handle_t h, const void* d_val, int dtype, 
   }
   const long long si = layout == SPTRSV_LAYOUT_ROW_MAJOR ? rhs : 1;
   const long long sk = layout == SPTRSV_LAYOUT_ROW_MAJOR ? 1 : h->n;
+  if (d_dval && !h->fused_grad) {
+    // transposed solve first, then one pass over the stored pattern for the gradient
+    const int saved = h->sync_check;
+    h->sync_check = 0;
+    int st = sptrsv_gb300_solve_adjoint(h, nullptr, dtype, rhs, layout, d_g, d_lambda, nullptr, nullptr, stream);
+    h->sync_check = saved;
+    if (st != SPTRSV_OK) return st;
+    return sptrsv_gb300_grad_values(h, dtype, rhs, layout, d_lambda, d_x, d_dval, stream);
+  }
   if (dtype == SPTRSV_DTYPE_F64) {
     if (!h->staged64) return SPTRSV_ERR_STATE;
     AdjointArgs<double> adj;

@@ -176,6 +176,148 @@ __global__ void __launch_bounds__(256) k_pull_vec(ExecArgs<T> a) {
   leave(a.ctl);
 }
 
+// ------------------------------------------------------------------ pull, warp-synchronous
+// One lane per unknown; the 32 lanes of a warp take 32 consecutive positions of
+// the chunk and advance in lockstep: every iteration each unfinished lane
+// consumes the dependencies that have arrived, issues the next loads (or
+// re-polls what is still pending), and publishes its x once its list is done;
+// __syncwarp() ends the iteration. A lane never spins while a lane of its own
+// warp that it depends on waits to run, so a chain inside a warp (common in
+// blocked orders of narrow DAGs) costs one short iteration per hop. Global
+// waits back off only when no lane of the warp made progress.
+template <typename T, bool EXACT, bool ADJ>
+__global__ void __launch_bounds__(256) k_pull_wsync(ExecArgs<T> a) {
+  using F = Flag<T>;
+  using Bits = typename F::Bits;
+  constexpr int U = 4;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* s_x = reinterpret_cast<T*>(smem_raw);
+  __shared__ unsigned s_chunk;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int* __restrict__ lptr = ADJ ? a.out_ptr : a.dep_ptr;
+  const int* __restrict__ lpos = ADJ ? a.out_pos : a.dep_pos;
+  const T* __restrict__ vals = ADJ ? (EXACT ? a.out_val : a.out_w) : (EXACT ? a.dep_val : a.dep_w);
+  const int last = a.n - 1;
+  for (;;) {
+    const unsigned c = next_chunk(a.ctl, a.nchunks, &s_chunk);
+    if (c >= (unsigned)a.nchunks) break;
+    const int base = static_cast<int>(c) * a.chunk;
+    const int cend = min(base + a.chunk, a.n);
+    const int len = cend - base;
+    if (a.smem_tier)
+      for (int i = threadIdx.x; i < len; i += blockDim.x) *reinterpret_cast<Bits*>(&s_x[i]) = F::EMPTY;
+    __syncthreads();
+    bool fail = false;
+    for (int seg = warp; seg * 32 < len && !fail; seg += nwarps) {
+      const int j = seg * 32 + lane;
+      bool done = j >= len;
+      const int pr = base + j;
+      const int p = ADJ ? last - pr : pr;
+      int row = 0, e = 0, e1 = 0;
+      T bi = T(0), sc = T(0), acc = T(0);
+      if (!done) {
+        row = a.perm[p];
+        e = lptr[p];
+        e1 = lptr[p + 1];
+        bi = a.b[(long long)row * a.b_si];
+        sc = EXACT ? a.diag[p] : a.rcp[p];
+        acc = EXACT ? T(0) : bi * sc;
+      }
+      auto slot = [&](int q) {
+        const int qr = ADJ ? last - q : q;
+        return (a.smem_tier && qr >= base) ? qr - base : -1;
+      };
+      int q[U], ls[U];
+      T w[U];
+      Bits bits[U];
+      unsigned todo = 0u;
+      auto load_batch = [&]() {
+        todo = 0u;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int ee = e + u;
+          q[u] = ee < e1 ? lpos[ee] : -1;
+          w[u] = ee < e1 ? vals[ee] : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          ls[u] = -1;
+          bits[u] = F::EMPTY;
+          if (q[u] >= 0) {
+            ls[u] = slot(q[u]);
+            bits[u] = ls[u] >= 0 ? F::load_shared(&s_x[ls[u]]) : F::load(&a.xw[q[u]]);
+            todo |= 1u << u;
+          }
+        }
+      };
+      if (!done) load_batch();
+      WaitBudget wb(a.timeout_ns);
+      unsigned nap = a.sleep_min, idle = 0u;
+      for (;;) {
+        bool progress = false, global_wait = false;
+        if (!done) {
+          bool prefix = true;
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            if (!(todo & (1u << u))) continue;
+            if (bits[u] != F::EMPTY && (!EXACT || prefix)) {
+              acc = EXACT ? exact_mul_add<T>(acc, w[u], F::value(bits[u])) : fma(-w[u], F::value(bits[u]), acc);
+              todo &= ~(1u << u);
+              progress = true;
+            } else {
+              prefix = false;
+              if (bits[u] == F::EMPTY && ls[u] < 0) global_wait = true;
+            }
+          }
+          if (!todo) {
+            e += U;
+            if (e < e1) {
+              load_batch();
+              progress = true;
+            } else {
+              const T xi = EXACT ? exact_finish<T>(bi, acc, sc) : acc;
+              if (a.smem_tier) F::store_shared(&s_x[pr - base], xi);
+              F::store(&a.xw[p], xi);
+              a.x[(long long)row * a.x_si] = xi;
+              if (ADJ && a.grad) {
+                for (int ee = a.dep_ptr[p]; ee < a.dep_ptr[p + 1]; ++ee)
+                  a.grad[a.dep_src[ee]] = -xi * a.xf[(long long)a.dep_col[ee] * a.xf_si];
+                a.grad[a.diag_src[p]] = -xi * a.xf[(long long)row * a.xf_si];
+              }
+              done = true;
+              progress = true;
+            }
+          } else {
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+              if ((todo & (1u << u)) && bits[u] == F::EMPTY)
+                bits[u] = ls[u] >= 0 ? F::load_shared(&s_x[ls[u]]) : F::load(&a.xw[q[u]]);
+          }
+        }
+        if (__all_sync(0xffffffffu, done)) break;
+        const bool any_progress = __any_sync(0xffffffffu, progress);
+        const bool any_global = __any_sync(0xffffffffu, global_wait);
+        __syncwarp();
+        if (!any_progress) {
+          if (any_global && a.sleep_max) {
+            __nanosleep(nap);
+            nap = nap * 2u < a.sleep_max ? nap * 2u : a.sleep_max;
+          }
+          if ((any_global || (++idle & 255u) == 0u) && !wb.poll(a.ctl, p)) fail = true;
+          if (__any_sync(0xffffffffu, fail)) {
+            fail = true;
+            break;
+          }
+        } else {
+          nap = a.sleep_min;
+        }
+      }
+    }
+    if (__syncthreads_or(fail)) break;
+  }
+  leave(a.ctl);
+}
+
 // ------------------------------------------------------------------ pull, many rhs
 // Lanes of a group cover right-hand sides; dependencies are walked in order.
 template <typename T, int G, int RPL, bool EXACT, bool ADJ>
@@ -570,6 +712,10 @@ template <typename T, bool ADJ>
 cudaError_t launch_pull_impl(ExecArgs<T>& a, int rhs, const ExecConfig& cfg, size_t smem, int num_sms,
                              cudaStream_t s) {
   const int block = cfg.block;
+  if (rhs == 1 && cfg.wsync) {
+    if (cfg.exact) return run(k_pull_wsync<T, true, ADJ>, a, block, smem, num_sms, s);
+    return run(k_pull_wsync<T, false, ADJ>, a, block, smem, num_sms, s);
+  }
   if (rhs == 1) {
     if (cfg.exact) return run(k_pull_vec<T, 1, true, 4, ADJ>, a, block, smem, num_sms, s);
     switch (cfg.lanes) {

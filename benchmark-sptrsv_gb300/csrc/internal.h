@@ -35,6 +35,7 @@ struct ExecConfig {
   int staged = 1;         // one right-hand side: TMA-staged chunk executor
   int emax = 0;           // staged: dependency entries per chunk (0: automatic)
   int stages = 2;         // staged: chunk buffers in the producer/consumer ring
+  int wsync = 0;          // unstaged one-rhs pull: warp-synchronous lanes (k_pull_wsync)
 };
 
 // Work units of the staged executor: chunk k covers walk indices

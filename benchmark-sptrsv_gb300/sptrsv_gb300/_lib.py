@@ -56,6 +56,8 @@ OPTION_CTAS_PER_SM = 11
 OPTION_STAGED = 12
 OPTION_STAGE_ENTRIES = 13
 OPTION_STAGES = 14
+OPTION_FUSED_GRAD = 15
+OPTION_WARP_SYNC = 16
 
 NOALLOC_MAX_N = 262144  # SPTRSV_NOALLOC_MAX_N
 

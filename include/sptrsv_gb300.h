@@ -91,7 +91,12 @@ typedef enum sptrsv_option {
   SPTRSV_OPTION_STAGED = 12,      /* 1 (default): one-rhs pull solves stream each chunk's layout slices
                                      into shared memory with bulk copies (TMA), double-buffered */
   SPTRSV_OPTION_STAGE_ENTRIES = 13, /* staged executor: dependency entries per chunk buffer (0 = auto) */
-  SPTRSV_OPTION_STAGES = 14       /* staged executor: chunk buffers in the producer/consumer ring (2-4) */
+  SPTRSV_OPTION_STAGES = 14,      /* staged executor: chunk buffers in the producer/consumer ring (2-4) */
+  SPTRSV_OPTION_FUSED_GRAD = 15,  /* sptrsv_gb300_solve_adjoint with d_dval: 1 = the transposed-solve
+                                     kernel writes the gradient as each lambda is known; 0 (default) =
+                                     transposed solve, then one gradient pass over the stored pattern */
+  SPTRSV_OPTION_WARP_SYNC = 16    /* one-rhs pull without staging: 1 = the 32 lanes of a warp advance in
+                                     lockstep (fast in-warp dependency chains; blocked orders) */
 } sptrsv_option;
 
 typedef struct sptrsv_info {
@@ -226,7 +231,8 @@ int sptrsv_gb300_solve_refine(sptrsv_handle_t handle, const double *d_val, int r
 
 /* Transposed (adjoint) solve op(L)^T Lambda = G on the same analysis, walked
  * in reverse dependency order (pull executor). With d_x (the forward solution
- * X, same layout) and d_dval both non-NULL, the same kernel also writes the
+ * X, same layout) and d_dval both non-NULL, the call also writes (in the solve
+ * kernel or in one pass after it, SPTRSV_OPTION_FUSED_GRAD) the
  * gradient of a loss with dLoss/dX = G with respect to every stored value:
  * d_dval[e] = -sum_k Lambda[row(e),k] * X[col(e),k] (CSC entry order); the
  * gradient with respect to B is Lambda itself. d_val as in sptrsv_gb300_solve. */

@@ -23,7 +23,10 @@ def relerr(x, ref):
 @pytest.mark.parametrize("cfg", [dict(lanes=1), dict(lanes=4, order_block=1), dict(lanes=32, order_block=10**9),
                                  dict(exact=True), dict(exact=True, order_block=10**9, chunk=64),
                                  dict(staged=False, lanes=1), dict(staged=False, exact=True),
-                                 dict(chunk=16, stage_entries=40), dict(chunk=16, stage_entries=40, exact=True)],
+                                 dict(chunk=16, stage_entries=40), dict(chunk=16, stage_entries=40, exact=True),
+                                 dict(fused_grad=1), dict(fused_grad=1, staged=False, lanes=4),
+                                 dict(staged=False, warp_sync=True, fused_grad=1),
+                                 dict(staged=False, warp_sync=True, exact=True, order_block=64, chunk=64)],
                          ids=lambda c: "-".join(f"{k}{v}" for k, v in c.items()))
 def test_adjoint_and_gradient_vs_oracle(cuda, name, cfg):
     from oracle import oracle

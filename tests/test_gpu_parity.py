@@ -52,6 +52,9 @@ CONFIGS = [
     dict(schedule=2, chunk=4096, block=64, ctas_per_sm=1, backoff_ns=0),
     dict(schedule=2, chunk=100, stages=3, order_block=10**9),
     dict(schedule=2, chunk=33, stages=4, stage_entries=48, block=128),
+    dict(schedule=2, staged=False, warp_sync=True),
+    dict(schedule=2, staged=False, warp_sync=True, order_block=64, chunk=64, block=64),
+    dict(schedule=2, staged=False, warp_sync=True, order_block=1, chunk=100, backoff_ns=0),
     dict(schedule=3, lanes=1),
     dict(schedule=3, lanes=8),
 ]
@@ -70,12 +73,13 @@ def test_fp64_matches_oracle(cuda, name, cfg):
 
 
 @pytest.mark.parametrize("name", golden_names())
-@pytest.mark.parametrize("order_block,staged,entries", [(1, True, 0), (256, True, 0), (10**9, True, 0),
-                                                        (256, False, 0), (10**9, True, 16)])
-def test_exact_pull_is_bit_identical(cuda, name, order_block, staged, entries):
+@pytest.mark.parametrize("order_block,staged,entries,wsync", [(1, True, 0, False), (256, True, 0, False),
+                                                              (10**9, True, 0, False), (256, False, 0, False),
+                                                              (10**9, True, 16, False), (256, False, 0, True)])
+def test_exact_pull_is_bit_identical(cuda, name, order_block, staged, entries, wsync):
     g = load_golden(name)
     s = make_solver(cuda, g, schedule=2, exact=True, order_block=order_block, staged=staged,
-                    stage_entries=entries, chunk=64 if entries else 0)
+                    stage_entries=entries, chunk=64 if entries else 0, warp_sync=wsync)
     x = s.solve(b_tensor(cuda, g)).cpu().numpy().ravel()
     assert np.array_equal(x.view(np.uint64), g["x64"].view(np.uint64))
     x32 = s.solve(b_tensor(cuda, g, np.float32)).cpu().numpy().ravel()
