@@ -60,10 +60,15 @@ def bytes_pass(n: int, nnz: int, rhs: int = 1, sv: int = 8, sx: int = 8) -> int:
     return 4 * (n + 1) + nnz * (4 + sv) + n * rhs * 2 * sx
 
 
-def make_cases():
+def make_cases(scale: float = 1.0):
     from sptrsv_gb300 import matgen
-    lap = matgen.system_laplace_2m(lower=True)
-    pl = matgen.system_powerlaw_4m(seed=1, lower=True)
+    if scale == 1.0:
+        lap = matgen.system_laplace_2m(lower=True)
+        pl = matgen.system_powerlaw_4m(seed=1, lower=True)
+    else:   # reduced copies of the same systems (profiling runs)
+        lap = matgen.laplace2d_lower(max(8, int(round(1414 * scale ** 0.5))))
+        pl = matgen.system_powerlaw_4m(seed=1, lower=True, n=max(1024, int(matgen.POWER_LAW_N * scale)),
+                                       target_nnz=max(4096, int(40_000_000 * scale)))
     cases = []
     for name, m in (("laplace_fwd", lap), ("laplace_bwd", lap.transpose()),
                     ("powerlaw_fwd", pl), ("powerlaw_bwd", pl.transpose())):
@@ -150,7 +155,7 @@ def run_reference(args, world, rank):
     from oracle import oracle
     imp = oracle.ref() or oracle.port()
     kind = "reference" if imp.kind == "ref" else "port"
-    cases = make_cases()
+    cases = make_cases(args.scale)
     degs = [imp.analyser(c["m"].row_idx, c["m"].n) for c in cases]
     total_bytes = sum(bytes_pass(c["m"].n, c["m"].nnz) for c in cases)
 
@@ -221,7 +226,7 @@ def run_gpu(args, world, rank, local):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
         pg = dist
-    cases = make_cases()
+    cases = make_cases(args.scale)
     solvers = []
     tuned = {}
     for c in cases:
@@ -342,7 +347,8 @@ def run_gpu(args, world, rank, local):
         "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(step_ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generators, x_true = 1)",
-        "config": {"workload": WORKLOAD, "rhs": 1, "parallelism": f"replicas x{world}",
+        "config": {"workload": WORKLOAD if args.scale == 1.0 else f"{WORKLOAD}, sizes x{args.scale}", "rhs": 1,
+                   "parallelism": f"replicas x{world}",
                    "l2": "flushed (256 MiB write) before every solve, outside the timed events",
                    "solver": args.solver_kw or ("defaults" if args.no_tune else "autotuned per system"),
                    "tuned": tuned},
@@ -436,6 +442,11 @@ def run_batch(args):
                        sync_check=False, **args.solver_kw)
     tan = time.perf_counter() - t0
     b = torch.from_numpy(np.concatenate(bs)).cuda()
+    tuned = None
+    if not args.no_tune and not args.solver_kw:
+        s.set_option(7, 1)
+        tuned = s.tune(b, values=torch.from_numpy(vals).cuda(), reps=2)
+        s.set_option(7, 0)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
     s.set_option(7, 1)
     xr, iters, est = s.solve_refine(b)
@@ -467,7 +478,7 @@ def run_batch(args):
     line = {"workload": "batch", "metric": "batched solves/s (FP32+FP64 refinement, one persistent launch per pass)",
             "value": round(nsys / (t_mixed * 1e-3), 2), "unit": "systems/s", "higher_is_better": True,
             "systems": nsys, "n_total": ntot, "nnz_total": nnz, "rhs": rhs,
-            "nlevels_batch": s.info()["nlevels"],
+            "nlevels_batch": s.info()["nlevels"], "tuned": tuned,
             "mixed_batched_ms": round(t_mixed, 3), "refine_steps": iters, "fp64_batched_ms": round(t_b64, 3),
             "fp64_per_system_launches_ms": round(t_per, 3),
             "speedup_vs_per_system_fp64": round(t_per / t_mixed, 2),
@@ -533,6 +544,8 @@ def main(argv=None) -> int:
     ap.add_argument("--order-block", type=int, default=None)
     ap.add_argument("--workload", choices=["deep_wide", "multi_rhs", "batch", "adjoint"], default="deep_wide")
     ap.add_argument("--batch-count", type=int, default=512)
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="size factor of the deep/wide systems (1.0 = the benchmark sizes; smaller for profiling)")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3

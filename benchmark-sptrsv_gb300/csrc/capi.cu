@@ -1263,26 +1263,28 @@ int sptrsv_gb300_tune(sptrsv_handle_t h, const void* d_val, int dtype, int rhs, 
   if (!h->analysed) return SPTRSV_ERR_STATE;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   struct Cand {
-    int sched, order_block, chunk, staged, backoff, ctas, lanes, stages;
+    int sched, order_block, chunk, staged, backoff, ctas, lanes, stages, wsync, block;
   };
   const int n = h->n;
   const int big = INT_MAX;
   std::vector<Cand> cands;
   if (rhs == 1) {
-    for (int ob : {big, 4096, 1024})
-      for (int ch : {224, 448, 896})
-        for (int bo : {0, 256}) cands.push_back({SCHED_PULL, ob, ob == 1024 ? 1024 : ch, 1, bo, 0, 1, 2});
-    cands.push_back({SCHED_PULL, big, 256, 0, 1024, 2, 1, 2});
-    cands.push_back({SCHED_PULL, big, 256, 0, 256, 0, 1, 2});
-    cands.push_back({SCHED_LEVELSET, big, 256, 0, 256, 1, 8, 2});
-    cands.push_back({SCHED_PUSH, 1024, 1024, 0, 256, 0, 1, 2});
+    // staged warp-specialised executor, level order
+    for (int bo : {0, 256}) cands.push_back({SCHED_PULL, big, 224, 1, bo, 0, 1, 2, 0, 256});
+    // warp-synchronous executor: level order, and blocked orders for deep narrow DAGs
+    for (int ch : {128, 256}) cands.push_back({SCHED_PULL, big, ch, 0, 128, 1, 1, 2, 1, ch});
+    for (int ob : {2048, 8192, 22624}) cands.push_back({SCHED_PULL, ob, ob, 0, 0, 0, 1, 2, 1, 128});
+    // thread-per-unknown executor, level order
+    cands.push_back({SCHED_PULL, big, 256, 0, 128, 1, 1, 2, 0, 256});
+    cands.push_back({SCHED_LEVELSET, big, 256, 0, 256, 1, 8, 2, 0, 256});
+    cands.push_back({SCHED_PUSH, 1024, 1024, 0, 256, 0, 1, 2, 0, 256});
   } else {
-    // chunk 0 = one unknown per lane group; larger chunks trade tickets for locality
-    for (int ch : {0, 32})
-      for (int bo : {64, 512})
-        for (int ctas : {0, 2}) cands.push_back({SCHED_PULL, big, ch, 0, bo, ctas, 1, 2});
-    cands.push_back({SCHED_LEVELSET, big, 256, 0, 256, 1, 8, 2});
-    cands.push_back({SCHED_PUSH, big, 0, 0, 256, 0, 1, 2});
+    // chunk 0 = one unknown per lane group
+    for (int bo : {64, 512}) cands.push_back({SCHED_PULL, big, 0, 0, bo, 0, 1, 2, 1, 256});
+    for (int ob : {1024, 4096}) cands.push_back({SCHED_PULL, ob, ob, 0, 0, 0, 1, 2, 1, 256});
+    cands.push_back({SCHED_PULL, big, 0, 0, 256, 0, 1, 2, 0, 256});
+    cands.push_back({SCHED_LEVELSET, big, 256, 0, 256, 1, 8, 2, 0, 256});
+    cands.push_back({SCHED_PUSH, big, 0, 0, 256, 0, 1, 2, 0, 256});
   }
   (void)n;
   const int saved_check = h->sync_check, saved_profile = h->profile;
@@ -1303,6 +1305,8 @@ int sptrsv_gb300_tune(sptrsv_handle_t h, const void* d_val, int dtype, int rhs, 
     h->ctas_per_sm = c.ctas;
     h->lanes_option = c.lanes;
     h->stages_option = c.stages;
+    h->wsync = c.wsync;
+    h->block_option = c.block;
     int st = sptrsv_gb300_solve(h, d_val, dtype, rhs, layout, d_b, d_x, stream);
     if (st == SPTRSV_OK) st = check_device(h, s);
     if (st != SPTRSV_OK) continue;  // a candidate that fails (or times out) is skipped
@@ -1339,6 +1343,8 @@ int sptrsv_gb300_tune(sptrsv_handle_t h, const void* d_val, int dtype, int rhs, 
   h->ctas_per_sm = c.ctas;
   h->lanes_option = c.lanes;
   h->stages_option = c.stages;
+  h->wsync = c.wsync;
+  h->block_option = c.block;
   ST_TRY(ensure_layout(h, s));
   ST_TRY(stage_values(h, d_val, dtype, s, false));
   if (best_ms) *best_ms = best;

@@ -318,6 +318,169 @@ __global__ void __launch_bounds__(256) k_pull_wsync(ExecArgs<T> a) {
   leave(a.ctl);
 }
 
+// ------------------------------------------------------------------ pull, warp-synchronous, many rhs
+// As k_pull_wsync, with G lanes per unknown (32/G unknowns per warp), each lane
+// covering RPL right-hand sides (rhs <= G*RPL). A group moves to its next
+// batch of dependencies once every lane of the group has consumed the batch.
+template <typename T, bool EXACT, bool ADJ, int G, int RPL>
+__global__ void __launch_bounds__(256) k_pull_wsync_multi(ExecArgs<T> a) {
+  using F = Flag<T>;
+  using Bits = typename F::Bits;
+  constexpr int UD = 2;
+  constexpr int P = 32 / G;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* s_x = reinterpret_cast<T*>(smem_raw);
+  __shared__ unsigned s_chunk;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int gi = lane / G, gl = lane % G;
+  const unsigned gmask = group_mask(G);
+  const int rhs = a.rhs;
+  const int* __restrict__ lptr = ADJ ? a.out_ptr : a.dep_ptr;
+  const int* __restrict__ lpos = ADJ ? a.out_pos : a.dep_pos;
+  const T* __restrict__ vals = ADJ ? (EXACT ? a.out_val : a.out_w) : (EXACT ? a.dep_val : a.dep_w);
+  const int last = a.n - 1;
+  for (;;) {
+    const unsigned c = next_chunk(a.ctl, a.nchunks, &s_chunk);
+    if (c >= (unsigned)a.nchunks) break;
+    const int base = static_cast<int>(c) * a.chunk;
+    const int cend = min(base + a.chunk, a.n);
+    const int len = cend - base;
+    if (a.smem_tier)
+      for (long long i = threadIdx.x; i < (long long)len * rhs; i += blockDim.x)
+        *reinterpret_cast<Bits*>(&s_x[i]) = F::EMPTY;
+    __syncthreads();
+    bool fail = false;
+    for (int seg = warp; seg * P < len && !fail; seg += nwarps) {
+      const int j = seg * P + gi;
+      bool done = j >= len;     // group-uniform
+      const int pr = base + j;
+      const int p = ADJ ? last - pr : pr;
+      int row = 0, e = 0, e1 = 0;
+      T sc = T(0);
+      T acc[RPL];
+#pragma unroll
+      for (int r = 0; r < RPL; ++r) acc[r] = T(0);
+      if (!done) {
+        row = a.perm[p];
+        e = lptr[p];
+        e1 = lptr[p + 1];
+        sc = EXACT ? a.diag[p] : a.rcp[p];
+        if (!EXACT) {
+#pragma unroll
+          for (int r = 0; r < RPL; ++r) {
+            const int k = gl + r * G;
+            if (k < rhs) acc[r] = a.b[(long long)row * a.b_si + (long long)k * a.b_sk] * sc;
+          }
+        }
+      }
+      int q[UD], sl[UD];
+      T w[UD];
+      Bits bits[UD][RPL];
+      unsigned todo = 0u;
+      auto load_batch = [&]() {
+        todo = 0u;
+#pragma unroll
+        for (int u = 0; u < UD; ++u) {
+          q[u] = e + u < e1 ? lpos[e + u] : -1;
+          w[u] = e + u < e1 ? vals[e + u] : T(0);
+          const int qr = ADJ ? last - q[u] : q[u];
+          sl[u] = (q[u] >= 0 && a.smem_tier && qr >= base) ? qr - base : -1;
+#pragma unroll
+          for (int r = 0; r < RPL; ++r) {
+            const int k = gl + r * G;
+            bits[u][r] = F::EMPTY;
+            if (q[u] >= 0 && k < rhs) {
+              bits[u][r] = sl[u] >= 0 ? F::load_shared(&s_x[(long long)sl[u] * rhs + k])
+                                      : F::load(&a.xw[(long long)q[u] * rhs + k]);
+              todo |= 1u << (u * RPL + r);
+            }
+          }
+        }
+      };
+      if (!done) load_batch();
+      WaitBudget wb(a.timeout_ns);
+      unsigned nap = a.sleep_min, idle = 0u;
+      for (;;) {
+        bool progress = false, global_wait = false;
+        if (!done) {
+#pragma unroll
+          for (int r = 0; r < RPL; ++r) {
+            bool prefix = true;
+#pragma unroll
+            for (int u = 0; u < UD; ++u) {
+              const unsigned bit = 1u << (u * RPL + r);
+              if (!(todo & bit)) continue;
+              if (bits[u][r] != F::EMPTY && (!EXACT || prefix)) {
+                acc[r] = EXACT ? exact_mul_add<T>(acc[r], w[u], F::value(bits[u][r])) : fma(-w[u], F::value(bits[u][r]), acc[r]);
+                todo &= ~bit;
+                progress = true;
+              } else {
+                prefix = false;
+                if (bits[u][r] == F::EMPTY && sl[u] < 0) global_wait = true;
+              }
+            }
+          }
+        }
+        // a group advances once all its lanes have consumed the batch
+        const unsigned empty_lanes = __ballot_sync(0xffffffffu, done || todo == 0u);
+        const bool group_clear = (empty_lanes & gmask) == gmask;
+        if (!done) {
+          if (group_clear) {
+            e += UD;
+            if (e < e1) {
+              load_batch();
+            } else {
+#pragma unroll
+              for (int r = 0; r < RPL; ++r) {
+                const int k = gl + r * G;
+                if (k < rhs) {
+                  const T xi = EXACT ? exact_finish<T>(a.b[(long long)row * a.b_si + (long long)k * a.b_sk], acc[r], sc)
+                                     : acc[r];
+                  acc[r] = xi;
+                  if (a.smem_tier) F::store_shared(&s_x[(long long)(pr - base) * rhs + k], xi);
+                  F::store(&a.xw[(long long)p * rhs + k], xi);
+                  a.x[(long long)row * a.x_si + (long long)k * a.x_sk] = xi;
+                }
+              }
+              done = true;
+            }
+            progress = true;
+          } else {
+#pragma unroll
+            for (int u = 0; u < UD; ++u)
+#pragma unroll
+              for (int r = 0; r < RPL; ++r) {
+                const int k = gl + r * G;
+                if ((todo & (1u << (u * RPL + r))) && bits[u][r] == F::EMPTY)
+                  bits[u][r] = sl[u] >= 0 ? F::load_shared(&s_x[(long long)sl[u] * rhs + k])
+                                          : F::load(&a.xw[(long long)q[u] * rhs + k]);
+              }
+          }
+        }
+        if (__all_sync(0xffffffffu, done)) break;
+        const bool any_progress = __any_sync(0xffffffffu, progress);
+        const bool any_global = __any_sync(0xffffffffu, global_wait);
+        __syncwarp();
+        if (!any_progress) {
+          if (any_global && a.sleep_max) {
+            __nanosleep(nap);
+            nap = nap * 2u < a.sleep_max ? nap * 2u : a.sleep_max;
+          }
+          if ((any_global || (++idle & 255u) == 0u) && !wb.poll(a.ctl, p)) fail = true;
+          if (__any_sync(0xffffffffu, fail)) {
+            fail = true;
+            break;
+          }
+        } else {
+          nap = a.sleep_min;
+        }
+      }
+    }
+    if (__syncthreads_or(fail)) break;
+  }
+  leave(a.ctl);
+}
+
 // ------------------------------------------------------------------ pull, many rhs
 // Lanes of a group cover right-hand sides; dependencies are walked in order.
 template <typename T, int G, int RPL, bool EXACT, bool ADJ>
@@ -728,6 +891,17 @@ cudaError_t launch_pull_impl(ExecArgs<T>& a, int rhs, const ExecConfig& cfg, siz
     }
   }
   // many right-hand sides: lanes over rhs
+  if (cfg.wsync && rhs <= 64 && a.grad == nullptr) {
+    if (cfg.exact) {
+      if (rhs <= 8) return run(k_pull_wsync_multi<T, true, ADJ, 8, 1>, a, block, smem, num_sms, s);
+      return run(k_pull_wsync_multi<T, true, ADJ, 32, 2>, a, block, smem, num_sms, s);
+    }
+    if (rhs <= 4) return run(k_pull_wsync_multi<T, false, ADJ, 4, 1>, a, block, smem, num_sms, s);
+    if (rhs <= 8) return run(k_pull_wsync_multi<T, false, ADJ, 8, 1>, a, block, smem, num_sms, s);
+    if (rhs <= 16) return run(k_pull_wsync_multi<T, false, ADJ, 16, 1>, a, block, smem, num_sms, s);
+    if (rhs <= 32) return run(k_pull_wsync_multi<T, false, ADJ, 32, 1>, a, block, smem, num_sms, s);
+    return run(k_pull_wsync_multi<T, false, ADJ, 32, 2>, a, block, smem, num_sms, s);
+  }
   if (cfg.exact) {
     if (rhs <= 8) return run(k_pull_multi<T, 8, 1, true, ADJ>, a, block, smem, num_sms, s);
     return run(k_pull_multi<T, 32, 2, true, ADJ>, a, block, smem, num_sms, s);

@@ -26,7 +26,8 @@ def relerr(x, ref):
                                  dict(chunk=16, stage_entries=40), dict(chunk=16, stage_entries=40, exact=True),
                                  dict(fused_grad=1), dict(fused_grad=1, staged=False, lanes=4),
                                  dict(staged=False, warp_sync=True, fused_grad=1),
-                                 dict(staged=False, warp_sync=True, exact=True, order_block=64, chunk=64)],
+                                 dict(staged=False, warp_sync=True, exact=True, order_block=64, chunk=64),
+                                 dict(staged=False, warp_sync=True, order_block=128, chunk=128)],
                          ids=lambda c: "-".join(f"{k}{v}" for k, v in c.items()))
 def test_adjoint_and_gradient_vs_oracle(cuda, name, cfg):
     from oracle import oracle
