@@ -431,6 +431,55 @@ cudaError_t launch_gather_int(const int* src, const int* idx, int* out, int coun
   return cudaGetLastError();
 }
 
+// ------------------------------------------------------------ ready-order lists
+// The fast (non-exact) executors consume a dependency list in batches and only
+// move to the next batch once the current one has arrived. Listing each
+// position's dependencies in the order they complete (ascending position for a
+// forward walk, descending for the reverse walk) leaves only the final batch
+// waiting on the last publication, instead of whatever followed it in the
+// serial (column) order.
+__global__ void k_rank_keys(const int* __restrict__ pos, int count, int n, int descending, unsigned* keys) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += stride)
+    keys[i] = static_cast<unsigned>(descending ? n - 1 - pos[i] : pos[i]);
+}
+__global__ void k_owner_keys(const int* __restrict__ owner, const int* __restrict__ idx, int count, unsigned* keys) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += stride)
+    keys[i] = static_cast<unsigned>(owner[idx[i]]);
+}
+
+cudaError_t launch_sort_lists(const int* ptr, const int* pos, const int* src, int n, int count, bool descending,
+                              int* pos_out, int* src_out, cudaStream_t s) {
+  if (count <= 0 || n <= 0) return cudaSuccess;
+  int bits = 1;
+  while (bits < 31 && (1u << bits) <= static_cast<unsigned>(n - 1)) ++bits;
+  unsigned *k1 = nullptr, *k2 = nullptr;
+  int *v1 = nullptr, *v2 = nullptr;
+  void* temp = nullptr;
+  cudaError_t err;
+  if ((err = cudaMallocAsync(reinterpret_cast<void**>(&k1), sizeof(unsigned) * count, s)) != cudaSuccess) return err;
+  if ((err = cudaMallocAsync(reinterpret_cast<void**>(&k2), sizeof(unsigned) * count, s)) != cudaSuccess) return err;
+  if ((err = cudaMallocAsync(reinterpret_cast<void**>(&v1), sizeof(int) * count, s)) != cudaSuccess) return err;
+  if ((err = cudaMallocAsync(reinterpret_cast<void**>(&v2), sizeof(int) * count, s)) != cudaSuccess) return err;
+  if ((err = cudaMallocAsync(&temp, radix_sort_temp_bytes(count), s)) != cudaSuccess) return err;
+  // entries by position of the dependency, then (stable) by owning position
+  k_rank_keys<<<grid_for(count), kThreads, 0, s>>>(pos, count, n, descending ? 1 : 0, k1);
+  if ((err = launch_iota(v1, count, 0, 1, s)) != cudaSuccess) return err;
+  if ((err = radix_sort_pairs(k1, v1, k2, v2, count, bits, temp, s)) != cudaSuccess) return err;
+  if ((err = launch_expand_cols(ptr, n, v1, s)) != cudaSuccess) return err;
+  k_owner_keys<<<grid_for(count), kThreads, 0, s>>>(v1, v2, count, k1);
+  if ((err = radix_sort_pairs(k1, v2, k2, v1, count, bits, temp, s)) != cudaSuccess) return err;
+  if ((err = launch_gather_int(pos, v1, pos_out, count, s)) != cudaSuccess) return err;
+  if ((err = launch_gather_int(src, v1, src_out, count, s)) != cudaSuccess) return err;
+  cudaFreeAsync(k1, s);
+  cudaFreeAsync(k2, s);
+  cudaFreeAsync(v1, s);
+  cudaFreeAsync(v2, s);
+  cudaFreeAsync(temp, s);
+  return cudaGetLastError();
+}
+
 // ------------------------------------------------------------ level sets
 // Breadth-first peeling of the in-degree, one grid barrier per level
 // (the level definition of SpTRSV_cuda/findlevel.h:6-69): level 0 holds rows
@@ -677,14 +726,15 @@ __global__ void k_stage_diag(const TV* __restrict__ val, const int* __restrict__
 }
 
 // w = v * (1/diag of the dependent row): x_p = b_p/d_p - sum_j w_j x_j needs one
-// fused multiply-add per dependency once the reciprocal is folded in.
-template <typename T>
-__global__ void k_stage_scaled(const int* __restrict__ dep_ptr, const T* __restrict__ dep_val,
-                               const T* __restrict__ rcp, T* dep_w, int n) {
+// fused multiply-add per dependency once the reciprocal is folded in. The scaled
+// lists follow the ready order (src_f), the plain ones the serial order.
+template <typename TV, typename T>
+__global__ void k_stage_scaled(const int* __restrict__ ptr, const TV* __restrict__ val, const int* __restrict__ src_f,
+                               const T* __restrict__ rcp, T* w, int n) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += stride) {
     const T r = rcp[p];
-    for (int e = dep_ptr[p]; e < dep_ptr[p + 1]; ++e) dep_w[e] = dep_val[e] * r;
+    for (int e = ptr[p]; e < ptr[p + 1]; ++e) w[e] = static_cast<T>(val[src_f[e]]) * r;
   }
 }
 
@@ -696,8 +746,8 @@ cudaError_t launch_stage_values(const Layout& L, const TV* val, Values<T>& V, in
   }
   if (L.n > 0) k_stage_diag<TV, T><<<grid_for(L.n), kThreads, 0, s>>>(val, L.diag_src, V.diag, V.rcp, L.n, flags);
   if (L.n > 0 && L.ndep > 0) {
-    k_stage_scaled<T><<<grid_for(L.n), kThreads, 0, s>>>(L.dep_ptr, V.dep_val, V.rcp, V.dep_w, L.n);
-    k_stage_scaled<T><<<grid_for(L.n), kThreads, 0, s>>>(L.out_ptr, V.out_val, V.rcp, V.out_w, L.n);
+    k_stage_scaled<TV, T><<<grid_for(L.n), kThreads, 0, s>>>(L.dep_ptr, val, L.dep_src_f, V.rcp, V.dep_w, L.n);
+    k_stage_scaled<TV, T><<<grid_for(L.n), kThreads, 0, s>>>(L.out_ptr, val, L.out_src_f, V.rcp, V.out_w, L.n);
   }
   return cudaGetLastError();
 }

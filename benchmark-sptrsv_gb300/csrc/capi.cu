@@ -152,6 +152,10 @@ void free_layout(Layout& L) {
   dev_free(&L.out_ptr);
   dev_free(&L.out_pos);
   dev_free(&L.out_src);
+  dev_free(&L.dep_pos_f);
+  dev_free(&L.dep_src_f);
+  dev_free(&L.out_pos_f);
+  dev_free(&L.out_src_f);
   dev_free(&L.level_ptr);
   L = Layout();
 }
@@ -286,6 +290,10 @@ int build_layout(sptrsv_gb300_handle_s* h, int block, cudaStream_t s) {
   ST_TRY(dev_alloc(h, &L.dep_col, ndep));
   ST_TRY(dev_alloc(h, &L.out_pos, ndep));
   ST_TRY(dev_alloc(h, &L.out_src, ndep));
+  ST_TRY(dev_alloc(h, &L.dep_pos_f, ndep));
+  ST_TRY(dev_alloc(h, &L.dep_src_f, ndep));
+  ST_TRY(dev_alloc(h, &L.out_pos_f, ndep));
+  ST_TRY(dev_alloc(h, &L.out_src_f, ndep));
   ST_TRY(dev_alloc(h, &L.diag_src, n));
 
   const bool level_order = block >= n;
@@ -339,6 +347,8 @@ int build_layout(sptrsv_gb300_handle_s* h, int block, cudaStream_t s) {
                               L.dep_pos, L.dep_src, L.dep_col, L.diag_src, s));
     CUDA_TRY(launch_fill_push(L.perm, L.iperm, h->csc_ptr, h->csc_row, L.out_ptr, n, sd, L.out_pos,
                               L.out_src, s));
+    CUDA_TRY(launch_sort_lists(L.dep_ptr, L.dep_pos, L.dep_src, n, ndep, false, L.dep_pos_f, L.dep_src_f, s));
+    CUDA_TRY(launch_sort_lists(L.out_ptr, L.out_pos, L.out_src, n, ndep, true, L.out_pos_f, L.out_src_f, s));
     std::vector<int> ptr((size_t)n + 1);
     CUDA_TRY(cudaMemcpyAsync(ptr.data(), L.dep_ptr, sizeof(int) * ((size_t)n + 1), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));

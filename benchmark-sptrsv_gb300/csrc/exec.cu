@@ -33,6 +33,7 @@ struct ExecArgs {
   const int* perm;
   const int* dep_ptr;
   const int* dep_pos;
+  const int* dep_pos_f;  // ready order (pairs with dep_w)
   const T* dep_val;
   const T* dep_w;
   const int* dep_src;
@@ -40,6 +41,7 @@ struct ExecArgs {
   const int* diag_src;
   const int* out_ptr;
   const int* out_pos;
+  const int* out_pos_f;  // ready order (pairs with out_w)
   const T* out_val;
   const T* out_w;
   T* grad;           // adjoint: gradient w.r.t. the stored values (CSC order), or null
@@ -126,7 +128,7 @@ __global__ void __launch_bounds__(256) k_pull_vec(ExecArgs<T> a) {
   const int g = threadIdx.x / G, lane = threadIdx.x % G;
   const unsigned gmask = group_mask(G);
   const int* __restrict__ lptr = ADJ ? a.out_ptr : a.dep_ptr;
-  const int* __restrict__ lpos = ADJ ? a.out_pos : a.dep_pos;
+  const int* __restrict__ lpos = ADJ ? (EXACT ? a.out_pos : a.out_pos_f) : (EXACT ? a.dep_pos : a.dep_pos_f);
   const T* __restrict__ vals = ADJ ? (EXACT ? a.out_val : a.out_w) : (EXACT ? a.dep_val : a.dep_w);
   const int last = a.n - 1;
   for (;;) {
@@ -195,7 +197,7 @@ __global__ void __launch_bounds__(256) k_pull_wsync(ExecArgs<T> a) {
   __shared__ unsigned s_chunk;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int* __restrict__ lptr = ADJ ? a.out_ptr : a.dep_ptr;
-  const int* __restrict__ lpos = ADJ ? a.out_pos : a.dep_pos;
+  const int* __restrict__ lpos = ADJ ? (EXACT ? a.out_pos : a.out_pos_f) : (EXACT ? a.dep_pos : a.dep_pos_f);
   const T* __restrict__ vals = ADJ ? (EXACT ? a.out_val : a.out_w) : (EXACT ? a.dep_val : a.dep_w);
   const int last = a.n - 1;
   for (;;) {
@@ -336,7 +338,7 @@ __global__ void __launch_bounds__(256) k_pull_wsync_multi(ExecArgs<T> a) {
   const unsigned gmask = group_mask(G);
   const int rhs = a.rhs;
   const int* __restrict__ lptr = ADJ ? a.out_ptr : a.dep_ptr;
-  const int* __restrict__ lpos = ADJ ? a.out_pos : a.dep_pos;
+  const int* __restrict__ lpos = ADJ ? (EXACT ? a.out_pos : a.out_pos_f) : (EXACT ? a.dep_pos : a.dep_pos_f);
   const T* __restrict__ vals = ADJ ? (EXACT ? a.out_val : a.out_w) : (EXACT ? a.dep_val : a.dep_w);
   const int last = a.n - 1;
   for (;;) {
@@ -494,7 +496,7 @@ __global__ void __launch_bounds__(256) k_pull_multi(ExecArgs<T> a) {
   const unsigned gmask = group_mask(G);
   const int rhs = a.rhs;
   const int* __restrict__ lptr = ADJ ? a.out_ptr : a.dep_ptr;
-  const int* __restrict__ lpos = ADJ ? a.out_pos : a.dep_pos;
+  const int* __restrict__ lpos = ADJ ? (EXACT ? a.out_pos : a.out_pos_f) : (EXACT ? a.dep_pos : a.dep_pos_f);
   const T* __restrict__ vals = ADJ ? (EXACT ? a.out_val : a.out_w) : (EXACT ? a.dep_val : a.dep_w);
   const int last = a.n - 1;
   for (;;) {
@@ -793,7 +795,7 @@ __global__ void __launch_bounds__(256) k_levelset(ExecArgs<T> a) {
       for (int k = 0; k < rhs; ++k) {
         T acc = lane == 0 ? a.b[(long long)row * a.b_si + (long long)k * a.b_sk] * rc : T(0);
         for (int e = e0 + lane; e < e1; e += G)
-          acc = fma(-a.dep_w[e], F::value(F::load(&a.xw[(long long)a.dep_pos[e] * rhs + k])), acc);
+          acc = fma(-a.dep_w[e], F::value(F::load(&a.xw[(long long)a.dep_pos_f[e] * rhs + k])), acc);
         if (G > 1) {
 #pragma unroll
           for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(gmask, acc, o);
@@ -821,6 +823,7 @@ ExecArgs<T> make_args(const Layout& L, const Values<T>& V, int rhs, const VecVie
   a.perm = L.perm;
   a.dep_ptr = L.dep_ptr;
   a.dep_pos = L.dep_pos;
+  a.dep_pos_f = L.dep_pos_f;
   a.dep_val = V.dep_val;
   a.dep_w = V.dep_w;
   a.dep_src = L.dep_src;
@@ -829,6 +832,7 @@ ExecArgs<T> make_args(const Layout& L, const Values<T>& V, int rhs, const VecVie
   a.out_w = V.out_w;
   a.out_ptr = L.out_ptr;
   a.out_pos = L.out_pos;
+  a.out_pos_f = L.out_pos_f;
   a.out_val = V.out_val;
   a.diag = V.diag;
   a.rcp = V.rcp;

@@ -414,7 +414,7 @@ cudaError_t launch_pull_staged(const Layout& L, const Values<T>& V, const ChunkT
   a.perm = L.perm;
   const bool is_adj = adj != nullptr;
   a.lptr = is_adj ? L.out_ptr : L.dep_ptr;
-  a.lpos = is_adj ? L.out_pos : L.dep_pos;
+  a.lpos = is_adj ? (cfg.exact ? L.out_pos : L.out_pos_f) : (cfg.exact ? L.dep_pos : L.dep_pos_f);
   a.lval = is_adj ? (cfg.exact ? V.out_val : V.out_w) : (cfg.exact ? V.dep_val : V.dep_w);
   a.dscale = cfg.exact ? V.diag : V.rcp;
   a.b = v.b;

@@ -77,6 +77,12 @@ struct Layout {
   int* out_ptr = nullptr;    // [n+1]
   int* out_pos = nullptr;    // [ndep]
   int* out_src = nullptr;    // [ndep]
+  // the same lists in ready order, for the fast executors: dependencies by
+  // ascending position, dependents by descending position (the adjoint walk)
+  int* dep_pos_f = nullptr;  // [ndep]
+  int* dep_src_f = nullptr;  // [ndep]
+  int* out_pos_f = nullptr;  // [ndep]
+  int* out_src_f = nullptr;  // [ndep]
   // level sets in position space (valid when the schedule is pure level order)
   int nlevels = 0;
   std::vector<int> level_ptr_host;
@@ -86,9 +92,9 @@ struct Layout {
 template <typename T>
 struct Values {
   T* dep_val = nullptr;  // [ndep]
-  T* dep_w = nullptr;    // [ndep] dep_val scaled by the reciprocal of its row's diagonal
+  T* dep_w = nullptr;    // [ndep] values scaled by the reciprocal of the row's diagonal (ready order)
   T* out_val = nullptr;  // [ndep]
-  T* out_w = nullptr;    // [ndep] out_val scaled by the reciprocal of the owning position's diagonal
+  T* out_w = nullptr;    // [ndep] values scaled by the reciprocal of the owning position's diagonal (ready order)
   T* diag = nullptr;     // [n]
   T* rcp = nullptr;      // [n] correctly rounded 1/diag
 };
@@ -145,6 +151,9 @@ cudaError_t launch_fill_pull(const int* perm, const int* iperm, const int* csr_p
 cudaError_t launch_fill_push(const int* perm, const int* iperm, const int* col_ptr, const int* row_idx,
                              const int* out_ptr, int n, const SysDesc& sd, int* out_pos, int* out_src,
                              cudaStream_t s);
+// Sorts every list [ptr[p], ptr[p+1]) of (pos, src) by pos (descending when asked).
+cudaError_t launch_sort_lists(const int* ptr, const int* pos, const int* src, int n, int count, bool descending,
+                              int* pos_out, int* src_out, cudaStream_t s);
 template <typename TV, typename T>
 cudaError_t launch_stage_values(const Layout& L, const TV* val, Values<T>& V, int* flags, cudaStream_t s);
 
