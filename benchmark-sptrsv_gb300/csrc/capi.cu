@@ -47,6 +47,7 @@ struct sptrsv_gb300_handle_s {
   int stages_option = 2;
   int fused_grad = 0;
   int wsync = 0;
+  int split = 32;
   // analysis
   bool analysed = false;
   int n = 0, nnz = 0, substitution = 0;
@@ -75,6 +76,7 @@ struct sptrsv_gb300_handle_s {
   std::vector<int> dep_cnt_host;   // dependencies per position
   std::vector<int> out_cnt_host;   // dependents per position
   ChunkTable tab_fwd, tab_adj;
+  PieceTable pc_fwd, pc_adj;
   // staged values
   Values<double> v64;
   Values<float> v32;
@@ -141,6 +143,14 @@ void free_table(ChunkTable& t) {
   t = ChunkTable();
 }
 
+void free_pieces(PieceTable& t) {
+  if (t.walk) cudaFree(t.walk);
+  if (t.lo) cudaFree(t.lo);
+  if (t.hi) cudaFree(t.hi);
+  if (t.cbase) cudaFree(t.cbase);
+  t = PieceTable();
+}
+
 void free_layout(Layout& L) {
   dev_free(&L.perm);
   dev_free(&L.iperm);
@@ -192,6 +202,8 @@ void free_analysis(sptrsv_gb300_handle_s* h) {
   free_layout(h->layout);
   free_table(h->tab_fwd);
   free_table(h->tab_adj);
+  free_pieces(h->pc_fwd);
+  free_pieces(h->pc_adj);
   free_values(h->v64);
   free_values(h->v32);
   h->staged64 = h->staged32 = false;
@@ -273,6 +285,8 @@ int build_layout(sptrsv_gb300_handle_s* h, int block, cudaStream_t s) {
   free_layout(h->layout);
   free_table(h->tab_fwd);
   free_table(h->tab_adj);
+  free_pieces(h->pc_fwd);
+  free_pieces(h->pc_adj);
   free_values(h->v64);
   free_values(h->v32);
   h->staged64 = h->staged32 = false;
@@ -419,6 +433,64 @@ int ensure_table(sptrsv_gb300_handle_s* h, bool adj, int cmax, int emax) {
   return build_table(h, t, adj ? h->out_cnt_host : h->dep_cnt_host, adj, cmax, emax);
 }
 
+// Piece table over a walk (see PieceTable): lists longer than `split` entries
+// are cut into min(32, ceil(len/split)) near-equal consecutive slices.
+int build_pieces(sptrsv_gb300_handle_s* h, PieceTable& t, const std::vector<int>& counts, bool reversed, int split,
+                 int chunk) {
+  free_pieces(t);
+  const int n = static_cast<int>(counts.size());
+  std::vector<long long> start((size_t)n + 1, 0);
+  for (int p = 0; p < n; ++p) start[p + 1] = start[p] + counts[p];
+  std::vector<int> walk, lo, hi;
+  walk.reserve((size_t)n + n / 8 + 32);
+  lo.reserve(walk.capacity());
+  hi.reserve(walk.capacity());
+  auto pad = [&]() {
+    while (walk.size() % 32) {
+      walk.push_back(-1);
+      lo.push_back(0);
+      hi.push_back(0);
+    }
+  };
+  for (int i = 0; i < n; ++i) {
+    const int p = reversed ? n - 1 - i : i;
+    const long long c = counts[p], e0 = start[p];
+    const int k = (split > 0 && c > split) ? static_cast<int>(std::min<long long>(32, (c + split - 1) / split)) : 1;
+    if (walk.size() % 32 + k > 32) pad();
+    for (int j = 0; j < k; ++j) {
+      walk.push_back(i);
+      lo.push_back(static_cast<int>(e0 + c * j / k));
+      hi.push_back(static_cast<int>(e0 + c * (j + 1) / k));
+    }
+  }
+  pad();
+  t.split = split;
+  t.segs_per_chunk = std::max(1, chunk / 32);
+  t.nseg = static_cast<int>(walk.size() / 32);
+  t.nchunks = (t.nseg + t.segs_per_chunk - 1) / t.segs_per_chunk;
+  std::vector<int> cbase(t.nchunks > 0 ? t.nchunks : 1, 0);
+  for (int c = 0; c < t.nchunks; ++c) cbase[c] = walk[(size_t)c * t.segs_per_chunk * 32];
+  const size_t np = walk.size() > 0 ? walk.size() : 1;
+  CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.walk), sizeof(int) * np));
+  CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.lo), sizeof(int) * np));
+  CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.hi), sizeof(int) * np));
+  CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.cbase), sizeof(int) * cbase.size()));
+  if (!walk.empty()) {
+    CUDA_TRY(cudaMemcpy(t.walk, walk.data(), sizeof(int) * walk.size(), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(t.lo, lo.data(), sizeof(int) * walk.size(), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(t.hi, hi.data(), sizeof(int) * walk.size(), cudaMemcpyHostToDevice));
+  }
+  CUDA_TRY(cudaMemcpy(t.cbase, cbase.data(), sizeof(int) * cbase.size(), cudaMemcpyHostToDevice));
+  h->device_bytes += sizeof(int) * (3 * np + cbase.size());
+  return SPTRSV_OK;
+}
+
+int ensure_pieces(sptrsv_gb300_handle_s* h, bool adj, int split, int chunk) {
+  PieceTable& t = adj ? h->pc_adj : h->pc_fwd;
+  if (t.walk && t.split == split && t.segs_per_chunk == std::max(1, chunk / 32)) return SPTRSV_OK;
+  return build_pieces(h, t, adj ? h->out_cnt_host : h->dep_cnt_host, adj, split, chunk);
+}
+
 // Largest per-chunk entry budget whose ring of stage buffers (plus the
 // shared-memory tier) fits one CTA's shared memory; 0 if none does.
 constexpr size_t kSmemCap = 220 * 1024;
@@ -504,6 +576,7 @@ ExecConfig pick_config(const sptrsv_gb300_handle_s* h, int rhs) {
   c.emax = h->emax_option;
   c.stages = h->stages_option;
   c.wsync = h->wsync;
+  c.split = h->split;
   return c;
 }
 
@@ -552,8 +625,13 @@ int solve_typed(sptrsv_gb300_handle_s* h, const Values<T>& V, int rhs, int layou
     CUDA_TRY(launch_pull_staged<T>(h->layout, V, adj ? h->tab_adj : h->tab_fwd, v, static_cast<T*>(h->xw.p), h->ctl,
                                    c, timeout_ns(h), h->num_sms, s, adj));
   } else {
+    const PieceTable* pc = nullptr;
+    if (rhs == 1 && c.wsync && !c.exact && c.split > 0 && !(adj && adj->grad)) {
+      ST_TRY(ensure_pieces(h, adj != nullptr, c.split, c.chunk));
+      pc = adj ? &h->pc_adj : &h->pc_fwd;
+    }
     CUDA_TRY(launch_pull<T>(h->layout, V, rhs, v, static_cast<T*>(h->xw.p), h->ctl, c, timeout_ns(h), h->num_sms,
-                            s, adj));
+                            s, adj, pc));
   }
   if (h->profile) {
     CUDA_TRY(cudaEventRecord(h->ev_exec[1], s));
@@ -711,6 +789,10 @@ int sptrsv_gb300_set_option(sptrsv_handle_t h, int option, long long value) {
     case SPTRSV_OPTION_WARP_SYNC:
       h->wsync = value != 0;
       return SPTRSV_OK;
+    case SPTRSV_OPTION_SPLIT:
+      if (value < 0 || (value > 0 && value < 4) || value > (1 << 20)) return SPTRSV_ERR_INVALID;
+      h->split = static_cast<int>(value);
+      return SPTRSV_OK;
     default:
       return SPTRSV_ERR_INVALID;
   }
@@ -736,6 +818,7 @@ int sptrsv_gb300_get_option(sptrsv_handle_t h, int option, long long* value) {
     case SPTRSV_OPTION_STAGES: *value = h->stages_option; break;
     case SPTRSV_OPTION_FUSED_GRAD: *value = h->fused_grad; break;
     case SPTRSV_OPTION_WARP_SYNC: *value = h->wsync; break;
+    case SPTRSV_OPTION_SPLIT: *value = h->split; break;
     default: return SPTRSV_ERR_INVALID;
   }
   return SPTRSV_OK;
@@ -1273,28 +1356,31 @@ int sptrsv_gb300_tune(sptrsv_handle_t h, const void* d_val, int dtype, int rhs, 
   if (!h->analysed) return SPTRSV_ERR_STATE;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   struct Cand {
-    int sched, order_block, chunk, staged, backoff, ctas, lanes, stages, wsync, block;
+    int sched, order_block, chunk, staged, backoff, ctas, lanes, stages, wsync, block, split;
   };
   const int n = h->n;
   const int big = INT_MAX;
   std::vector<Cand> cands;
+  const int sp = 32;  // split length of the warp-synchronous candidates
   if (rhs == 1) {
     // staged warp-specialised executor, level order
-    for (int bo : {0, 256}) cands.push_back({SCHED_PULL, big, 224, 1, bo, 0, 1, 2, 0, 256});
-    // warp-synchronous executor: level order, and blocked orders for deep narrow DAGs
-    for (int ch : {128, 256}) cands.push_back({SCHED_PULL, big, ch, 0, 128, 1, 1, 2, 1, ch});
-    for (int ob : {2048, 8192, 22624}) cands.push_back({SCHED_PULL, ob, ob, 0, 0, 0, 1, 2, 1, 128});
+    for (int bo : {0, 256}) cands.push_back({SCHED_PULL, big, 224, 1, bo, 0, 1, 2, 0, 256, sp});
+    // warp-synchronous executor (long lists split over lanes): level order, and
+    // blocked orders for deep narrow DAGs
+    for (int ch : {128, 256}) cands.push_back({SCHED_PULL, big, ch, 0, 128, 1, 1, 2, 1, ch, sp});
+    cands.push_back({SCHED_PULL, big, 256, 0, 128, 1, 1, 2, 1, 256, 0});
+    for (int ob : {2048, 8192, 22624}) cands.push_back({SCHED_PULL, ob, ob, 0, 0, 0, 1, 2, 1, 128, sp});
     // thread-per-unknown executor, level order
-    cands.push_back({SCHED_PULL, big, 256, 0, 128, 1, 1, 2, 0, 256});
-    cands.push_back({SCHED_LEVELSET, big, 256, 0, 256, 1, 8, 2, 0, 256});
-    cands.push_back({SCHED_PUSH, 1024, 1024, 0, 256, 0, 1, 2, 0, 256});
+    cands.push_back({SCHED_PULL, big, 256, 0, 128, 1, 1, 2, 0, 256, sp});
+    cands.push_back({SCHED_LEVELSET, big, 256, 0, 256, 1, 8, 2, 0, 256, sp});
+    cands.push_back({SCHED_PUSH, 1024, 1024, 0, 256, 0, 1, 2, 0, 256, sp});
   } else {
     // chunk 0 = one unknown per lane group
-    for (int bo : {64, 512}) cands.push_back({SCHED_PULL, big, 0, 0, bo, 0, 1, 2, 1, 256});
-    for (int ob : {1024, 4096}) cands.push_back({SCHED_PULL, ob, ob, 0, 0, 0, 1, 2, 1, 256});
-    cands.push_back({SCHED_PULL, big, 0, 0, 256, 0, 1, 2, 0, 256});
-    cands.push_back({SCHED_LEVELSET, big, 256, 0, 256, 1, 8, 2, 0, 256});
-    cands.push_back({SCHED_PUSH, big, 0, 0, 256, 0, 1, 2, 0, 256});
+    for (int bo : {64, 512}) cands.push_back({SCHED_PULL, big, 0, 0, bo, 0, 1, 2, 1, 256, sp});
+    for (int ob : {1024, 4096}) cands.push_back({SCHED_PULL, ob, ob, 0, 0, 0, 1, 2, 1, 256, sp});
+    cands.push_back({SCHED_PULL, big, 0, 0, 256, 0, 1, 2, 0, 256, sp});
+    cands.push_back({SCHED_LEVELSET, big, 256, 0, 256, 1, 8, 2, 0, 256, sp});
+    cands.push_back({SCHED_PUSH, big, 0, 0, 256, 0, 1, 2, 0, 256, sp});
   }
   (void)n;
   const int saved_check = h->sync_check, saved_profile = h->profile;
@@ -1317,6 +1403,7 @@ int sptrsv_gb300_tune(sptrsv_handle_t h, const void* d_val, int dtype, int rhs, 
     h->stages_option = c.stages;
     h->wsync = c.wsync;
     h->block_option = c.block;
+    h->split = c.split;
     int st = sptrsv_gb300_solve(h, d_val, dtype, rhs, layout, d_b, d_x, stream);
     if (st == SPTRSV_OK) st = check_device(h, s);
     if (st != SPTRSV_OK) continue;  // a candidate that fails (or times out) is skipped
@@ -1355,6 +1442,7 @@ int sptrsv_gb300_tune(sptrsv_handle_t h, const void* d_val, int dtype, int rhs, 
   h->stages_option = c.stages;
   h->wsync = c.wsync;
   h->block_option = c.block;
+  h->split = c.split;
   ST_TRY(ensure_layout(h, s));
   ST_TRY(stage_values(h, d_val, dtype, s, false));
   if (best_ms) *best_ms = best;

@@ -60,6 +60,14 @@ struct ExecArgs {
   unsigned sleep_min, sleep_max;  // backoff of global polls (ns)
   const int* level_ptr;
   int nlevels;
+  // split-list work units (k_pull_wsync_split): piece i covers entries
+  // [pc_lo[i], pc_hi[i]) of walk index pc_walk[i] (-1: padding); 32 pieces per
+  // warp segment, pc_spc segments per chunk, chunk c starting at walk pc_cbase[c]
+  const int* pc_walk;
+  const int* pc_lo;
+  const int* pc_hi;
+  const int* pc_cbase;
+  int pc_spc, pc_nseg;
 };
 
 template <typename T>
@@ -307,6 +315,165 @@ __global__ void __launch_bounds__(256) k_pull_wsync(ExecArgs<T> a) {
           }
           if ((any_global || (++idle & 255u) == 0u) && !wb.poll(a.ctl, p)) fail = true;
           if (__any_sync(0xffffffffu, fail)) {
+            fail = true;
+            break;
+          }
+        } else {
+          nap = a.sleep_min;
+        }
+      }
+    }
+    if (__syncthreads_or(fail)) break;
+  }
+  leave(a.ctl);
+}
+
+// ------------------------------------------------------------------ pull, warp-synchronous, split lists
+// As k_pull_wsync (fast arithmetic), over pieces: a dependency list longer than
+// the split length is cut into up to 32 consecutive slices of its ready-ordered
+// list, held by adjacent lanes of one warp segment. Every lane accumulates its
+// slice in lockstep with the others; once all slices of an unknown are in, a
+// segmented suffix sum over its lanes hands the head lane the value to publish.
+// A 1000-entry list then takes about as many lockstep iterations as a
+// 30-entry one, and only its last slice waits on the latest dependencies.
+template <typename T, bool ADJ>
+__global__ void __launch_bounds__(256) k_pull_wsync_split(ExecArgs<T> a) {
+  using F = Flag<T>;
+  using Bits = typename F::Bits;
+  constexpr int U = 4;
+  constexpr unsigned kFull = 0xffffffffu;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* s_x = reinterpret_cast<T*>(smem_raw);
+  __shared__ unsigned s_chunk;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int* __restrict__ lpos = ADJ ? a.out_pos_f : a.dep_pos_f;
+  const T* __restrict__ vals = ADJ ? a.out_w : a.dep_w;
+  const int last = a.n - 1;
+  const unsigned at_or_below = (2u << lane) - 1u;  // lanes 0..lane (wraps to all lanes for lane 31)
+  for (;;) {
+    const unsigned c = next_chunk(a.ctl, a.nchunks, &s_chunk);
+    if (c >= (unsigned)a.nchunks) break;
+    const int seg0 = static_cast<int>(c) * a.pc_spc;
+    const int seg1 = min(seg0 + a.pc_spc, a.pc_nseg);
+    const int cbase = a.pc_cbase[c];
+    if (a.smem_tier)
+      for (int i = threadIdx.x; i < (seg1 - seg0) * 32; i += blockDim.x) *reinterpret_cast<Bits*>(&s_x[i]) = F::EMPTY;
+    __syncthreads();
+    bool fail = false;
+    for (int seg = seg0 + warp; seg < seg1 && !fail; seg += nwarps) {
+      const int pi = seg * 32 + lane;
+      const int walk = a.pc_walk[pi];
+      int e = a.pc_lo[pi];
+      const int e1 = a.pc_hi[pi];
+      const int prev = __shfl_up_sync(kFull, walk, 1);
+      const bool valid = walk >= 0;
+      const bool head = valid && (lane == 0 || prev != walk);
+      const unsigned heads = __ballot_sync(kFull, head);
+      const unsigned valids = __ballot_sync(kFull, valid);
+      const bool split = heads != valids;  // some unknown spans several lanes
+      // this lane's group: from its head (at or below) to the lane before the next head
+      const unsigned above = heads & ~at_or_below;
+      const int ge = above ? __ffs(above) - 2 : 31 - __clz(valids);
+      const int gs = valid ? 31 - __clz(heads & at_or_below) : lane;
+      // head lanes: the lanes of their unknown (ge >= lane >= 0 there)
+      const unsigned gmask = head ? (ge >= 31 ? kFull : ((2u << ge) - 1u)) & ~((1u << lane) - 1u) : 0u;
+      const int p = ADJ ? last - walk : walk;
+      int row = 0;
+      T acc = T(0);
+      if (head) {
+        row = a.perm[p];
+        acc = a.b[(long long)row * a.b_si] * a.rcp[p];
+      }
+      auto slot = [&](int q) {
+        const int qr = ADJ ? last - q : q;
+        return (a.smem_tier && qr >= cbase) ? qr - cbase : -1;
+      };
+      int q[U], ls[U];
+      T w[U];
+      Bits bits[U];
+      unsigned todo = 0u;
+      auto load_batch = [&]() {
+        todo = 0u;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int ee = e + u;
+          q[u] = ee < e1 ? lpos[ee] : -1;
+          w[u] = ee < e1 ? vals[ee] : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          ls[u] = -1;
+          bits[u] = F::EMPTY;
+          if (q[u] >= 0) {
+            ls[u] = slot(q[u]);
+            bits[u] = ls[u] >= 0 ? F::load_shared(&s_x[ls[u]]) : F::load(&a.xw[q[u]]);
+            todo |= 1u << u;
+          }
+        }
+      };
+      bool sdone = !valid || e >= e1;  // slice consumed
+      bool done = !valid;              // unknown published
+      if (!sdone) load_batch();
+      WaitBudget wb(a.timeout_ns);
+      unsigned nap = a.sleep_min, idle = 0u;
+      for (;;) {
+        bool progress = false, global_wait = false;
+        if (!sdone) {
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            if (!(todo & (1u << u))) continue;
+            if (bits[u] != F::EMPTY) {
+              acc = fma(-w[u], F::value(bits[u]), acc);
+              todo &= ~(1u << u);
+              progress = true;
+            } else if (ls[u] < 0) {
+              global_wait = true;
+            }
+          }
+          if (!todo) {
+            e += U;
+            if (e < e1) load_batch();
+            else sdone = true;
+            progress = true;
+          } else {
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+              if ((todo & (1u << u)) && bits[u] == F::EMPTY)
+                bits[u] = ls[u] >= 0 ? F::load_shared(&s_x[ls[u]]) : F::load(&a.xw[q[u]]);
+          }
+        }
+        // publish every unknown whose slices are all in
+        const unsigned sd = __ballot_sync(kFull, sdone);
+        const bool ready = head && !done && (sd & gmask) == gmask;
+        if (__any_sync(kFull, ready)) {
+          T xi = acc;
+          if (split) {
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+              const T t = __shfl_down_sync(kFull, xi, off);
+              if (lane + off <= ge) xi += t;
+            }
+          }
+          if (ready) {
+            if (a.smem_tier) F::store_shared(&s_x[walk - cbase], xi);
+            F::store(&a.xw[p], xi);
+            a.x[(long long)row * a.x_si] = xi;
+            done = true;
+            progress = true;
+          }
+          const unsigned pub = __ballot_sync(kFull, head && done);
+          if (valid && !head) done = (pub >> gs) & 1u;
+        }
+        if (__all_sync(kFull, done)) break;
+        const bool any_progress = __any_sync(kFull, progress);
+        const bool any_global = __any_sync(kFull, global_wait);
+        if (!any_progress) {
+          if (any_global && a.sleep_max) {
+            __nanosleep(nap);
+            nap = nap * 2u < a.sleep_max ? nap * 2u : a.sleep_max;
+          }
+          if ((any_global || (++idle & 255u) == 0u) && !wb.poll(a.ctl, p)) fail = true;
+          if (__any_sync(kFull, fail)) {
             fail = true;
             break;
           }
@@ -879,6 +1046,8 @@ template <typename T, bool ADJ>
 cudaError_t launch_pull_impl(ExecArgs<T>& a, int rhs, const ExecConfig& cfg, size_t smem, int num_sms,
                              cudaStream_t s) {
   const int block = cfg.block;
+  if (rhs == 1 && cfg.wsync && !cfg.exact && a.grad == nullptr && a.pc_walk != nullptr)
+    return run(k_pull_wsync_split<T, ADJ>, a, block, smem, num_sms, s);
   if (rhs == 1 && cfg.wsync) {
     if (cfg.exact) return run(k_pull_wsync<T, true, ADJ>, a, block, smem, num_sms, s);
     return run(k_pull_wsync<T, false, ADJ>, a, block, smem, num_sms, s);
@@ -920,9 +1089,19 @@ cudaError_t launch_pull_impl(ExecArgs<T>& a, int rhs, const ExecConfig& cfg, siz
 template <typename T>
 cudaError_t launch_pull(const Layout& L, const Values<T>& V, int rhs, const VecView<T>& v, T* xw, DeviceCtl* ctl,
                         const ExecConfig& cfg, unsigned long long timeout_ns, int num_sms, cudaStream_t s,
-                        const AdjointArgs<T>* adj) {
+                        const AdjointArgs<T>* adj, const PieceTable* pc) {
   if (L.n == 0) return cudaSuccess;
   ExecArgs<T> a = make_args<T>(L, V, rhs, v, cfg.chunk);
+  const bool use_pc = pc && pc->walk && rhs == 1 && cfg.wsync && !cfg.exact && !(adj && adj->grad);
+  if (use_pc) {
+    a.pc_walk = pc->walk;
+    a.pc_lo = pc->lo;
+    a.pc_hi = pc->hi;
+    a.pc_cbase = pc->cbase;
+    a.pc_spc = pc->segs_per_chunk;
+    a.pc_nseg = pc->nseg;
+    a.nchunks = pc->nchunks;
+  }
   a.xw = xw;
   a.ctl = ctl;
   a.timeout_ns = timeout_ns;
@@ -932,7 +1111,7 @@ cudaError_t launch_pull(const Layout& L, const Values<T>& V, int rhs, const VecV
   size_t smem = 0;
   a.smem_tier = 0;
   if (cfg.smem_tier) {
-    smem = pull_smem_bytes(cfg.chunk, rhs, sizeof(T));
+    smem = use_pc ? (size_t)pc->segs_per_chunk * 32 * sizeof(T) : pull_smem_bytes(cfg.chunk, rhs, sizeof(T));
     if (smem <= 200 * 1024) a.smem_tier = 1;
     else smem = 0;
   }
@@ -1128,7 +1307,7 @@ cudaError_t launch_ref_executor(const int* col_ptr, const int* row_idx, const T*
 #define SPTRSV_INSTANTIATE(T)                                                                                    \
   template cudaError_t launch_pull<T>(const Layout&, const Values<T>&, int, const VecView<T>&, T*, DeviceCtl*,   \
                                       const ExecConfig&, unsigned long long, int, cudaStream_t,                  \
-                                      const AdjointArgs<T>*);                                                    \
+                                      const AdjointArgs<T>*, const PieceTable*);                                 \
   template cudaError_t launch_push<T>(const Layout&, const Values<T>&, int, const VecView<T>&, T*, unsigned*,    \
                                       DeviceCtl*, const ExecConfig&, unsigned long long, int, cudaStream_t);     \
   template cudaError_t launch_levelset<T>(const Layout&, const Values<T>&, int, const VecView<T>&, T*,           \

@@ -36,6 +36,7 @@ struct ExecConfig {
   int emax = 0;           // staged: dependency entries per chunk (0: automatic)
   int stages = 2;         // staged: chunk buffers in the producer/consumer ring
   int wsync = 0;          // unstaged one-rhs pull: warp-synchronous lanes (k_pull_wsync)
+  int split = 0;          // warp-synchronous, fast arithmetic: split lists longer than this (0: never)
 };
 
 // Work units of the staged executor: chunk k covers walk indices
@@ -47,6 +48,18 @@ struct ChunkTable {
   int nchunks = 0, cmax = 0, emax = 0;
   int* start = nullptr;   // device [nchunks+1]
   int* mode = nullptr;    // device [nchunks]
+};
+
+// Work units of the split-list warp-synchronous executor: a walk's dependency
+// lists cut into pieces of at most `split` entries (at most 32 per unknown),
+// 32 pieces per warp segment with no unknown straddling two segments (padding
+// pieces have walk -1), segs_per_chunk segments per chunk.
+struct PieceTable {
+  int split = 0, segs_per_chunk = 0, nseg = 0, nchunks = 0;
+  int* walk = nullptr;    // device [nseg*32]
+  int* lo = nullptr;      // device [nseg*32] first entry
+  int* hi = nullptr;      // device [nseg*32] end entry
+  int* cbase = nullptr;   // device [nchunks] first walk index of each chunk
 };
 
 // Solve-time description of one right-hand-side block. Element (i, k) of b
@@ -168,7 +181,8 @@ struct AdjointArgs {
 template <typename T>
 cudaError_t launch_pull(const Layout& L, const Values<T>& V, int rhs, const VecView<T>& v, T* xw,
                         DeviceCtl* ctl, const ExecConfig& cfg, unsigned long long timeout_ns,
-                        int num_sms, cudaStream_t s, const AdjointArgs<T>* adj = nullptr);
+                        int num_sms, cudaStream_t s, const AdjointArgs<T>* adj = nullptr,
+                        const PieceTable* pc = nullptr);
 template <typename T>
 cudaError_t launch_push(const Layout& L, const Values<T>& V, int rhs, const VecView<T>& v, T* left_sum,
                         unsigned* counters, DeviceCtl* ctl, const ExecConfig& cfg,

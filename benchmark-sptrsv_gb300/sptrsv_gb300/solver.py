@@ -97,7 +97,7 @@ class SyncFreeSolver:
                  exact: bool = False, smem_tier: bool = True, timeout_ms: int = 1000, sync_check: bool = True,
                  profile: bool = False, block: int = 0, backoff_ns: int | None = None, ctas_per_sm: int = 0,
                  staged: bool = True, stage_entries: int = 0, stages: int = 2, warp_sync: bool = False,
-                 fused_grad: bool = False, stream=None):
+                 split: int | None = None, fused_grad: bool = False, stream=None):
         torch = _torch()
         self._lib = load()
         self.device = torch.device("cuda", torch.cuda.current_device())
@@ -147,6 +147,8 @@ class SyncFreeSolver:
         self.set_option(_lib.OPTION_STAGE_ENTRIES, int(stage_entries))
         self.set_option(_lib.OPTION_STAGES, int(stages))
         self.set_option(_lib.OPTION_WARP_SYNC, int(warp_sync))
+        if split is not None:
+            self.set_option(_lib.OPTION_SPLIT, int(split))
         self.set_option(_lib.OPTION_FUSED_GRAD, int(fused_grad))
         self._stream = stream
         self.analyse()
@@ -309,7 +311,7 @@ class SyncFreeSolver:
         return dval
 
     TUNED_OPTIONS = ("SCHEDULE", "ORDER_BLOCK", "CHUNK", "STAGED", "BACKOFF_NS", "CTAS_PER_SM", "LANES", "STAGES",
-                     "WARP_SYNC", "BLOCK")
+                     "WARP_SYNC", "BLOCK", "SPLIT")
 
     def tune(self, b, values=None, reps: int = 3) -> dict:
         """Autotune the executor on this right-hand side; returns the chosen options and time."""

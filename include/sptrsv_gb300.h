@@ -95,8 +95,11 @@ typedef enum sptrsv_option {
   SPTRSV_OPTION_FUSED_GRAD = 15,  /* sptrsv_gb300_solve_adjoint with d_dval: 1 = the transposed-solve
                                      kernel writes the gradient as each lambda is known; 0 (default) =
                                      transposed solve, then one gradient pass over the stored pattern */
-  SPTRSV_OPTION_WARP_SYNC = 16    /* one-rhs pull without staging: 1 = the 32 lanes of a warp advance in
+  SPTRSV_OPTION_WARP_SYNC = 16,   /* one-rhs pull without staging: 1 = the 32 lanes of a warp advance in
                                      lockstep (fast in-warp dependency chains; blocked orders) */
+  SPTRSV_OPTION_SPLIT = 17        /* warp-synchronous one-rhs pull (not exact): dependency lists longer
+                                     than this many entries are split over up to 32 lanes (default 32;
+                                     0 = one lane per unknown) */
 } sptrsv_option;
 
 typedef struct sptrsv_info {

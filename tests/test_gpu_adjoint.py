@@ -27,7 +27,9 @@ def relerr(x, ref):
                                  dict(fused_grad=1), dict(fused_grad=1, staged=False, lanes=4),
                                  dict(staged=False, warp_sync=True, fused_grad=1),
                                  dict(staged=False, warp_sync=True, exact=True, order_block=64, chunk=64),
-                                 dict(staged=False, warp_sync=True, order_block=128, chunk=128)],
+                                 dict(staged=False, warp_sync=True, order_block=128, chunk=128),
+                                 dict(staged=False, warp_sync=True, split=4),
+                                 dict(staged=False, warp_sync=True, split=0)],
                          ids=lambda c: "-".join(f"{k}{v}" for k, v in c.items()))
 def test_adjoint_and_gradient_vs_oracle(cuda, name, cfg):
     from oracle import oracle

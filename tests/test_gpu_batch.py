@@ -36,7 +36,8 @@ def _solver(systems, **kw):
                                  dict(schedule=1), dict(schedule=3), dict(staged=False, lanes=4),
                                  dict(chunk=40, stage_entries=40, stages=3),
                                  dict(staged=False, warp_sync=True), dict(staged=False, warp_sync=True,
-                                                                          order_block=256, chunk=256)],
+                                                                          order_block=256, chunk=256),
+                                 dict(staged=False, warp_sync=True, split=4)],
                          ids=lambda c: "-".join(f"{k}{v}" for k, v in c.items()) or "default")
 @pytest.mark.parametrize("rhs", [1, 4])
 def test_batch_matches_per_system_oracle(cuda, oracle_port, systems, cfg, rhs):

@@ -93,6 +93,20 @@ def test_handle_timeout_option(cuda):
         s.set_option(_lib.OPTION_TIMEOUT_MS, 0)
 
 
+def test_split_option_validated(cuda):
+    """Split lengths below 4 (other than 0 = off) are rejected; valid ones read back."""
+    from sptrsv_gb300 import _lib, matgen, SyncFreeSolver, SptrsvError
+    m = matgen.poisson_band(500, 3.0, 50, seed=2)
+    s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, 0, values=m.val)
+    assert s.get_option(_lib.OPTION_SPLIT) == 32
+    for bad in (-1, 1, 3):
+        with pytest.raises(SptrsvError):
+            s.set_option(_lib.OPTION_SPLIT, bad)
+    for ok in (0, 4, 64):
+        s.set_option(_lib.OPTION_SPLIT, ok)
+        assert s.get_option(_lib.OPTION_SPLIT) == ok
+
+
 @pytest.mark.parametrize("cfg", [dict(schedule=2), dict(schedule=1)])
 def test_wait_budget_expires_cleanly_then_recovers(cuda, cfg):
     """Natural order on the 2-D Laplacian makes single waits last far longer than

@@ -55,6 +55,10 @@ CONFIGS = [
     dict(schedule=2, staged=False, warp_sync=True),
     dict(schedule=2, staged=False, warp_sync=True, order_block=64, chunk=64, block=64),
     dict(schedule=2, staged=False, warp_sync=True, order_block=1, chunk=100, backoff_ns=0),
+    dict(schedule=2, staged=False, warp_sync=True, split=0),
+    dict(schedule=2, staged=False, warp_sync=True, split=4),
+    dict(schedule=2, staged=False, warp_sync=True, split=5, chunk=32, smem_tier=False),
+    dict(schedule=2, staged=False, warp_sync=True, split=4, order_block=64, chunk=96, block=64),
     dict(schedule=3, lanes=1),
     dict(schedule=3, lanes=8),
 ]
