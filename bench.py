@@ -427,9 +427,20 @@ def run_batch(args):
     import torch
 
     from oracle import oracle
-    from sptrsv_gb300 import SyncFreeSolver, matgen
+    from sptrsv_gb300 import SyncFreeSolver, matgen, shard
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     t0 = time.perf_counter()
-    systems = matgen.batch_uneven(count=args.batch_count, seed=3)
+    systems_all = matgen.batch_uneven(count=args.batch_count, seed=3)
+    # independent systems shard over ranks with no exchange (nnz-balanced assignment)
+    mine = shard.shard_of([m.nnz for m in systems_all], world, rank)
+    systems = [systems_all[k] for k in mine]
     tgen = time.perf_counter() - t0
     rhs = 4
     rng = np.random.default_rng(4)
@@ -474,9 +485,24 @@ def run_batch(args):
         m = systems[k]
         ref = oracle.port().solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, bs[k])
         err = max(err, float(np.abs(xr_h[off[k]:off[k + 1]] - ref).max() / np.abs(ref).max()))
-    nsys = len(systems)
+    if dist is not None:
+        # whole-job time = the slowest rank
+        t = torch.tensor([t_mixed, t_b64, t_per], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_mixed, t_b64, t_per = (float(v) for v in t.tolist())
+        tot = torch.tensor([ntot, nnz], dtype=torch.float64, device="cuda")
+        dist.all_reduce(tot)
+        ntot, nnz = (int(v) for v in tot.tolist())
+        e = torch.tensor([err], dtype=torch.float64, device="cuda")
+        dist.all_reduce(e, op=dist.ReduceOp.MAX)
+        err = float(e.item())
+        dist.destroy_process_group()
+        if rank != 0:
+            return 0
+    nsys = len(systems_all)
     line = {"workload": "batch", "metric": "batched solves/s (FP32+FP64 refinement, one persistent launch per pass)",
             "value": round(nsys / (t_mixed * 1e-3), 2), "unit": "systems/s", "higher_is_better": True,
+            "n_gpus": world, "scaling": "strong" if world > 1 else None,
             "systems": nsys, "n_total": ntot, "nnz_total": nnz, "rhs": rhs,
             "nlevels_batch": s.info()["nlevels"], "tuned": tuned,
             "mixed_batched_ms": round(t_mixed, 3), "refine_steps": iters, "fp64_batched_ms": round(t_b64, 3),
@@ -485,7 +511,9 @@ def run_batch(args):
             "speedup_vs_batched_fp64": round(t_b64 / t_mixed, 3),
             "fwd_err_vs_oracle_sampled": err, "sampled_systems": len(sample),
             "generate_s": round(tgen, 1), "analyse_s": round(tan, 2),
-            "config": {"workload": f"{nsys} systems, rhs=4, FP32+FP64 refinement"}}
+            "config": {"workload": f"{nsys} systems, rhs=4, FP32+FP64 refinement",
+                       "parallelism": f"systems sharded over {world} rank(s), nnz-balanced" if world > 1
+                       else "one GPU"}}
     print(json.dumps(line), flush=True)
     return 0
 
