@@ -145,6 +145,7 @@ void free_table(ChunkTable& t) {
 
 void free_pieces(PieceTable& t) {
   if (t.walk) cudaFree(t.walk);
+  if (t.row) cudaFree(t.row);
   if (t.lo) cudaFree(t.lo);
   if (t.hi) cudaFree(t.hi);
   if (t.cbase) cudaFree(t.cbase);
@@ -436,7 +437,7 @@ int ensure_table(sptrsv_gb300_handle_s* h, bool adj, int cmax, int emax) {
 // Piece table over a walk (see PieceTable): lists longer than `split` entries
 // are cut into min(32, ceil(len/split)) near-equal consecutive slices.
 int build_pieces(sptrsv_gb300_handle_s* h, PieceTable& t, const std::vector<int>& counts, bool reversed, int split,
-                 int chunk) {
+                 int chunk, cudaStream_t s) {
   free_pieces(t);
   const int n = static_cast<int>(counts.size());
   std::vector<long long> start((size_t)n + 1, 0);
@@ -472,23 +473,35 @@ int build_pieces(sptrsv_gb300_handle_s* h, PieceTable& t, const std::vector<int>
   for (int c = 0; c < t.nchunks; ++c) cbase[c] = walk[(size_t)c * t.segs_per_chunk * 32];
   const size_t np = walk.size() > 0 ? walk.size() : 1;
   CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.walk), sizeof(int) * np));
+  CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.row), sizeof(int) * np));
   CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.lo), sizeof(int) * np));
   CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.hi), sizeof(int) * np));
   CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.cbase), sizeof(int) * cbase.size()));
   if (!walk.empty()) {
     CUDA_TRY(cudaMemcpy(t.walk, walk.data(), sizeof(int) * walk.size(), cudaMemcpyHostToDevice));
+    // row of each piece's unknown: perm gathered on the device (padding reads position 0)
+    std::vector<int> posv(walk.size());
+    for (size_t i = 0; i < walk.size(); ++i)
+      posv[i] = walk[i] < 0 ? 0 : (reversed ? n - 1 - walk[i] : walk[i]);
+    int* pos_dev = nullptr;
+    CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&pos_dev), sizeof(int) * posv.size()));
+    cudaError_t err = cudaMemcpyAsync(pos_dev, posv.data(), sizeof(int) * posv.size(), cudaMemcpyHostToDevice, s);
+    if (err == cudaSuccess) err = launch_gather_int(h->layout.perm, pos_dev, t.row, static_cast<int>(posv.size()), s);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+    cudaFree(pos_dev);
+    CUDA_TRY(err);
     CUDA_TRY(cudaMemcpy(t.lo, lo.data(), sizeof(int) * walk.size(), cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(t.hi, hi.data(), sizeof(int) * walk.size(), cudaMemcpyHostToDevice));
   }
   CUDA_TRY(cudaMemcpy(t.cbase, cbase.data(), sizeof(int) * cbase.size(), cudaMemcpyHostToDevice));
-  h->device_bytes += sizeof(int) * (3 * np + cbase.size());
+  h->device_bytes += sizeof(int) * (4 * np + cbase.size());
   return SPTRSV_OK;
 }
 
-int ensure_pieces(sptrsv_gb300_handle_s* h, bool adj, int split, int chunk) {
+int ensure_pieces(sptrsv_gb300_handle_s* h, bool adj, int split, int chunk, cudaStream_t s) {
   PieceTable& t = adj ? h->pc_adj : h->pc_fwd;
   if (t.walk && t.split == split && t.segs_per_chunk == std::max(1, chunk / 32)) return SPTRSV_OK;
-  return build_pieces(h, t, adj ? h->out_cnt_host : h->dep_cnt_host, adj, split, chunk);
+  return build_pieces(h, t, adj ? h->out_cnt_host : h->dep_cnt_host, adj, split, chunk, s);
 }
 
 // Largest per-chunk entry budget whose ring of stage buffers (plus the
@@ -627,7 +640,7 @@ int solve_typed(sptrsv_gb300_handle_s* h, const Values<T>& V, int rhs, int layou
   } else {
     const PieceTable* pc = nullptr;
     if (rhs == 1 && c.wsync && !c.exact && c.split > 0 && !(adj && adj->grad)) {
-      ST_TRY(ensure_pieces(h, adj != nullptr, c.split, c.chunk));
+      ST_TRY(ensure_pieces(h, adj != nullptr, c.split, c.chunk, s));
       pc = adj ? &h->pc_adj : &h->pc_fwd;
     }
     CUDA_TRY(launch_pull<T>(h->layout, V, rhs, v, static_cast<T*>(h->xw.p), h->ctl, c, timeout_ns(h), h->num_sms,

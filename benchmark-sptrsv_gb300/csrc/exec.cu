@@ -64,6 +64,7 @@ struct ExecArgs {
   // [pc_lo[i], pc_hi[i]) of walk index pc_walk[i] (-1: padding); 32 pieces per
   // warp segment, pc_spc segments per chunk, chunk c starting at walk pc_cbase[c]
   const int* pc_walk;
+  const int* pc_row;    // row of the piece's unknown (perm of its position)
   const int* pc_lo;
   const int* pc_hi;
   const int* pc_cbase;
@@ -218,17 +219,29 @@ __global__ void __launch_bounds__(256) k_pull_wsync(ExecArgs<T> a) {
       for (int i = threadIdx.x; i < len; i += blockDim.x) *reinterpret_cast<Bits*>(&s_x[i]) = F::EMPTY;
     __syncthreads();
     bool fail = false;
+    // row and list bounds of this warp's next segment are loaded one segment ahead
+    int n_row = 0, n_e = 0, n_e1 = 0;
+    auto fetch = [&](int sg) {
+      const int jj = sg * 32 + lane;
+      if (jj < len) {
+        const int pp = ADJ ? last - (base + jj) : base + jj;
+        n_row = a.perm[pp];
+        n_e = lptr[pp];
+        n_e1 = lptr[pp + 1];
+      }
+    };
+    if (warp * 32 < len) fetch(warp);
     for (int seg = warp; seg * 32 < len && !fail; seg += nwarps) {
       const int j = seg * 32 + lane;
       bool done = j >= len;
       const int pr = base + j;
       const int p = ADJ ? last - pr : pr;
-      int row = 0, e = 0, e1 = 0;
+      const int row = n_row;
+      int e = n_e;
+      const int e1 = n_e1;
+      if ((seg + nwarps) * 32 < len) fetch(seg + nwarps);
       T bi = T(0), sc = T(0), acc = T(0);
       if (!done) {
-        row = a.perm[p];
-        e = lptr[p];
-        e1 = lptr[p + 1];
         bi = a.b[(long long)row * a.b_si];
         sc = EXACT ? a.diag[p] : a.rcp[p];
         acc = EXACT ? T(0) : bi * sc;
@@ -360,11 +373,27 @@ __global__ void __launch_bounds__(256) k_pull_wsync_split(ExecArgs<T> a) {
       for (int i = threadIdx.x; i < (seg1 - seg0) * 32; i += blockDim.x) *reinterpret_cast<Bits*>(&s_x[i]) = F::EMPTY;
     __syncthreads();
     bool fail = false;
+    // piece data of this warp's next segment is loaded one segment ahead
+    int n_walk = -1, n_lo = 0, n_hi = 0, n_row = 0;
+    if (seg0 + warp < seg1) {
+      const int pi = (seg0 + warp) * 32 + lane;
+      n_walk = a.pc_walk[pi];
+      n_lo = a.pc_lo[pi];
+      n_hi = a.pc_hi[pi];
+      n_row = a.pc_row[pi];
+    }
     for (int seg = seg0 + warp; seg < seg1 && !fail; seg += nwarps) {
-      const int pi = seg * 32 + lane;
-      const int walk = a.pc_walk[pi];
-      int e = a.pc_lo[pi];
-      const int e1 = a.pc_hi[pi];
+      const int walk = n_walk;
+      int e = n_lo;
+      const int e1 = n_hi;
+      const int row = n_row;
+      if (seg + nwarps < seg1) {
+        const int pn = (seg + nwarps) * 32 + lane;
+        n_walk = a.pc_walk[pn];
+        n_lo = a.pc_lo[pn];
+        n_hi = a.pc_hi[pn];
+        n_row = a.pc_row[pn];
+      }
       const int prev = __shfl_up_sync(kFull, walk, 1);
       const bool valid = walk >= 0;
       const bool head = valid && (lane == 0 || prev != walk);
@@ -378,12 +407,8 @@ __global__ void __launch_bounds__(256) k_pull_wsync_split(ExecArgs<T> a) {
       // head lanes: the lanes of their unknown (ge >= lane >= 0 there)
       const unsigned gmask = head ? (ge >= 31 ? kFull : ((2u << ge) - 1u)) & ~((1u << lane) - 1u) : 0u;
       const int p = ADJ ? last - walk : walk;
-      int row = 0;
       T acc = T(0);
-      if (head) {
-        row = a.perm[p];
-        acc = a.b[(long long)row * a.b_si] * a.rcp[p];
-      }
+      if (head) acc = a.b[(long long)row * a.b_si] * a.rcp[p];
       auto slot = [&](int q) {
         const int qr = ADJ ? last - q : q;
         return (a.smem_tier && qr >= cbase) ? qr - cbase : -1;
@@ -443,26 +468,32 @@ __global__ void __launch_bounds__(256) k_pull_wsync_split(ExecArgs<T> a) {
           }
         }
         // publish every unknown whose slices are all in
-        const unsigned sd = __ballot_sync(kFull, sdone);
-        const bool ready = head && !done && (sd & gmask) == gmask;
-        if (__any_sync(kFull, ready)) {
-          T xi = acc;
-          if (split) {
+        if (split) {
+          const unsigned sd = __ballot_sync(kFull, sdone);
+          const bool ready = head && !done && (sd & gmask) == gmask;
+          if (__any_sync(kFull, ready)) {
+            T xi = acc;
 #pragma unroll
             for (int off = 1; off < 32; off <<= 1) {
               const T t = __shfl_down_sync(kFull, xi, off);
               if (lane + off <= ge) xi += t;
             }
+            if (ready) {
+              if (a.smem_tier) F::store_shared(&s_x[walk - cbase], xi);
+              F::store(&a.xw[p], xi);
+              a.x[(long long)row * a.x_si] = xi;
+              done = true;
+              progress = true;
+            }
+            const unsigned pub = __ballot_sync(kFull, head && done);
+            if (valid && !head) done = (pub >> gs) & 1u;
           }
-          if (ready) {
-            if (a.smem_tier) F::store_shared(&s_x[walk - cbase], xi);
-            F::store(&a.xw[p], xi);
-            a.x[(long long)row * a.x_si] = xi;
-            done = true;
-            progress = true;
-          }
-          const unsigned pub = __ballot_sync(kFull, head && done);
-          if (valid && !head) done = (pub >> gs) & 1u;
+        } else if (sdone && !done) {  // one lane per unknown
+          if (a.smem_tier) F::store_shared(&s_x[walk - cbase], acc);
+          F::store(&a.xw[p], acc);
+          a.x[(long long)row * a.x_si] = acc;
+          done = true;
+          progress = true;
         }
         if (__all_sync(kFull, done)) break;
         const bool any_progress = __any_sync(kFull, progress);
@@ -1095,6 +1126,7 @@ cudaError_t launch_pull(const Layout& L, const Values<T>& V, int rhs, const VecV
   const bool use_pc = pc && pc->walk && rhs == 1 && cfg.wsync && !cfg.exact && !(adj && adj->grad);
   if (use_pc) {
     a.pc_walk = pc->walk;
+    a.pc_row = pc->row;
     a.pc_lo = pc->lo;
     a.pc_hi = pc->hi;
     a.pc_cbase = pc->cbase;

@@ -57,6 +57,7 @@ struct ChunkTable {
 struct PieceTable {
   int split = 0, segs_per_chunk = 0, nseg = 0, nchunks = 0;
   int* walk = nullptr;    // device [nseg*32]
+  int* row = nullptr;     // device [nseg*32] row of the unknown (perm of its position; 0 for padding)
   int* lo = nullptr;      // device [nseg*32] first entry
   int* hi = nullptr;      // device [nseg*32] end entry
   int* cbase = nullptr;   // device [nchunks] first walk index of each chunk
