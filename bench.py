@@ -19,7 +19,10 @@ Arms:
                    oracle: a C restatement of SpTRSV_cuda/sptrsv_syncfree_serialref.h,
                    or the reference build where it exists), the four solves of a
                    step run concurrently on four host threads.
-Multi-GPU: every rank solves the same workload independently (replicas).
+Multi-GPU: every rank solves the same workload independently (replicas);
+the batch workload instead shards its systems over the ranks (nnz-balanced).
+Profiling runs: --scale shrinks the systems, --cases picks a subset, and
+--opt KEY=VALUE fixes a solver option (the autotuner is then skipped).
 
 Other workloads (--workload; each prints one JSON line of its own metric):
   multi_rhs  n = 1,000,000, Poisson(9) off-diagonals in a band of 20,000,
@@ -60,7 +63,10 @@ def bytes_pass(n: int, nnz: int, rhs: int = 1, sv: int = 8, sx: int = 8) -> int:
     return 4 * (n + 1) + nnz * (4 + sv) + n * rhs * 2 * sx
 
 
-def make_cases(scale: float = 1.0):
+CASE_NAMES = ("laplace_fwd", "laplace_bwd", "powerlaw_fwd", "powerlaw_bwd")
+
+
+def make_cases(scale: float = 1.0, only=None):
     from sptrsv_gb300 import matgen
     if scale == 1.0:
         lap = matgen.system_laplace_2m(lower=True)
@@ -72,6 +78,8 @@ def make_cases(scale: float = 1.0):
     cases = []
     for name, m in (("laplace_fwd", lap), ("laplace_bwd", lap.transpose()),
                     ("powerlaw_fwd", pl), ("powerlaw_bwd", pl.transpose())):
+        if only and name not in only:
+            continue
         x_true = np.ones(m.n)
         b = m.matvec(x_true)
         cases.append(dict(name=name, m=m, b=b))
@@ -226,7 +234,7 @@ def run_gpu(args, world, rank, local):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
         pg = dist
-    cases = make_cases(args.scale)
+    cases = make_cases(args.scale, args.cases)
     solvers = []
     tuned = {}
     for c in cases:
@@ -574,7 +582,16 @@ def main(argv=None) -> int:
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--scale", type=float, default=1.0,
                     help="size factor of the deep/wide systems (1.0 = the benchmark sizes; smaller for profiling)")
+    ap.add_argument("--cases", default=None,
+                    help="comma-separated subset of " + ",".join(CASE_NAMES) + " (profiling runs)")
+    ap.add_argument("--opt", action="append", default=[], metavar="KEY=VALUE",
+                    help="SyncFreeSolver option (e.g. warp_sync=1, split=32, staged=0); disables the autotuner")
     args = ap.parse_args(argv)
+    if args.cases:
+        args.cases = [c.strip() for c in args.cases.split(",") if c.strip()]
+        bad = [c for c in args.cases if c not in CASE_NAMES]
+        if bad:
+            ap.error(f"unknown case(s) {bad}")
     if args.warmup < 3:
         args.warmup = 3
     kw = {}
@@ -582,6 +599,11 @@ def main(argv=None) -> int:
         v = getattr(args, k)
         if v is not None:
             kw[k] = v
+    for o in args.opt:
+        k, _, v = o.partition("=")
+        if not k or not v:
+            ap.error(f"--opt wants KEY=VALUE, got {o!r}")
+        kw[k.strip()] = int(v)
     args.solver_kw = kw
     world, rank, local = dist_env()
     if args.impl == "reference":

@@ -75,6 +75,7 @@ struct sptrsv_gb300_handle_s {
   int layout_block = -1;
   std::vector<int> dep_cnt_host;   // dependencies per position
   std::vector<int> out_cnt_host;   // dependents per position
+  int max_dep_cnt = 0, max_out_cnt = 0;
   ChunkTable tab_fwd, tab_adj;
   PieceTable pc_fwd, pc_adj;
   // staged values
@@ -148,7 +149,7 @@ void free_pieces(PieceTable& t) {
   if (t.row) cudaFree(t.row);
   if (t.lo) cudaFree(t.lo);
   if (t.hi) cudaFree(t.hi);
-  if (t.cbase) cudaFree(t.cbase);
+  if (t.cseg) cudaFree(t.cseg);
   t = PieceTable();
 }
 
@@ -368,11 +369,19 @@ int build_layout(sptrsv_gb300_handle_s* h, int block, cudaStream_t s) {
     CUDA_TRY(cudaMemcpyAsync(ptr.data(), L.dep_ptr, sizeof(int) * ((size_t)n + 1), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
     h->dep_cnt_host.resize(n);
-    for (int p = 0; p < n; ++p) h->dep_cnt_host[p] = ptr[p + 1] - ptr[p];
+    h->max_dep_cnt = 0;
+    for (int p = 0; p < n; ++p) {
+      h->dep_cnt_host[p] = ptr[p + 1] - ptr[p];
+      h->max_dep_cnt = std::max(h->max_dep_cnt, h->dep_cnt_host[p]);
+    }
     CUDA_TRY(cudaMemcpyAsync(ptr.data(), L.out_ptr, sizeof(int) * ((size_t)n + 1), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
     h->out_cnt_host.resize(n);
-    for (int p = 0; p < n; ++p) h->out_cnt_host[p] = ptr[p + 1] - ptr[p];
+    h->max_out_cnt = 0;
+    for (int p = 0; p < n; ++p) {
+      h->out_cnt_host[p] = ptr[p + 1] - ptr[p];
+      h->max_out_cnt = std::max(h->max_out_cnt, h->out_cnt_host[p]);
+    }
   }
   if (level_order) {
     L.nlevels = h->nlevels;
@@ -453,10 +462,15 @@ int build_pieces(sptrsv_gb300_handle_s* h, PieceTable& t, const std::vector<int>
       hi.push_back(0);
     }
   };
+  std::vector<int> cseg;
   for (int i = 0; i < n; ++i) {
     const int p = reversed ? n - 1 - i : i;
     const long long c = counts[p], e0 = start[p];
     const int k = (split > 0 && c > split) ? static_cast<int>(std::min<long long>(32, (c + split - 1) / split)) : 1;
+    if (i % chunk == 0) {  // a chunk starts on a fresh segment
+      pad();
+      cseg.push_back(static_cast<int>(walk.size() / 32));
+    }
     if (walk.size() % 32 + k > 32) pad();
     for (int j = 0; j < k; ++j) {
       walk.push_back(i);
@@ -466,17 +480,16 @@ int build_pieces(sptrsv_gb300_handle_s* h, PieceTable& t, const std::vector<int>
   }
   pad();
   t.split = split;
-  t.segs_per_chunk = std::max(1, chunk / 32);
+  t.chunk = chunk;
   t.nseg = static_cast<int>(walk.size() / 32);
-  t.nchunks = (t.nseg + t.segs_per_chunk - 1) / t.segs_per_chunk;
-  std::vector<int> cbase(t.nchunks > 0 ? t.nchunks : 1, 0);
-  for (int c = 0; c < t.nchunks; ++c) cbase[c] = walk[(size_t)c * t.segs_per_chunk * 32];
+  t.nchunks = static_cast<int>(cseg.size());
+  cseg.push_back(t.nseg);
   const size_t np = walk.size() > 0 ? walk.size() : 1;
   CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.walk), sizeof(int) * np));
   CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.row), sizeof(int) * np));
   CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.lo), sizeof(int) * np));
   CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.hi), sizeof(int) * np));
-  CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.cbase), sizeof(int) * cbase.size()));
+  CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.cseg), sizeof(int) * cseg.size()));
   if (!walk.empty()) {
     CUDA_TRY(cudaMemcpy(t.walk, walk.data(), sizeof(int) * walk.size(), cudaMemcpyHostToDevice));
     // row of each piece's unknown: perm gathered on the device (padding reads position 0)
@@ -493,14 +506,14 @@ int build_pieces(sptrsv_gb300_handle_s* h, PieceTable& t, const std::vector<int>
     CUDA_TRY(cudaMemcpy(t.lo, lo.data(), sizeof(int) * walk.size(), cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(t.hi, hi.data(), sizeof(int) * walk.size(), cudaMemcpyHostToDevice));
   }
-  CUDA_TRY(cudaMemcpy(t.cbase, cbase.data(), sizeof(int) * cbase.size(), cudaMemcpyHostToDevice));
-  h->device_bytes += sizeof(int) * (4 * np + cbase.size());
+  CUDA_TRY(cudaMemcpy(t.cseg, cseg.data(), sizeof(int) * cseg.size(), cudaMemcpyHostToDevice));
+  h->device_bytes += sizeof(int) * (4 * np + cseg.size());
   return SPTRSV_OK;
 }
 
 int ensure_pieces(sptrsv_gb300_handle_s* h, bool adj, int split, int chunk, cudaStream_t s) {
   PieceTable& t = adj ? h->pc_adj : h->pc_fwd;
-  if (t.walk && t.split == split && t.segs_per_chunk == std::max(1, chunk / 32)) return SPTRSV_OK;
+  if (t.walk && t.split == split && t.chunk == chunk) return SPTRSV_OK;
   return build_pieces(h, t, adj ? h->out_cnt_host : h->dep_cnt_host, adj, split, chunk, s);
 }
 
@@ -639,7 +652,8 @@ int solve_typed(sptrsv_gb300_handle_s* h, const Values<T>& V, int rhs, int layou
                                    c, timeout_ns(h), h->num_sms, s, adj));
   } else {
     const PieceTable* pc = nullptr;
-    if (rhs == 1 && c.wsync && !c.exact && c.split > 0 && !(adj && adj->grad)) {
+    const int longest = adj ? h->max_out_cnt : h->max_dep_cnt;
+    if (rhs == 1 && c.wsync && !c.exact && c.split > 0 && longest > c.split && !(adj && adj->grad)) {
       ST_TRY(ensure_pieces(h, adj != nullptr, c.split, c.chunk, s));
       pc = adj ? &h->pc_adj : &h->pc_fwd;
     }

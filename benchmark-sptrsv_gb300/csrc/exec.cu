@@ -62,13 +62,13 @@ struct ExecArgs {
   int nlevels;
   // split-list work units (k_pull_wsync_split): piece i covers entries
   // [pc_lo[i], pc_hi[i]) of walk index pc_walk[i] (-1: padding); 32 pieces per
-  // warp segment, pc_spc segments per chunk, chunk c starting at walk pc_cbase[c]
+  // warp segment; chunk c = walk indices [c*chunk, (c+1)*chunk) = segments
+  // [pc_cseg[c], pc_cseg[c+1])
   const int* pc_walk;
   const int* pc_row;    // row of the piece's unknown (perm of its position)
   const int* pc_lo;
   const int* pc_hi;
-  const int* pc_cbase;
-  int pc_spc, pc_nseg;
+  const int* pc_cseg;
 };
 
 template <typename T>
@@ -366,11 +366,12 @@ __global__ void __launch_bounds__(256) k_pull_wsync_split(ExecArgs<T> a) {
   for (;;) {
     const unsigned c = next_chunk(a.ctl, a.nchunks, &s_chunk);
     if (c >= (unsigned)a.nchunks) break;
-    const int seg0 = static_cast<int>(c) * a.pc_spc;
-    const int seg1 = min(seg0 + a.pc_spc, a.pc_nseg);
-    const int cbase = a.pc_cbase[c];
+    const int seg0 = a.pc_cseg[c];
+    const int seg1 = a.pc_cseg[c + 1];
+    const int cbase = static_cast<int>(c) * a.chunk;
     if (a.smem_tier)
-      for (int i = threadIdx.x; i < (seg1 - seg0) * 32; i += blockDim.x) *reinterpret_cast<Bits*>(&s_x[i]) = F::EMPTY;
+      for (int i = threadIdx.x; i < min(a.chunk, a.n - cbase); i += blockDim.x)
+        *reinterpret_cast<Bits*>(&s_x[i]) = F::EMPTY;
     __syncthreads();
     bool fail = false;
     // piece data of this warp's next segment is loaded one segment ahead
@@ -1129,10 +1130,7 @@ cudaError_t launch_pull(const Layout& L, const Values<T>& V, int rhs, const VecV
     a.pc_row = pc->row;
     a.pc_lo = pc->lo;
     a.pc_hi = pc->hi;
-    a.pc_cbase = pc->cbase;
-    a.pc_spc = pc->segs_per_chunk;
-    a.pc_nseg = pc->nseg;
-    a.nchunks = pc->nchunks;
+    a.pc_cseg = pc->cseg;
   }
   a.xw = xw;
   a.ctl = ctl;
@@ -1143,7 +1141,7 @@ cudaError_t launch_pull(const Layout& L, const Values<T>& V, int rhs, const VecV
   size_t smem = 0;
   a.smem_tier = 0;
   if (cfg.smem_tier) {
-    smem = use_pc ? (size_t)pc->segs_per_chunk * 32 * sizeof(T) : pull_smem_bytes(cfg.chunk, rhs, sizeof(T));
+    smem = pull_smem_bytes(cfg.chunk, rhs, sizeof(T));
     if (smem <= 200 * 1024) a.smem_tier = 1;
     else smem = 0;
   }

@@ -52,15 +52,16 @@ struct ChunkTable {
 
 // Work units of the split-list warp-synchronous executor: a walk's dependency
 // lists cut into pieces of at most `split` entries (at most 32 per unknown),
-// 32 pieces per warp segment with no unknown straddling two segments (padding
-// pieces have walk -1), segs_per_chunk segments per chunk.
+// 32 pieces per warp segment with no unknown straddling two segments and no
+// segment straddling two chunks of `chunk` walk indices (padding pieces have
+// walk -1).
 struct PieceTable {
-  int split = 0, segs_per_chunk = 0, nseg = 0, nchunks = 0;
+  int split = 0, chunk = 0, nseg = 0, nchunks = 0;
   int* walk = nullptr;    // device [nseg*32]
   int* row = nullptr;     // device [nseg*32] row of the unknown (perm of its position; 0 for padding)
   int* lo = nullptr;      // device [nseg*32] first entry
   int* hi = nullptr;      // device [nseg*32] end entry
-  int* cbase = nullptr;   // device [nchunks] first walk index of each chunk
+  int* cseg = nullptr;    // device [nchunks+1] first segment of each chunk
 };
 
 // Solve-time description of one right-hand-side block. Element (i, k) of b
