@@ -150,6 +150,7 @@ void free_pieces(PieceTable& t) {
   if (t.lo) cudaFree(t.lo);
   if (t.hi) cudaFree(t.hi);
   if (t.cseg) cudaFree(t.cseg);
+  if (t.cbase) cudaFree(t.cbase);
   t = PieceTable();
 }
 
@@ -462,16 +463,22 @@ int build_pieces(sptrsv_gb300_handle_s* h, PieceTable& t, const std::vector<int>
       hi.push_back(0);
     }
   };
-  std::vector<int> cseg;
+  std::vector<int> cseg, cbase;
+  const size_t seg_cap = static_cast<size_t>(std::max(1, (chunk + 31) / 32));
   for (int i = 0; i < n; ++i) {
     const int p = reversed ? n - 1 - i : i;
     const long long c = counts[p], e0 = start[p];
     const int k = (split > 0 && c > split) ? static_cast<int>(std::min<long long>(32, (c + split - 1) / split)) : 1;
-    if (i % chunk == 0) {  // a chunk starts on a fresh segment
-      pad();
+    const bool seg_full = walk.size() % 32 + k > 32;
+    const size_t first = seg_full ? (walk.size() + 31) / 32 * 32 : walk.size();
+    const size_t segs_after = (first + k - 1) / 32 + 1;  // segments in use once i is placed
+    if (i % chunk == 0 || (!cseg.empty() && segs_after - cseg.back() > seg_cap)) {
+      pad();  // a chunk starts on a fresh segment
       cseg.push_back(static_cast<int>(walk.size() / 32));
+      cbase.push_back(i);
+    } else if (seg_full) {
+      pad();
     }
-    if (walk.size() % 32 + k > 32) pad();
     for (int j = 0; j < k; ++j) {
       walk.push_back(i);
       lo.push_back(static_cast<int>(e0 + c * j / k));
@@ -490,6 +497,9 @@ int build_pieces(sptrsv_gb300_handle_s* h, PieceTable& t, const std::vector<int>
   CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.lo), sizeof(int) * np));
   CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.hi), sizeof(int) * np));
   CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.cseg), sizeof(int) * cseg.size()));
+  CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.cbase), sizeof(int) * (cbase.empty() ? 1 : cbase.size())));
+  if (!cbase.empty())
+    CUDA_TRY(cudaMemcpy(t.cbase, cbase.data(), sizeof(int) * cbase.size(), cudaMemcpyHostToDevice));
   if (!walk.empty()) {
     CUDA_TRY(cudaMemcpy(t.walk, walk.data(), sizeof(int) * walk.size(), cudaMemcpyHostToDevice));
     // row of each piece's unknown: perm gathered on the device (padding reads position 0)
@@ -507,7 +517,7 @@ int build_pieces(sptrsv_gb300_handle_s* h, PieceTable& t, const std::vector<int>
     CUDA_TRY(cudaMemcpy(t.hi, hi.data(), sizeof(int) * walk.size(), cudaMemcpyHostToDevice));
   }
   CUDA_TRY(cudaMemcpy(t.cseg, cseg.data(), sizeof(int) * cseg.size(), cudaMemcpyHostToDevice));
-  h->device_bytes += sizeof(int) * (4 * np + cseg.size());
+  h->device_bytes += sizeof(int) * (4 * np + cseg.size() + cbase.size());
   return SPTRSV_OK;
 }
 

@@ -62,13 +62,14 @@ struct ExecArgs {
   int nlevels;
   // split-list work units (k_pull_wsync_split): piece i covers entries
   // [pc_lo[i], pc_hi[i]) of walk index pc_walk[i] (-1: padding); 32 pieces per
-  // warp segment; chunk c = walk indices [c*chunk, (c+1)*chunk) = segments
-  // [pc_cseg[c], pc_cseg[c+1])
+  // warp segment; chunk c = segments [pc_cseg[c], pc_cseg[c+1]), starting at
+  // walk index pc_cbase[c] and spanning at most `chunk` walk indices
   const int* pc_walk;
   const int* pc_row;    // row of the piece's unknown (perm of its position)
   const int* pc_lo;
   const int* pc_hi;
   const int* pc_cseg;
+  const int* pc_cbase;
 };
 
 template <typename T>
@@ -368,7 +369,7 @@ __global__ void __launch_bounds__(256) k_pull_wsync_split(ExecArgs<T> a) {
     if (c >= (unsigned)a.nchunks) break;
     const int seg0 = a.pc_cseg[c];
     const int seg1 = a.pc_cseg[c + 1];
-    const int cbase = static_cast<int>(c) * a.chunk;
+    const int cbase = a.pc_cbase[c];
     if (a.smem_tier)
       for (int i = threadIdx.x; i < min(a.chunk, a.n - cbase); i += blockDim.x)
         *reinterpret_cast<Bits*>(&s_x[i]) = F::EMPTY;
@@ -1131,6 +1132,8 @@ cudaError_t launch_pull(const Layout& L, const Values<T>& V, int rhs, const VecV
     a.pc_lo = pc->lo;
     a.pc_hi = pc->hi;
     a.pc_cseg = pc->cseg;
+    a.pc_cbase = pc->cbase;
+    a.nchunks = pc->nchunks;
   }
   a.xw = xw;
   a.ctl = ctl;

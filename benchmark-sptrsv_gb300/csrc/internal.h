@@ -52,9 +52,10 @@ struct ChunkTable {
 
 // Work units of the split-list warp-synchronous executor: a walk's dependency
 // lists cut into pieces of at most `split` entries (at most 32 per unknown),
-// 32 pieces per warp segment with no unknown straddling two segments and no
-// segment straddling two chunks of `chunk` walk indices (padding pieces have
-// walk -1).
+// 32 pieces per warp segment with no unknown straddling two segments (padding
+// pieces have walk -1). A chunk holds at most ceil(chunk/32) segments (one
+// per warp when chunk = threads per CTA) and never crosses a multiple of
+// `chunk` walk indices (so chunks stay inside order blocks of that size).
 struct PieceTable {
   int split = 0, chunk = 0, nseg = 0, nchunks = 0;
   int* walk = nullptr;    // device [nseg*32]
@@ -62,6 +63,7 @@ struct PieceTable {
   int* lo = nullptr;      // device [nseg*32] first entry
   int* hi = nullptr;      // device [nseg*32] end entry
   int* cseg = nullptr;    // device [nchunks+1] first segment of each chunk
+  int* cbase = nullptr;   // device [nchunks] first walk index of each chunk
 };
 
 // Solve-time description of one right-hand-side block. Element (i, k) of b
