@@ -222,6 +222,53 @@ def cpu_baseline_sample(cases):
 
 
 # ------------------------------------------------------------------ GPU arm
+# DRAM bytes per stored entry of the split-list executor on the power-law
+# backward system: ncu capture of the 1/4-size case (156.1 MB for 9,474,199
+# stored entries; traffic grows with the stored entries), scaled to a launch.
+TRAFFIC_PER_ENTRY = {"powerlaw_bwd": 156.148480e6 / 9474199}
+TRAFFIC_SOURCE = ("ncu --set full capture of k_pull_wsync_split on powerlaw_bwd at 1/4 size, scaled by stored "
+                  "entries (profiles/k_pull_wsync_split_powerlaw_bwd.md)")
+
+
+def traffic_bytes(case):
+    per = TRAFFIC_PER_ENTRY.get(case["name"])
+    return int(round(per * case["m"].nnz)) if per else None
+
+
+def reference_scheme_ms(cases, dev, reps: int = 3) -> dict:
+    """Median device time of the reference's executor scheme (kernel-level surface) per case."""
+    import torch
+
+    from sptrsv_gb300 import OPT_WARP_AUTO, analyser, executor
+    out = {}
+    for c in cases:
+        m = c["m"]
+        cp = torch.from_numpy(m.col_ptr).to(dev)
+        ri = torch.from_numpy(m.row_idx).to(dev)
+        va = torch.from_numpy(m.val).to(dev)
+        deg0 = torch.zeros(m.n, dtype=torch.int32, device=dev)
+        analyser(ri, m.n, m.nnz, deg0)
+        deg = torch.empty_like(deg0)
+        left = torch.zeros(m.n, dtype=torch.float64, device=dev)
+        b = c["b_dev"]
+        x = torch.empty_like(b)
+        ts = []
+        for _ in range(reps + 1):
+            deg.copy_(deg0)
+            left.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            executor(cp, ri, va, deg, left, m.n, m.substitution, 1, OPT_WARP_AUTO, b, x)
+            e1.record()
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        if float((x - 1.0).abs().max()) > 1e-9:
+            raise RuntimeError(f"reference scheme gave a wrong solution on {c['name']}")
+        out[c["name"]] = statistics.median(ts[1:])
+    return out
+
+
 def run_gpu(args, world, rank, local):
     import torch
 
@@ -332,6 +379,12 @@ def run_gpu(args, world, rank, local):
         e2e_step = float(t.item())
     e2e_val = world * total_bytes / (e2e_step * 1e-3) / 1e9
 
+    # the reference's own GPU scheme on the same systems (outside the timed region):
+    # warp per column, in-degree countdown counters and atomic partial sums
+    # (SpTRSV_cuda/sptrsv_syncfree_cuda.h:8-107), restated with ticket order and
+    # bounded waits, through the kernel-level C-ABI surface
+    ref_scheme = reference_scheme_ms(cases, dev) if not args.no_ref_scheme else {}
+
     # roofline of the dominant kernel (the executor on the case with the largest share)
     peak, peak_kind = read_peaks()
     dom = max(cases, key=lambda c: statistics.mean(exec_ms[c["name"]]))
@@ -350,6 +403,9 @@ def run_gpu(args, world, rank, local):
             "us_per_level": round(1e3 * ems / max(info[c["name"]]["nlevels"], 1), 3),
             "max_abs_err": errs[c["name"]], "analysis_ms": round(info[c["name"]]["analysis_ms"], 2),
         }
+        if c["name"] in ref_scheme:
+            details[c["name"]]["reference_scheme_ms"] = round(ref_scheme[c["name"]], 4)
+            details[c["name"]]["speedup_vs_reference_scheme"] = round(ref_scheme[c["name"]] / ms, 2)
     if rank != 0:
         return 0
     cpu = cpu_baseline_sample(cases) if (world == 1 and not args.no_cpu_baseline) else None
@@ -363,8 +419,10 @@ def run_gpu(args, world, rank, local):
                    "solver": args.solver_kw or ("defaults" if args.no_tune else "autotuned per system"),
                    "tuned": tuned},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 3), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 5), "traffic": None, "kernel": f"executor on {dom['name']}",
-                     "peak_source": peak_kind},
+                     "frac": round(achieved / peak, 5), "traffic": traffic_bytes(dom),
+                     "traffic_unit": "bytes per launch (DRAM read + write)",
+                     "traffic_source": TRAFFIC_SOURCE if traffic_bytes(dom) else None,
+                     "kernel": f"executor on {dom['name']}", "peak_source": peak_kind},
         "cpu_baseline": cpu,
         "e2e": {"value": round(e2e_val, 3), "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": round(e2e_step, 4)},
@@ -372,6 +430,11 @@ def run_gpu(args, world, rank, local):
         "clocks": clock_info,
         "wall_s_timed": round(t_wall, 3),
         "cases": details,
+        "reference_scheme_gpu": ({"ms_per_step": round(sum(ref_scheme.values()), 4),
+                                  "gbs": round(total_bytes / (sum(ref_scheme.values()) * 1e-3) / 1e9, 3),
+                                  "what": "the reference's warp-per-column push executor scheme (in-degree counters + "
+                                          "atomic partial sums), restated with ticket order and bounded waits, "
+                                          "same systems, L2 not flushed"} if ref_scheme else None),
     }
     print(json.dumps(line), flush=True)
     if pg:
@@ -576,6 +639,8 @@ def main(argv=None) -> int:
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--no-ref-scheme", action="store_true",
+                    help="skip timing the reference's GPU scheme (kernel-level executor) beside the library")
     ap.add_argument("--schedule", type=int, default=None)
     ap.add_argument("--lanes", type=int, default=None)
     ap.add_argument("--chunk", type=int, default=None)
