@@ -151,6 +151,7 @@ void free_pieces(PieceTable& t) {
   if (t.hi) cudaFree(t.hi);
   if (t.cseg) cudaFree(t.cseg);
   if (t.cbase) cudaFree(t.cbase);
+  if (t.seg_split) cudaFree(t.seg_split);
   t = PieceTable();
 }
 
@@ -464,6 +465,7 @@ int build_pieces(sptrsv_gb300_handle_s* h, PieceTable& t, const std::vector<int>
     }
   };
   std::vector<int> cseg, cbase;
+  std::vector<unsigned char> seg_split_host;
   const size_t seg_cap = static_cast<size_t>(std::max(1, (chunk + 31) / 32));
   for (int i = 0; i < n; ++i) {
     const int p = reversed ? n - 1 - i : i;
@@ -478,6 +480,11 @@ int build_pieces(sptrsv_gb300_handle_s* h, PieceTable& t, const std::vector<int>
       cbase.push_back(i);
     } else if (seg_full) {
       pad();
+    }
+    if (k > 1) {  // this unknown spans lanes of the segment it starts (after any padding above)
+      const size_t sg = walk.size() / 32;
+      if (seg_split_host.size() <= sg) seg_split_host.resize(sg + 1, 0);
+      seg_split_host[sg] = 1;
     }
     for (int j = 0; j < k; ++j) {
       walk.push_back(i);
@@ -498,6 +505,9 @@ int build_pieces(sptrsv_gb300_handle_s* h, PieceTable& t, const std::vector<int>
   CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.hi), sizeof(int) * np));
   CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.cseg), sizeof(int) * cseg.size()));
   CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.cbase), sizeof(int) * (cbase.empty() ? 1 : cbase.size())));
+  seg_split_host.resize(t.nseg > 0 ? t.nseg : 1, 0);
+  CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.seg_split), seg_split_host.size()));
+  CUDA_TRY(cudaMemcpy(t.seg_split, seg_split_host.data(), seg_split_host.size(), cudaMemcpyHostToDevice));
   if (!cbase.empty())
     CUDA_TRY(cudaMemcpy(t.cbase, cbase.data(), sizeof(int) * cbase.size(), cudaMemcpyHostToDevice));
   if (!walk.empty()) {

@@ -70,6 +70,7 @@ struct ExecArgs {
   const int* pc_hi;
   const int* pc_cseg;
   const int* pc_cbase;
+  const unsigned char* pc_split;  // per segment: 1 if an unknown spans several lanes
 };
 
 template <typename T>
@@ -396,18 +397,23 @@ __global__ void __launch_bounds__(256) k_pull_wsync_split(ExecArgs<T> a) {
         n_hi = a.pc_hi[pn];
         n_row = a.pc_row[pn];
       }
-      const int prev = __shfl_up_sync(kFull, walk, 1);
       const bool valid = walk >= 0;
-      const bool head = valid && (lane == 0 || prev != walk);
-      const unsigned heads = __ballot_sync(kFull, head);
-      const unsigned valids = __ballot_sync(kFull, valid);
-      const bool split = heads != valids;  // some unknown spans several lanes
-      // this lane's group: from its head (at or below) to the lane before the next head
-      const unsigned above = heads & ~at_or_below;
-      const int ge = above ? __ffs(above) - 2 : 31 - __clz(valids);
-      const int gs = valid ? 31 - __clz(heads & at_or_below) : lane;
-      // head lanes: the lanes of their unknown (ge >= lane >= 0 there)
-      const unsigned gmask = head ? (ge >= 31 ? kFull : ((2u << ge) - 1u)) & ~((1u << lane) - 1u) : 0u;
+      const bool split = a.pc_split[seg] != 0;  // some unknown of the segment spans several lanes
+      bool head = valid;
+      int ge = lane, gs = lane;
+      unsigned gmask = 0u;
+      if (split) {
+        const int prev = __shfl_up_sync(kFull, walk, 1);
+        head = valid && (lane == 0 || prev != walk);
+        const unsigned heads = __ballot_sync(kFull, head);
+        const unsigned valids = __ballot_sync(kFull, valid);
+        // this lane's group: from its head (at or below) to the lane before the next head
+        const unsigned above = heads & ~at_or_below;
+        ge = above ? __ffs(above) - 2 : 31 - __clz(valids);
+        gs = valid ? 31 - __clz(heads & at_or_below) : lane;
+        // head lanes: the lanes of their unknown (ge >= lane >= 0 there)
+        gmask = head ? (ge >= 31 ? kFull : ((2u << ge) - 1u)) & ~((1u << lane) - 1u) : 0u;
+      }
       const int p = ADJ ? last - walk : walk;
       T acc = T(0);
       if (head) acc = a.b[(long long)row * a.b_si] * a.rcp[p];
@@ -459,8 +465,17 @@ __global__ void __launch_bounds__(256) k_pull_wsync_split(ExecArgs<T> a) {
           }
           if (!todo) {
             e += U;
-            if (e < e1) load_batch();
-            else sdone = true;
+            if (e < e1) {
+              load_batch();
+            } else {
+              sdone = true;
+              if (!split) {  // one lane per unknown: publish at once
+                if (a.smem_tier) F::store_shared(&s_x[walk - cbase], acc);
+                F::store(&a.xw[p], acc);
+                a.x[(long long)row * a.x_si] = acc;
+                done = true;
+              }
+            }
             progress = true;
           } else {
 #pragma unroll
@@ -490,7 +505,7 @@ __global__ void __launch_bounds__(256) k_pull_wsync_split(ExecArgs<T> a) {
             const unsigned pub = __ballot_sync(kFull, head && done);
             if (valid && !head) done = (pub >> gs) & 1u;
           }
-        } else if (sdone && !done) {  // one lane per unknown
+        } else if (sdone && !done) {  // a list with no entries
           if (a.smem_tier) F::store_shared(&s_x[walk - cbase], acc);
           F::store(&a.xw[p], acc);
           a.x[(long long)row * a.x_si] = acc;
@@ -1133,6 +1148,7 @@ cudaError_t launch_pull(const Layout& L, const Values<T>& V, int rhs, const VecV
     a.pc_hi = pc->hi;
     a.pc_cseg = pc->cseg;
     a.pc_cbase = pc->cbase;
+    a.pc_split = pc->seg_split;
     a.nchunks = pc->nchunks;
   }
   a.xw = xw;

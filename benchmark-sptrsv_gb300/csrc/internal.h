@@ -64,6 +64,7 @@ struct PieceTable {
   int* hi = nullptr;      // device [nseg*32] end entry
   int* cseg = nullptr;    // device [nchunks+1] first segment of each chunk
   int* cbase = nullptr;   // device [nchunks] first walk index of each chunk
+  unsigned char* seg_split = nullptr;  // device [nseg] 1 if an unknown of the segment spans several lanes
 };
 
 // Solve-time description of one right-hand-side block. Element (i, k) of b
