@@ -480,6 +480,32 @@ cudaError_t launch_sort_lists(const int* ptr, const int* pos, const int* src, in
   return cudaGetLastError();
 }
 
+// ------------------------------------------------------------ schedule heuristics
+// Off-diagonal entries whose row and column fall in the same block of `block`
+// unknowns of the natural execution order (ascending for a forward solve,
+// descending for a backward one): how much of the DAG a blocked order keeps
+// inside one CTA.
+__global__ void k_block_locality(const int* __restrict__ row, const int* __restrict__ col, int nnz, int n,
+                                 int block, int backward, unsigned long long* count) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  unsigned local = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nnz; i += stride) {
+    const int r = row[i], c = col[i];
+    if (r == c) continue;
+    const int pr = backward ? n - 1 - r : r, pc = backward ? n - 1 - c : c;
+    local += (pr / block == pc / block) ? 1u : 0u;
+  }
+  for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+  if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, (unsigned long long)local);
+}
+
+cudaError_t launch_block_locality(const int* row, const int* col, int nnz, int n, int block, bool backward,
+                                  unsigned long long* count, cudaStream_t s) {
+  if (nnz <= 0) return cudaSuccess;
+  k_block_locality<<<grid_for(nnz), kThreads, 0, s>>>(row, col, nnz, n, block, backward ? 1 : 0, count);
+  return cudaGetLastError();
+}
+
 // ------------------------------------------------------------ level sets
 // Breadth-first peeling of the in-degree, one grid barrier per level
 // (the level definition of SpTRSV_cuda/findlevel.h:6-69): level 0 holds rows

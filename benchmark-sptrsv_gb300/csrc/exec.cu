@@ -469,12 +469,6 @@ __global__ void __launch_bounds__(256) k_pull_wsync_split(ExecArgs<T> a) {
               load_batch();
             } else {
               sdone = true;
-              if (!split) {  // one lane per unknown: publish at once
-                if (a.smem_tier) F::store_shared(&s_x[walk - cbase], acc);
-                F::store(&a.xw[p], acc);
-                a.x[(long long)row * a.x_si] = acc;
-                done = true;
-              }
             }
             progress = true;
           } else {
@@ -505,7 +499,8 @@ __global__ void __launch_bounds__(256) k_pull_wsync_split(ExecArgs<T> a) {
             const unsigned pub = __ballot_sync(kFull, head && done);
             if (valid && !head) done = (pub >> gs) & 1u;
           }
-        } else if (sdone && !done) {  // a list with no entries
+        } else if (sdone && !done) {  // one lane per unknown
+          // (publishing here rather than next to the last batch measured faster)
           if (a.smem_tier) F::store_shared(&s_x[walk - cbase], acc);
           F::store(&a.xw[p], acc);
           a.x[(long long)row * a.x_si] = acc;

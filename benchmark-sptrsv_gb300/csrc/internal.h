@@ -169,6 +169,10 @@ cudaError_t launch_fill_pull(const int* perm, const int* iperm, const int* csr_p
 cudaError_t launch_fill_push(const int* perm, const int* iperm, const int* col_ptr, const int* row_idx,
                              const int* out_ptr, int n, const SysDesc& sd, int* out_pos, int* out_src,
                              cudaStream_t s);
+// count += off-diagonal entries whose row and column share a block of `block`
+// unknowns in the natural execution order.
+cudaError_t launch_block_locality(const int* row, const int* col, int nnz, int n, int block, bool backward,
+                                  unsigned long long* count, cudaStream_t s);
 // Sorts every list [ptr[p], ptr[p+1]) of (pos, src) by pos (descending when asked).
 cudaError_t launch_sort_lists(const int* ptr, const int* pos, const int* src, int n, int count, bool descending,
                               int* pos_out, int* src_out, cudaStream_t s);

@@ -88,6 +88,11 @@ class Info(ctypes.Structure):
         ("order_block", ctypes.c_int),
         ("analysis_ms", ctypes.c_double),
         ("device_bytes", ctypes.c_size_t),
+        ("block", ctypes.c_int),
+        ("warp_sync", ctypes.c_int),
+        ("staged", ctypes.c_int),
+        ("split", ctypes.c_int),
+        ("locality_permille", ctypes.c_int),
     ]
 
 

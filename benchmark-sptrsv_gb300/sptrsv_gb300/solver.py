@@ -93,11 +93,13 @@ class SyncFreeSolver:
 
     def __init__(self, col_ptr=None, row_idx=None, n: int | None = None, substitution: int = 0, *, values=None,
                  batch=None,
-                 schedule: int = SCHED_AUTO, lanes: int = 0, chunk: int = 0, order_block: int | None = None,
-                 exact: bool = False, smem_tier: bool = True, timeout_ms: int = 1000, sync_check: bool = True,
-                 profile: bool = False, block: int = 0, backoff_ns: int | None = None, ctas_per_sm: int = 0,
-                 staged: bool = True, stage_entries: int = 0, stages: int = 2, warp_sync: bool = False,
-                 split: int | None = None, fused_grad: bool = False, stream=None):
+                 schedule: int | None = None, lanes: int | None = None, chunk: int | None = None,
+                 order_block: int | None = None, exact: bool | None = None, smem_tier: bool | None = None,
+                 timeout_ms: int | None = None, sync_check: bool | None = None, profile: bool | None = None,
+                 block: int | None = None, backoff_ns: int | None = None, ctas_per_sm: int | None = None,
+                 staged: bool | None = None, stage_entries: int | None = None, stages: int | None = None,
+                 warp_sync: bool | None = None, split: int | None = None, fused_grad: bool | None = None,
+                 stream=None):
         torch = _torch()
         self._lib = load()
         self.device = torch.device("cuda", torch.cuda.current_device())
@@ -129,27 +131,19 @@ class SyncFreeSolver:
         h = ctypes.c_void_p()
         check(self._lib.sptrsv_gb300_create(ctypes.byref(h)), "create")
         self._h = h
-        self.set_option(_lib.OPTION_SCHEDULE, schedule)
-        self.set_option(_lib.OPTION_LANES, lanes)
-        self.set_option(_lib.OPTION_CHUNK, chunk)
-        if order_block is not None:
-            self.set_option(_lib.OPTION_ORDER_BLOCK, order_block)
-        self.set_option(_lib.OPTION_EXACT, int(exact))
-        self.set_option(_lib.OPTION_SMEM_TIER, int(smem_tier))
-        self.set_option(_lib.OPTION_TIMEOUT_MS, timeout_ms)
-        self.set_option(_lib.OPTION_SYNC_CHECK, int(sync_check))
-        self.set_option(_lib.OPTION_PROFILE, int(profile))
-        self.set_option(_lib.OPTION_BLOCK, int(block))
-        if backoff_ns is not None:
-            self.set_option(_lib.OPTION_BACKOFF_NS, int(backoff_ns))
-        self.set_option(_lib.OPTION_CTAS_PER_SM, int(ctas_per_sm))
-        self.set_option(_lib.OPTION_STAGED, int(staged))
-        self.set_option(_lib.OPTION_STAGE_ENTRIES, int(stage_entries))
-        self.set_option(_lib.OPTION_STAGES, int(stages))
-        self.set_option(_lib.OPTION_WARP_SYNC, int(warp_sync))
-        if split is not None:
-            self.set_option(_lib.OPTION_SPLIT, int(split))
-        self.set_option(_lib.OPTION_FUSED_GRAD, int(fused_grad))
+        # only the options given here are set; the rest keep the library's
+        # defaults (with the automatic schedule, the plan chosen at analysis)
+        for opt, v in ((_lib.OPTION_SCHEDULE, schedule), (_lib.OPTION_LANES, lanes), (_lib.OPTION_CHUNK, chunk),
+                       (_lib.OPTION_ORDER_BLOCK, order_block), (_lib.OPTION_EXACT, exact),
+                       (_lib.OPTION_SMEM_TIER, smem_tier), (_lib.OPTION_TIMEOUT_MS, timeout_ms),
+                       (_lib.OPTION_SYNC_CHECK, sync_check), (_lib.OPTION_PROFILE, profile),
+                       (_lib.OPTION_BLOCK, block), (_lib.OPTION_BACKOFF_NS, backoff_ns),
+                       (_lib.OPTION_CTAS_PER_SM, ctas_per_sm), (_lib.OPTION_STAGED, staged),
+                       (_lib.OPTION_STAGE_ENTRIES, stage_entries), (_lib.OPTION_STAGES, stages),
+                       (_lib.OPTION_WARP_SYNC, warp_sync), (_lib.OPTION_SPLIT, split),
+                       (_lib.OPTION_FUSED_GRAD, fused_grad)):
+            if v is not None:
+                self.set_option(opt, int(v))
         self._stream = stream
         self.analyse()
         self.values = None

@@ -65,7 +65,10 @@ typedef enum sptrsv_dtype {
 } sptrsv_dtype;
 
 typedef enum sptrsv_schedule {
-  SPTRSV_SCHED_AUTO = 0,      /* autotuned choice (pull unless tuned otherwise) */
+  SPTRSV_SCHED_AUTO = 0,      /* pull executor with a plan chosen from the analysis (one rhs: warp-
+                                 synchronous lanes; level order, or level order inside blocks of ~32
+                                 level widths when >= 90 % of the dependencies stay inside them);
+                                 options the caller sets explicitly override the plan */
   SPTRSV_SCHED_PUSH = 1,      /* in-degree counters + atomic partial sums (the reference scheme) */
   SPTRSV_SCHED_PULL = 2,      /* dependency gather with value-as-flag words (deterministic) */
   SPTRSV_SCHED_LEVELSET = 3   /* level sets with one grid barrier per level */
@@ -117,6 +120,12 @@ typedef struct sptrsv_info {
   int order_block;
   double analysis_ms;   /* device time of the last analyse */
   size_t device_bytes;  /* device memory held by the handle */
+  /* one-rhs executor settings in effect (explicit options or the automatic plan) */
+  int block;            /* threads per CTA */
+  int warp_sync;        /* 1: warp-synchronous lanes */
+  int staged;           /* 1: TMA-staged chunks */
+  int split;            /* split length of the forward walk (0: one lane per unknown) */
+  int locality_permille; /* automatic plan: dependencies inside order blocks, per mille */
 } sptrsv_info;
 
 typedef struct sptrsv_gb300_handle_s *sptrsv_handle_t;
