@@ -475,6 +475,9 @@ int build_pieces(sptrsv_gb300_handle_s* h, PieceTable& t, const std::vector<int>
   std::vector<int> cseg, cbase;
   std::vector<unsigned char> seg_split_host;
   const size_t seg_cap = static_cast<size_t>(std::max(1, (chunk + 31) / 32));
+  // a reverse walk is shifted so that its chunk boundaries fall on multiples of
+  // `chunk` positions (the order blocks of a blocked layout)
+  const int shift = reversed ? (chunk - n % chunk) % chunk : 0;
   for (int i = 0; i < n; ++i) {
     const int p = reversed ? n - 1 - i : i;
     const long long c = counts[p], e0 = start[p];
@@ -482,7 +485,7 @@ int build_pieces(sptrsv_gb300_handle_s* h, PieceTable& t, const std::vector<int>
     const bool seg_full = walk.size() % 32 + k > 32;
     const size_t first = seg_full ? (walk.size() + 31) / 32 * 32 : walk.size();
     const size_t segs_after = (first + k - 1) / 32 + 1;  // segments in use once i is placed
-    if (i % chunk == 0 || (!cseg.empty() && segs_after - cseg.back() > seg_cap)) {
+    if ((i + shift) % chunk == 0 || i == 0 || (!cseg.empty() && segs_after - cseg.back() > seg_cap)) {
       pad();  // a chunk starts on a fresh segment
       cseg.push_back(static_cast<int>(walk.size() / 32));
       cbase.push_back(i);

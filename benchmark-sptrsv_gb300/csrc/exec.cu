@@ -30,6 +30,9 @@ namespace {
 template <typename T>
 struct ExecArgs {
   int n, rhs, chunk, nchunks, smem_tier, ctas_per_sm;
+  // pull walks: chunk c covers walk indices [c*chunk - walk_pad, (c+1)*chunk - walk_pad);
+  // the reverse (adjoint) walk is shifted so its chunks line up with order blocks
+  int walk_pad;
   const int* perm;
   const int* dep_ptr;
   const int* dep_pos;
@@ -145,8 +148,9 @@ __global__ void __launch_bounds__(256) k_pull_vec(ExecArgs<T> a) {
   for (;;) {
     const unsigned c = next_chunk(a.ctl, a.nchunks, &s_chunk);
     if (c >= (unsigned)a.nchunks) break;
-    const int base = static_cast<int>(c) * a.chunk;
-    const int cend = min(base + a.chunk, a.n);
+    const int base0 = static_cast<int>(c) * a.chunk - a.walk_pad;
+    const int base = max(base0, 0);
+    const int cend = min(base0 + a.chunk, a.n);
     if (a.smem_tier)
       for (int i = threadIdx.x; i < cend - base; i += blockDim.x)
         *reinterpret_cast<Bits*>(&s_x[i]) = F::EMPTY;
@@ -214,8 +218,9 @@ __global__ void __launch_bounds__(256) k_pull_wsync(ExecArgs<T> a) {
   for (;;) {
     const unsigned c = next_chunk(a.ctl, a.nchunks, &s_chunk);
     if (c >= (unsigned)a.nchunks) break;
-    const int base = static_cast<int>(c) * a.chunk;
-    const int cend = min(base + a.chunk, a.n);
+    const int base0 = static_cast<int>(c) * a.chunk - a.walk_pad;
+    const int base = max(base0, 0);
+    const int cend = min(base0 + a.chunk, a.n);
     const int len = cend - base;
     if (a.smem_tier)
       for (int i = threadIdx.x; i < len; i += blockDim.x) *reinterpret_cast<Bits*>(&s_x[i]) = F::EMPTY;
@@ -554,8 +559,9 @@ __global__ void __launch_bounds__(256) k_pull_wsync_multi(ExecArgs<T> a) {
   for (;;) {
     const unsigned c = next_chunk(a.ctl, a.nchunks, &s_chunk);
     if (c >= (unsigned)a.nchunks) break;
-    const int base = static_cast<int>(c) * a.chunk;
-    const int cend = min(base + a.chunk, a.n);
+    const int base0 = static_cast<int>(c) * a.chunk - a.walk_pad;
+    const int base = max(base0, 0);
+    const int cend = min(base0 + a.chunk, a.n);
     const int len = cend - base;
     if (a.smem_tier)
       for (long long i = threadIdx.x; i < (long long)len * rhs; i += blockDim.x)
@@ -712,8 +718,9 @@ __global__ void __launch_bounds__(256) k_pull_multi(ExecArgs<T> a) {
   for (;;) {
     const unsigned c = next_chunk(a.ctl, a.nchunks, &s_chunk);
     if (c >= (unsigned)a.nchunks) break;
-    const int base = static_cast<int>(c) * a.chunk;
-    const int cend = min(base + a.chunk, a.n);
+    const int base0 = static_cast<int>(c) * a.chunk - a.walk_pad;
+    const int base = max(base0, 0);
+    const int cend = min(base0 + a.chunk, a.n);
     if (a.smem_tier)
       for (long long i = threadIdx.x; i < (long long)(cend - base) * rhs; i += blockDim.x)
         *reinterpret_cast<typename F::Bits*>(&s_x[i]) = F::EMPTY;
@@ -1164,6 +1171,10 @@ cudaError_t launch_pull(const Layout& L, const Values<T>& V, int rhs, const VecV
     a.xf = adj->xf;
     a.xf_si = adj->xf_si;
     a.xf_sk = adj->xf_sk;
+    if (!use_pc) {
+      a.walk_pad = (a.chunk - a.n % a.chunk) % a.chunk;
+      a.nchunks = (a.n + a.walk_pad + a.chunk - 1) / a.chunk;
+    }
     return launch_pull_impl<T, true>(a, rhs, cfg, smem, num_sms, s);
   }
   return launch_pull_impl<T, false>(a, rhs, cfg, smem, num_sms, s);
