@@ -706,6 +706,12 @@ ExecConfig pick_config(const sptrsv_gb300_handle_s* h, int rhs) {
     if (planned(h, SPTRSV_OPTION_BACKOFF_NS)) c.sleep_max = static_cast<unsigned>(h->plan.backoff);
     if (planned(h, SPTRSV_OPTION_STAGED)) c.staged = h->plan.staged;
     if (planned(h, SPTRSV_OPTION_WARP_SYNC)) c.wsync = h->plan.wsync;
+  } else if (rhs > 1 && h->sched_option == SCHED_AUTO && h->plan.valid) {
+    // many rhs: warp-synchronous lane groups (up to 64 rhs), one unknown per group
+    // per chunk; a single CTA per SM measured fastest for narrow groups (rhs <= 4)
+    if (planned(h, SPTRSV_OPTION_WARP_SYNC)) c.wsync = rhs <= 64 ? 1 : 0;
+    if (planned(h, SPTRSV_OPTION_CTAS_PER_SM)) c.ctas_per_sm = rhs <= 4 ? 1 : 0;
+    if (planned(h, SPTRSV_OPTION_BACKOFF_NS)) c.sleep_max = rhs <= 4 ? 0u : 64u;
   }
   return c;
 }

@@ -356,19 +356,153 @@ __global__ void __launch_bounds__(256) k_pull_wsync(ExecArgs<T> a) {
 // segmented suffix sum over its lanes hands the head lane the value to publish.
 // A 1000-entry list then takes about as many lockstep iterations as a
 // 30-entry one, and only its last slice waits on the latest dependencies.
-template <typename T, bool ADJ>
-__global__ void __launch_bounds__(256) k_pull_wsync_split(ExecArgs<T> a) {
+// Segments without a split list run the one-lane loop (SPLIT = false).
+template <typename T, bool ADJ, bool SPLIT>
+__device__ __forceinline__ bool wsync_segment(const ExecArgs<T>& a, T* s_x, int cbase, int walk, int row, int e,
+                                              const int e1, unsigned at_or_below) {
   using F = Flag<T>;
   using Bits = typename F::Bits;
   constexpr int U = 4;
   constexpr unsigned kFull = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int* __restrict__ lpos = ADJ ? a.out_pos_f : a.dep_pos_f;
+  const T* __restrict__ vals = ADJ ? a.out_w : a.dep_w;
+  const int last = a.n - 1;
+  const bool valid = walk >= 0;
+  bool head = valid;
+  int ge = lane, gs = lane;
+  unsigned gmask = 0u;
+  if (SPLIT) {
+    const int prev = __shfl_up_sync(kFull, walk, 1);
+    head = valid && (lane == 0 || prev != walk);
+    const unsigned heads = __ballot_sync(kFull, head);
+    const unsigned valids = __ballot_sync(kFull, valid);
+    // this lane's group: from its head (at or below) to the lane before the next head
+    const unsigned above = heads & ~at_or_below;
+    ge = above ? __ffs(above) - 2 : 31 - __clz(valids);
+    gs = valid ? 31 - __clz(heads & at_or_below) : lane;
+    // head lanes: the lanes of their unknown (ge >= lane >= 0 there)
+    gmask = head ? (ge >= 31 ? kFull : ((2u << ge) - 1u)) & ~((1u << lane) - 1u) : 0u;
+  }
+  const int p = ADJ ? last - walk : walk;
+  T acc = T(0);
+  if (head) acc = a.b[(long long)row * a.b_si] * a.rcp[p];
+  auto slot = [&](int q) {
+    const int qr = ADJ ? last - q : q;
+    return (a.smem_tier && qr >= cbase) ? qr - cbase : -1;
+  };
+  auto publish = [&](T xi) {
+    if (a.smem_tier) F::store_shared(&s_x[walk - cbase], xi);
+    F::store(&a.xw[p], xi);
+    a.x[(long long)row * a.x_si] = xi;
+  };
+  int q[U], ls[U];
+  T w[U];
+  Bits bits[U];
+  unsigned todo = 0u;
+  auto load_batch = [&]() {
+    todo = 0u;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int ee = e + u;
+      q[u] = ee < e1 ? lpos[ee] : -1;
+      w[u] = ee < e1 ? vals[ee] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      ls[u] = -1;
+      bits[u] = F::EMPTY;
+      if (q[u] >= 0) {
+        ls[u] = slot(q[u]);
+        bits[u] = ls[u] >= 0 ? F::load_shared(&s_x[ls[u]]) : F::load(&a.xw[q[u]]);
+        todo |= 1u << u;
+      }
+    }
+  };
+  bool sdone = !valid;  // slice consumed (one-lane unknowns publish at the same moment)
+  bool done = !valid;   // unknown published
+  if (!sdone) load_batch();
+  WaitBudget wb(a.timeout_ns);
+  unsigned nap = a.sleep_min, idle = 0u;
+  for (;;) {
+    bool progress = false, global_wait = false;
+    if (!sdone) {
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (!(todo & (1u << u))) continue;
+        if (bits[u] != F::EMPTY) {
+          acc = fma(-w[u], F::value(bits[u]), acc);
+          todo &= ~(1u << u);
+          progress = true;
+        } else if (ls[u] < 0) {
+          global_wait = true;
+        }
+      }
+      if (!todo) {
+        e += U;
+        if (e < e1) {
+          load_batch();
+        } else {
+          sdone = true;
+          if (!SPLIT) {
+            publish(acc);
+            done = true;
+          }
+        }
+        progress = true;
+      } else {
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+          if ((todo & (1u << u)) && bits[u] == F::EMPTY)
+            bits[u] = ls[u] >= 0 ? F::load_shared(&s_x[ls[u]]) : F::load(&a.xw[q[u]]);
+      }
+    }
+    if (SPLIT) {
+      // publish every unknown whose slices are all in
+      const unsigned sd = __ballot_sync(kFull, sdone);
+      const bool ready = head && !done && (sd & gmask) == gmask;
+      if (__any_sync(kFull, ready)) {
+        T xi = acc;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          const T t = __shfl_down_sync(kFull, xi, off);
+          if (lane + off <= ge) xi += t;
+        }
+        if (ready) {
+          publish(xi);
+          done = true;
+          progress = true;
+        }
+        const unsigned pub = __ballot_sync(kFull, head && done);
+        if (valid && !head) done = (pub >> gs) & 1u;
+      }
+    }
+    if (__all_sync(kFull, done)) return false;
+    const bool any_progress = __any_sync(kFull, progress);
+    const bool any_global = __any_sync(kFull, global_wait);
+    __syncwarp();
+    if (!any_progress) {
+      if (any_global && a.sleep_max) {
+        __nanosleep(nap);
+        nap = nap * 2u < a.sleep_max ? nap * 2u : a.sleep_max;
+      }
+      bool fail = false;
+      if ((any_global || (++idle & 255u) == 0u) && !wb.poll(a.ctl, p)) fail = true;
+      if (__any_sync(kFull, fail)) return true;
+    } else {
+      nap = a.sleep_min;
+    }
+  }
+}
+
+template <typename T, bool ADJ>
+__global__ void __launch_bounds__(256) k_pull_wsync_split(ExecArgs<T> a) {
+  using F = Flag<T>;
+  using Bits = typename F::Bits;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* s_x = reinterpret_cast<T*>(smem_raw);
   __shared__ unsigned s_chunk;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  const int* __restrict__ lpos = ADJ ? a.out_pos_f : a.dep_pos_f;
-  const T* __restrict__ vals = ADJ ? a.out_w : a.dep_w;
-  const int last = a.n - 1;
   const unsigned at_or_below = (2u << lane) - 1u;  // lanes 0..lane (wraps to all lanes for lane 31)
   for (;;) {
     const unsigned c = next_chunk(a.ctl, a.nchunks, &s_chunk);
@@ -382,153 +516,22 @@ __global__ void __launch_bounds__(256) k_pull_wsync_split(ExecArgs<T> a) {
     __syncthreads();
     bool fail = false;
     // piece data of this warp's next segment is loaded one segment ahead
-    int n_walk = -1, n_lo = 0, n_hi = 0, n_row = 0;
-    if (seg0 + warp < seg1) {
-      const int pi = (seg0 + warp) * 32 + lane;
+    int n_walk = -1, n_lo = 0, n_hi = 0, n_row = 0, n_split = 0;
+    auto fetch = [&](int sg) {
+      const int pi = sg * 32 + lane;
       n_walk = a.pc_walk[pi];
       n_lo = a.pc_lo[pi];
       n_hi = a.pc_hi[pi];
       n_row = a.pc_row[pi];
-    }
+      n_split = a.pc_split[sg];
+    };
+    if (seg0 + warp < seg1) fetch(seg0 + warp);
     for (int seg = seg0 + warp; seg < seg1 && !fail; seg += nwarps) {
-      const int walk = n_walk;
-      int e = n_lo;
-      const int e1 = n_hi;
-      const int row = n_row;
-      if (seg + nwarps < seg1) {
-        const int pn = (seg + nwarps) * 32 + lane;
-        n_walk = a.pc_walk[pn];
-        n_lo = a.pc_lo[pn];
-        n_hi = a.pc_hi[pn];
-        n_row = a.pc_row[pn];
-      }
-      const bool valid = walk >= 0;
-      const bool split = a.pc_split[seg] != 0;  // some unknown of the segment spans several lanes
-      bool head = valid;
-      int ge = lane, gs = lane;
-      unsigned gmask = 0u;
-      if (split) {
-        const int prev = __shfl_up_sync(kFull, walk, 1);
-        head = valid && (lane == 0 || prev != walk);
-        const unsigned heads = __ballot_sync(kFull, head);
-        const unsigned valids = __ballot_sync(kFull, valid);
-        // this lane's group: from its head (at or below) to the lane before the next head
-        const unsigned above = heads & ~at_or_below;
-        ge = above ? __ffs(above) - 2 : 31 - __clz(valids);
-        gs = valid ? 31 - __clz(heads & at_or_below) : lane;
-        // head lanes: the lanes of their unknown (ge >= lane >= 0 there)
-        gmask = head ? (ge >= 31 ? kFull : ((2u << ge) - 1u)) & ~((1u << lane) - 1u) : 0u;
-      }
-      const int p = ADJ ? last - walk : walk;
-      T acc = T(0);
-      if (head) acc = a.b[(long long)row * a.b_si] * a.rcp[p];
-      auto slot = [&](int q) {
-        const int qr = ADJ ? last - q : q;
-        return (a.smem_tier && qr >= cbase) ? qr - cbase : -1;
-      };
-      int q[U], ls[U];
-      T w[U];
-      Bits bits[U];
-      unsigned todo = 0u;
-      auto load_batch = [&]() {
-        todo = 0u;
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int ee = e + u;
-          q[u] = ee < e1 ? lpos[ee] : -1;
-          w[u] = ee < e1 ? vals[ee] : T(0);
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          ls[u] = -1;
-          bits[u] = F::EMPTY;
-          if (q[u] >= 0) {
-            ls[u] = slot(q[u]);
-            bits[u] = ls[u] >= 0 ? F::load_shared(&s_x[ls[u]]) : F::load(&a.xw[q[u]]);
-            todo |= 1u << u;
-          }
-        }
-      };
-      bool sdone = !valid || e >= e1;  // slice consumed
-      bool done = !valid;              // unknown published
-      if (!sdone) load_batch();
-      WaitBudget wb(a.timeout_ns);
-      unsigned nap = a.sleep_min, idle = 0u;
-      for (;;) {
-        bool progress = false, global_wait = false;
-        if (!sdone) {
-#pragma unroll
-          for (int u = 0; u < U; ++u) {
-            if (!(todo & (1u << u))) continue;
-            if (bits[u] != F::EMPTY) {
-              acc = fma(-w[u], F::value(bits[u]), acc);
-              todo &= ~(1u << u);
-              progress = true;
-            } else if (ls[u] < 0) {
-              global_wait = true;
-            }
-          }
-          if (!todo) {
-            e += U;
-            if (e < e1) {
-              load_batch();
-            } else {
-              sdone = true;
-            }
-            progress = true;
-          } else {
-#pragma unroll
-            for (int u = 0; u < U; ++u)
-              if ((todo & (1u << u)) && bits[u] == F::EMPTY)
-                bits[u] = ls[u] >= 0 ? F::load_shared(&s_x[ls[u]]) : F::load(&a.xw[q[u]]);
-          }
-        }
-        // publish every unknown whose slices are all in
-        if (split) {
-          const unsigned sd = __ballot_sync(kFull, sdone);
-          const bool ready = head && !done && (sd & gmask) == gmask;
-          if (__any_sync(kFull, ready)) {
-            T xi = acc;
-#pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-              const T t = __shfl_down_sync(kFull, xi, off);
-              if (lane + off <= ge) xi += t;
-            }
-            if (ready) {
-              if (a.smem_tier) F::store_shared(&s_x[walk - cbase], xi);
-              F::store(&a.xw[p], xi);
-              a.x[(long long)row * a.x_si] = xi;
-              done = true;
-              progress = true;
-            }
-            const unsigned pub = __ballot_sync(kFull, head && done);
-            if (valid && !head) done = (pub >> gs) & 1u;
-          }
-        } else if (sdone && !done) {  // one lane per unknown
-          // (publishing here rather than next to the last batch measured faster)
-          if (a.smem_tier) F::store_shared(&s_x[walk - cbase], acc);
-          F::store(&a.xw[p], acc);
-          a.x[(long long)row * a.x_si] = acc;
-          done = true;
-          progress = true;
-        }
-        if (__all_sync(kFull, done)) break;
-        const bool any_progress = __any_sync(kFull, progress);
-        const bool any_global = __any_sync(kFull, global_wait);
-        if (!any_progress) {
-          if (any_global && a.sleep_max) {
-            __nanosleep(nap);
-            nap = nap * 2u < a.sleep_max ? nap * 2u : a.sleep_max;
-          }
-          if ((any_global || (++idle & 255u) == 0u) && !wb.poll(a.ctl, p)) fail = true;
-          if (__any_sync(kFull, fail)) {
-            fail = true;
-            break;
-          }
-        } else {
-          nap = a.sleep_min;
-        }
-      }
+      const int walk = n_walk, lo = n_lo, hi = n_hi, row = n_row;
+      const bool split = n_split != 0;  // some unknown of the segment spans several lanes
+      if (seg + nwarps < seg1) fetch(seg + nwarps);
+      fail = split ? wsync_segment<T, ADJ, true>(a, s_x, cbase, walk, row, lo, hi, at_or_below)
+                   : wsync_segment<T, ADJ, false>(a, s_x, cbase, walk, row, lo, hi, at_or_below);
     }
     if (__syncthreads_or(fail)) break;
   }
