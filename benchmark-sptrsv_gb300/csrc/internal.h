@@ -211,6 +211,10 @@ template <typename T>
 cudaError_t launch_grad_values(const int* csc_row, const int* csc_col, int nnz, int rhs, const T* lambda,
                                const T* x, long long si, long long sk, T* dval, cudaStream_t s);
 
+// out (cols x rows, row-major) = transpose of in (rows x cols, row-major)
+template <typename T>
+cudaError_t launch_transpose(const T* in, T* out, int rows, int cols, cudaStream_t s);
+
 // ---------------------------------------------------------------- mixed precision
 cudaError_t launch_cast_d2f(const double* in, float* out, long long count, cudaStream_t s);
 cudaError_t launch_residual(const Layout& L, const Values<double>& V, int rhs, const double* b, const double* x,

@@ -79,6 +79,36 @@ __global__ void k_init_x(double* x, const float* __restrict__ d, long long count
   if ((threadIdx.x & 31) == 0) atomicMax(&stats[1], static_cast<unsigned long long>(__double_as_longlong(xmax)));
 }
 
+// out[c * rows + r] = in[r * cols + c]: a rows x cols row-major matrix to its
+// transpose, through 32 x 32 shared-memory tiles (coalesced on both sides);
+// one CTA per tile, tiles numbered row-major over the input.
+template <typename T>
+__global__ void k_transpose(const T* __restrict__ in, T* __restrict__ out, int rows, int cols, long long ctiles) {
+  __shared__ T tile[32][33];
+  const long long t = blockIdx.x;
+  const int r0 = static_cast<int>(t / ctiles) * 32, c0 = static_cast<int>(t % ctiles) * 32;
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int r = r0 + i, c = c0 + threadIdx.x;
+    if (r < rows && c < cols) tile[i][threadIdx.x] = in[(long long)r * cols + c];
+  }
+  __syncthreads();
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int c = c0 + i, r = r0 + threadIdx.x;
+    if (r < rows && c < cols) out[(long long)c * rows + r] = tile[threadIdx.x][i];
+  }
+}
+
+template <typename T>
+cudaError_t launch_transpose(const T* in, T* out, int rows, int cols, cudaStream_t s) {
+  if (rows <= 0 || cols <= 0) return cudaSuccess;
+  const long long rtiles = (rows + 31) / 32, ctiles = (cols + 31) / 32;
+  if (rtiles * ctiles > 0x7fffffffLL) return cudaErrorInvalidValue;
+  k_transpose<T><<<static_cast<unsigned>(rtiles * ctiles), dim3(32, 8), 0, s>>>(in, out, rows, cols, ctiles);
+  return cudaGetLastError();
+}
+template cudaError_t launch_transpose<double>(const double*, double*, int, int, cudaStream_t);
+template cudaError_t launch_transpose<float>(const float*, float*, int, int, cudaStream_t);
+
 cudaError_t launch_cast_d2f(const double* in, float* out, long long count, cudaStream_t s) {
   if (count <= 0) return cudaSuccess;
   k_cast<double, float><<<grid_1d(count), 256, 0, s>>>(in, out, count);
