@@ -713,6 +713,13 @@ ExecConfig pick_config(const sptrsv_gb300_handle_s* h, int rhs) {
     if (planned(h, SPTRSV_OPTION_WARP_SYNC)) c.wsync = rhs <= 64 ? 1 : 0;
     if (planned(h, SPTRSV_OPTION_CTAS_PER_SM)) c.ctas_per_sm = rhs <= 4 ? 1 : 0;
     if (planned(h, SPTRSV_OPTION_BACKOFF_NS)) c.sleep_max = rhs <= 4 ? 0u : 64u;
+    // a blocked layout: one CTA per order block (small chunks would hand the
+    // blocks out one after another); the shared-memory tier does not fit there
+    if (planned(h, SPTRSV_OPTION_CHUNK) && h->layout_block > 0 && h->layout_block < h->n) {
+      c.chunk = h->layout_block;
+      c.ctas_per_sm = 0;
+      c.sleep_max = 0u;
+    }
   }
   return c;
 }
@@ -1573,7 +1580,8 @@ int sptrsv_gb300_tune(sptrsv_handle_t h, const void* d_val, int dtype, int rhs, 
   } else {
     // chunk 0 = one unknown per lane group
     for (int bo : {64, 512}) cands.push_back({SCHED_PULL, big, 0, 0, bo, 0, 1, 2, 1, 256, sp});
-    for (int ob : {1024, 4096}) cands.push_back({SCHED_PULL, ob, ob, 0, 0, 0, 1, 2, 1, 256, sp});
+    cands.push_back({SCHED_PULL, big, 0, 0, 0, 1, 1, 2, 1, 256, sp});
+    for (int ob : {1024, 4096, 16384}) cands.push_back({SCHED_PULL, ob, ob, 0, 0, 0, 1, 2, 1, 256, sp});
     cands.push_back({SCHED_PULL, big, 0, 0, 256, 0, 1, 2, 0, 256, sp});
     cands.push_back({SCHED_LEVELSET, big, 256, 0, 256, 1, 8, 2, 0, 256, sp});
     cands.push_back({SCHED_PUSH, big, 0, 0, 256, 0, 1, 2, 0, 256, sp});
