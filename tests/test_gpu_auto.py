@@ -1,0 +1,81 @@
+"""The automatic executor plan (SPTRSV_SCHED_AUTO): what it picks from the
+analysis and that every path it picks matches the oracle (FP64, <= 1e-12
+relative in the max norm)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+
+
+def relerr(x, ref):
+    x = np.asarray(x, dtype=np.float64).ravel()
+    ref = np.asarray(ref, dtype=np.float64).ravel()
+    return float(np.max(np.abs(x - ref)) / max(np.max(np.abs(ref)), 1e-300))
+
+
+def _solver(m, **kw):
+    from sptrsv_gb300 import SyncFreeSolver
+    return SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, values=m.val, **kw)
+
+
+@pytest.mark.parametrize("lower", [True, False])
+def test_local_deep_dag_gets_blocked_order(cuda, oracle_port, lower):
+    from sptrsv_gb300 import matgen
+    m = matgen.laplace2d_lower(200, lower=lower)          # 399 levels, 100 unknowns per level
+    s = _solver(m)
+    inf = s.info()
+    assert inf["nlevels"] == 399
+    blk = 32 * -(-m.n // inf["nlevels"])                  # 32 level widths
+    assert inf["order_block"] == blk and inf["chunk"] == blk and inf["warp_sync"] == 1 and inf["staged"] == 0
+    assert inf["locality_permille"] >= 900
+    for rhs in (1, 4, 16):
+        b = np.random.default_rng(rhs).standard_normal((m.n, rhs))
+        ref = oracle_port.solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, b)
+        x = s.solve(cuda.from_numpy(b).cuda()).cpu().numpy()
+        assert relerr(x, ref) <= TOL64
+    # the transposed solve walks the blocked layout in reverse
+    g = np.random.default_rng(7).standard_normal(m.n)
+    t = m.transpose()
+    ref = oracle_port.solve(t.col_ptr, t.row_idx, t.val, t.n, t.substitution, g)
+    lam = s.solve_adjoint(cuda.from_numpy(g).cuda()).cpu().numpy()
+    assert relerr(lam, ref) <= TOL64
+
+
+def test_wide_dag_stays_in_level_order(cuda, oracle_port):
+    from sptrsv_gb300 import matgen
+    m = matgen.poisson_band(20_000, 9.0, 4000, seed=5)     # dependencies spread over 4000 rows
+    s = _solver(m)
+    inf = s.info()
+    assert inf["order_block"] >= m.n and inf["chunk"] == 256 and inf["block"] == 256 and inf["warp_sync"] == 1
+    b = np.random.default_rng(1).standard_normal(m.n)
+    ref = oracle_port.solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, b)
+    assert relerr(s.solve(cuda.from_numpy(b).cuda()).cpu().numpy(), ref) <= TOL64
+
+
+def test_long_lists_get_split(cuda, oracle_port):
+    from sptrsv_gb300 import matgen
+    m = matgen.power_law_band(30_000, 300_000, 3000, seed=3, lower=False)   # long rows in the upper triangle
+    s = _solver(m)
+    assert s.info()["split"] == 32
+    b = np.random.default_rng(2).standard_normal(m.n)
+    ref = oracle_port.solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, b)
+    assert relerr(s.solve(cuda.from_numpy(b).cuda()).cpu().numpy(), ref) <= TOL64
+
+
+def test_explicit_options_override_the_plan(cuda, oracle_port):
+    from sptrsv_gb300 import _lib, matgen
+    m = matgen.laplace2d_lower(200)
+    s = _solver(m, order_block=10**9, staged=True)
+    inf = s.info()
+    assert inf["order_block"] >= m.n and inf["staged"] == 1
+    s2 = _solver(m, schedule=2)                              # explicit schedule: no plan at all
+    assert s2.info()["warp_sync"] == 0
+    b = np.random.default_rng(3).standard_normal(m.n)
+    ref = oracle_port.solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, b)
+    for solver in (s, s2):
+        assert relerr(solver.solve(cuda.from_numpy(b).cuda()).cpu().numpy(), ref) <= TOL64
+    assert s.get_option(_lib.OPTION_SCHEDULE) == 0
