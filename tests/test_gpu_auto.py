@@ -41,7 +41,8 @@ def test_local_deep_dag_gets_blocked_order(cuda, oracle_port, lower):
     g = np.random.default_rng(7).standard_normal(m.n)
     t = m.transpose()
     ref = oracle_port.solve(t.col_ptr, t.row_idx, t.val, t.n, t.substitution, g)
-    lam = s.solve_adjoint(cuda.from_numpy(g).cuda()).cpu().numpy()
+    lam, _ = s.solve_adjoint(cuda.from_numpy(g).cuda())
+    lam = lam.cpu().numpy()
     assert relerr(lam, ref) <= TOL64
 
 
