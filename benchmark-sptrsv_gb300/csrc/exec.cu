@@ -118,10 +118,6 @@ __device__ __forceinline__ typename Flag<T>::Bits wait_flag(const T* p, DeviceCt
   return wait_flag_dev<T, SHARED>(p, ctl, timeout, where, sleep_min, sleep_max);
 }
 
-// Warp-synchronous executors: global polls are read every this many lockstep
-// iterations while shared-memory dependencies are pending in the warp.
-constexpr unsigned kGlobalEvery = 8u;
-
 // ------------------------------------------------------------------ pull, one rhs
 // x_p = b_p/d_p - sum_j w_j x_j with w = L(p,j)/d_p staged in advance, so each
 // dependency costs one fused multiply-add once its value is published
@@ -287,32 +283,13 @@ __global__ void __launch_bounds__(256) k_pull_wsync(ExecArgs<T> a) {
       if (!done) load_batch();
       WaitBudget wb(a.timeout_ns);
       unsigned nap = a.sleep_min, idle = 0u;
-      // While some lane of the warp waits on a shared-memory dependency, global
-      // dependencies are read only every kGlobalEvery-th iteration: reading a
-      // global poll stalls the whole warp for an L2 round trip, which would
-      // otherwise set the pace of in-chunk (shared-memory) hops.
-      unsigned it = 0u;
-      bool check_global;
-      {
-        bool local_wait = false;
-#pragma unroll
-        for (int u = 0; u < U; ++u)
-          if (!done && (todo & (1u << u)) && ls[u] >= 0) local_wait = true;
-        check_global = !__any_sync(0xffffffffu, local_wait);
-      }
       for (;;) {
         bool progress = false, global_wait = false;
-        const bool polled_global = check_global;
         if (!done) {
           bool prefix = true;
 #pragma unroll
           for (int u = 0; u < U; ++u) {
             if (!(todo & (1u << u))) continue;
-            if (ls[u] < 0 && !check_global) {  // global slot not read this iteration
-              prefix = false;
-              global_wait = true;
-              continue;
-            }
             if (bits[u] != F::EMPTY && (!EXACT || prefix)) {
               acc = EXACT ? exact_mul_add<T>(acc, w[u], F::value(bits[u])) : fma(-w[u], F::value(bits[u]), acc);
               todo &= ~(1u << u);
@@ -342,33 +319,21 @@ __global__ void __launch_bounds__(256) k_pull_wsync(ExecArgs<T> a) {
             }
           } else {
 #pragma unroll
-            for (int u = 0; u < U; ++u) {
-              if (!(todo & (1u << u))) continue;
-              if (ls[u] >= 0) {
-                if (bits[u] == F::EMPTY) bits[u] = F::load_shared(&s_x[ls[u]]);
-              } else if (check_global && bits[u] == F::EMPTY) {
-                bits[u] = F::load(&a.xw[q[u]]);
-              }
-            }
+            for (int u = 0; u < U; ++u)
+              if ((todo & (1u << u)) && bits[u] == F::EMPTY)
+                bits[u] = ls[u] >= 0 ? F::load_shared(&s_x[ls[u]]) : F::load(&a.xw[q[u]]);
           }
         }
         if (__all_sync(0xffffffffu, done)) break;
-        bool local_wait = false;
-#pragma unroll
-        for (int u = 0; u < U; ++u)
-          if (!done && (todo & (1u << u)) && ls[u] >= 0) local_wait = true;
         const bool any_progress = __any_sync(0xffffffffu, progress);
         const bool any_global = __any_sync(0xffffffffu, global_wait);
-        const bool any_local = __any_sync(0xffffffffu, local_wait);
-        ++it;
-        check_global = !any_local || (it & (kGlobalEvery - 1u)) == 0u;
         __syncwarp();
         if (!any_progress) {
-          if (any_global && polled_global && a.sleep_max) {
+          if (any_global && a.sleep_max) {
             __nanosleep(nap);
             nap = nap * 2u < a.sleep_max ? nap * 2u : a.sleep_max;
           }
-          if (((any_global && polled_global) || (++idle & 255u) == 0u) && !wb.poll(a.ctl, p)) fail = true;
+          if ((any_global || (++idle & 255u) == 0u) && !wb.poll(a.ctl, p)) fail = true;
           if (__any_sync(0xffffffffu, fail)) {
             fail = true;
             break;
