@@ -180,7 +180,6 @@ void free_layout(Layout& L) {
   dev_free(&L.out_pos_f);
   dev_free(&L.out_src_f);
   dev_free(&L.level_ptr);
-  dev_free(&L.level_long);
   L = Layout();
 }
 
@@ -402,16 +401,6 @@ int build_layout(sptrsv_gb300_handle_s* h, int block, cudaStream_t s) {
     ST_TRY(dev_alloc(h, &L.level_ptr, (size_t)h->nlevels + 1));
     CUDA_TRY(cudaMemcpyAsync(L.level_ptr, L.level_ptr_host.data(), sizeof(int) * (h->nlevels + 1),
                              cudaMemcpyHostToDevice, s));
-    // the run of long lists at the head of each level (the layout puts them first)
-    std::vector<int> lng(h->nlevels > 0 ? h->nlevels : 1, 0);
-    for (int l = 0; l < h->nlevels; ++l) {
-      int p = L.level_ptr_host[l];
-      const int p1 = L.level_ptr_host[l + 1];
-      while (p < p1 && h->dep_cnt_host[p] > kLongDeps) ++p;
-      lng[l] = p;
-    }
-    ST_TRY(dev_alloc(h, &L.level_long, lng.size()));
-    CUDA_TRY(cudaMemcpyAsync(L.level_long, lng.data(), sizeof(int) * lng.size(), cudaMemcpyHostToDevice, s));
   }
   CUDA_TRY(cudaStreamSynchronize(s));
   h->layout_block = block;
@@ -586,7 +575,7 @@ bool planned(const sptrsv_gb300_handle_s* h, int opt) {
 }
 
 int effective_block(const sptrsv_gb300_handle_s* h) {
-  if (h->sched_option == SCHED_LEVELSET || h->sched_option == SCHED_LEVEL_CTA) return INT_MAX;
+  if (h->sched_option == SCHED_LEVELSET) return INT_MAX;
   if (planned(h, SPTRSV_OPTION_ORDER_BLOCK)) return h->plan.order_block;
   return h->order_block;
 }
@@ -758,8 +747,7 @@ int solve_typed(sptrsv_gb300_handle_s* h, const Values<T>& V, int rhs, int layou
     ST_TRY(ensure_buf(h, h->counters, (size_t)n * sizeof(unsigned), 1, s));
   } else {
     ST_TRY(ensure_buf(h, h->xw, elems * sizeof(T), 0, s));
-    if (c.sched != SCHED_LEVELSET && c.sched != SCHED_LEVEL_CTA)
-      CUDA_TRY(cudaMemsetAsync(h->xw.p, 0xFF, elems * sizeof(T), s));
+    if (c.sched != SCHED_LEVELSET) CUDA_TRY(cudaMemsetAsync(h->xw.p, 0xFF, elems * sizeof(T), s));
   }
   if (h->profile) {
     if (!h->ev_exec[0]) {
@@ -771,9 +759,7 @@ int solve_typed(sptrsv_gb300_handle_s* h, const Values<T>& V, int rhs, int layou
   if (c.sched == SCHED_PUSH) {
     CUDA_TRY(launch_push<T>(h->layout, V, rhs, v, static_cast<T*>(h->left_sum.p),
                             static_cast<unsigned*>(h->counters.p), h->ctl, c, timeout_ns(h), h->num_sms, s));
-  } else if (c.sched == SCHED_LEVEL_CTA && rhs == 1 && !adj && !c.exact && h->layout.level_long) {
-    CUDA_TRY(launch_levelset_cta<T>(h->layout, V, v, static_cast<T*>(h->xw.p), s));
-  } else if (c.sched == SCHED_LEVELSET || c.sched == SCHED_LEVEL_CTA) {
+  } else if (c.sched == SCHED_LEVELSET) {
     CUDA_TRY(launch_levelset<T>(h->layout, V, rhs, v, static_cast<T*>(h->xw.p), h->ctl, c, timeout_ns(h), s));
   } else if (rhs == 1 && c.staged &&
              (c.emax > 0 ? fit_emax(c.chunk, sizeof(T), c.stages, c.smem_tier, c.emax) == c.emax
@@ -898,7 +884,7 @@ int sptrsv_gb300_set_option(sptrsv_handle_t h, int option, long long value) {
 static int set_option_value(sptrsv_handle_t h, int option, long long value) {
   switch (option) {
     case SPTRSV_OPTION_SCHEDULE:
-      if (value < SCHED_AUTO || value > SCHED_LEVEL_CTA) return SPTRSV_ERR_INVALID;
+      if (value < SCHED_AUTO || value > SCHED_LEVELSET) return SPTRSV_ERR_INVALID;
       h->sched_option = static_cast<int>(value);
       return SPTRSV_OK;
     case SPTRSV_OPTION_LANES:
@@ -1427,7 +1413,7 @@ int sptrsv_gb300_solve_adjoint(sptrsv_handle_t h, const void* d_val, int dtype, 
   if (dtype != SPTRSV_DTYPE_F64 && dtype != SPTRSV_DTYPE_F32) return SPTRSV_ERR_INVALID;
   if (h->n == 0) return SPTRSV_OK;
   if (!d_g || !d_lambda || (d_dval && !d_x)) return SPTRSV_ERR_INVALID;
-  if (h->sched_option == SCHED_LEVELSET || h->sched_option == SCHED_LEVEL_CTA) return SPTRSV_ERR_UNSUPPORTED;
+  if (h->sched_option == SCHED_LEVELSET) return SPTRSV_ERR_UNSUPPORTED;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int before = h->layout_block;
   ST_TRY(ensure_layout(h, s));

@@ -63,8 +63,6 @@ struct ExecArgs {
   unsigned sleep_min, sleep_max;  // backoff of global polls (ns)
   const int* level_ptr;
   int nlevels;
-  const int* level_long;  // level_long[l]: end of the long lists at the head of level l
-  int win;                // single-CTA level executor: shared-memory window (power of two)
   // split-list work units (k_pull_wsync_split): piece i covers entries
   // [pc_lo[i], pc_hi[i]) of walk index pc_walk[i] (-1: padding); 32 pieces per
   // warp segment; chunk c = segments [pc_cseg[c], pc_cseg[c+1]), starting at
@@ -1033,66 +1031,6 @@ __global__ void __launch_bounds__(256) k_levelset(ExecArgs<T> a) {
   }
 }
 
-// ------------------------------------------------------------------ level sets inside one CTA
-// Deep DAGs with narrow levels: one CTA of 1024 threads walks the levels with
-// a CTA barrier between them (a few hundred cycles, against a global-memory
-// hop of ~1 µs per level for the grid-wide executors). The values of the
-// last `win` positions stay in a shared-memory ring: during level l a
-// dependency q is read from the ring when q >= level_end(l) - win (those
-// slots are not rewritten during the level), from global memory otherwise
-// (published in an earlier level by this CTA; visible after the barrier).
-// Lists longer than 32 entries (placed first in each level) take a warp each.
-// No waits: every thread reaches every barrier.
-template <typename T>
-__global__ void __launch_bounds__(1024) k_levelset_cta(ExecArgs<T> a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* s_x = reinterpret_cast<T*>(smem_raw);
-  const int mask = a.win - 1;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
-  const int* __restrict__ pos = a.dep_pos_f;
-  const T* __restrict__ w = a.dep_w;
-  T* xw = a.xw;
-  for (int l = 0; l < a.nlevels; ++l) {
-    const int p0 = a.level_ptr[l], p1 = a.level_ptr[l + 1], pl = a.level_long[l];
-    const int lo = p1 - a.win;
-    auto xval = [&](int q) -> T { return q >= lo ? s_x[q & mask] : xw[q]; };
-    for (int p = p0 + warp; p < pl; p += nwarps) {  // long lists: a warp each
-      const int e0 = a.dep_ptr[p], e1 = a.dep_ptr[p + 1];
-      T acc = T(0);
-      for (int e = e0 + lane; e < e1; e += 32) acc = fma(-w[e], xval(pos[e]), acc);
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-      if (lane == 0) {
-        const int row = a.perm[p];
-        const T xi = fma(a.b[(long long)row * a.b_si], a.rcp[p], acc);
-        s_x[p & mask] = xi;
-        xw[p] = xi;
-        a.x[(long long)row * a.x_si] = xi;
-      }
-    }
-    for (int p = pl + tid; p < p1; p += blockDim.x) {  // short lists: a thread each
-      const int row = a.perm[p];
-      const int e0 = a.dep_ptr[p], e1 = a.dep_ptr[p + 1];
-      T acc = a.b[(long long)row * a.b_si] * a.rcp[p];
-      int e = e0;
-      for (; e + 4 <= e1; e += 4) {  // four independent gathers in flight
-        const int q0 = pos[e], q1 = pos[e + 1], q2 = pos[e + 2], q3 = pos[e + 3];
-        const T v0 = xval(q0), v1 = xval(q1), v2 = xval(q2), v3 = xval(q3);
-        acc = fma(-w[e], v0, acc);
-        acc = fma(-w[e + 1], v1, acc);
-        acc = fma(-w[e + 2], v2, acc);
-        acc = fma(-w[e + 3], v3, acc);
-      }
-      for (; e < e1; ++e) acc = fma(-w[e], xval(pos[e]), acc);
-      s_x[p & mask] = acc;
-      xw[p] = acc;
-      a.x[(long long)row * a.x_si] = acc;
-    }
-    __syncthreads();
-  }
-}
-
-
 template <typename T>
 ExecArgs<T> make_args(const Layout& L, const Values<T>& V, int rhs, const VecView<T>& v, int chunk) {
   ExecArgs<T> a{};
@@ -1284,24 +1222,6 @@ cudaError_t launch_push(const Layout& L, const Values<T>& V, int rhs, const VecV
   return run(k_push_multi<T, 32, 2>, a, block, 0, num_sms, s);
 }
 
-size_t levelset_cta_smem_bytes(size_t elem) { return (size_t)(elem == 8 ? 16384 : 32768) * elem; }
-
-template <typename T>
-cudaError_t launch_levelset_cta(const Layout& L, const Values<T>& V, const VecView<T>& v, T* xw, cudaStream_t s) {
-  if (L.n == 0) return cudaSuccess;
-  ExecArgs<T> a = make_args<T>(L, V, 1, v, 1024);
-  a.xw = xw;
-  a.level_ptr = L.level_ptr;
-  a.level_long = L.level_long;
-  a.nlevels = L.nlevels;
-  a.win = sizeof(T) == 8 ? 16384 : 32768;
-  const size_t smem = levelset_cta_smem_bytes(sizeof(T));
-  cudaError_t e = cudaFuncSetAttribute(k_levelset_cta<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  k_levelset_cta<T><<<1, 1024, smem, s>>>(a);
-  return cudaGetLastError();
-}
-
 template <typename T>
 cudaError_t launch_levelset(const Layout& L, const Values<T>& V, int rhs, const VecView<T>& v, T* xw, DeviceCtl* ctl,
                             const ExecConfig& cfg, unsigned long long timeout_ns, cudaStream_t s) {
@@ -1450,8 +1370,6 @@ cudaError_t launch_ref_executor(const int* col_ptr, const int* row_idx, const T*
                                       DeviceCtl*, const ExecConfig&, unsigned long long, int, cudaStream_t);     \
   template cudaError_t launch_levelset<T>(const Layout&, const Values<T>&, int, const VecView<T>&, T*,           \
                                           DeviceCtl*, const ExecConfig&, unsigned long long, cudaStream_t);      \
-  template cudaError_t launch_levelset_cta<T>(const Layout&, const Values<T>&, const VecView<T>&, T*,            \
-                                              cudaStream_t);                                                     \
   template cudaError_t launch_grad_values<T>(const int*, const int*, int, int, const T*, const T*, long long,     \
                                              long long, T*, cudaStream_t);                                       \
   template cudaError_t launch_ref_executor<T>(const int*, const int*, const T*, int*, T*, int, int, int, int,    \

@@ -21,7 +21,7 @@ enum StructFlags : int {
 };
 
 // Executor families.
-enum Sched : int { SCHED_AUTO = 0, SCHED_PUSH = 1, SCHED_PULL = 2, SCHED_LEVELSET = 3, SCHED_LEVEL_CTA = 4 };
+enum Sched : int { SCHED_AUTO = 0, SCHED_PUSH = 1, SCHED_PULL = 2, SCHED_LEVELSET = 3 };
 
 struct ExecConfig {
   int sched = SCHED_PULL;
@@ -105,7 +105,6 @@ struct Layout {
   int nlevels = 0;
   std::vector<int> level_ptr_host;
   int* level_ptr = nullptr;  // [nlevels+1] (positions)
-  int* level_long = nullptr; // [nlevels] end of the lists longer than 32 entries at the head of each level
 };
 
 template <typename T>
@@ -202,10 +201,6 @@ cudaError_t launch_levelset(const Layout& L, const Values<T>& V, int rhs, const 
                             DeviceCtl* ctl, const ExecConfig& cfg, unsigned long long timeout_ns,
                             cudaStream_t s);
 size_t pull_smem_bytes(int chunk, int rhs, size_t elem);
-// one CTA, level by level, recent values in a shared-memory window (one rhs, level-order layout)
-size_t levelset_cta_smem_bytes(size_t elem);
-template <typename T>
-cudaError_t launch_levelset_cta(const Layout& L, const Values<T>& V, const VecView<T>& v, T* xw, cudaStream_t s);
 size_t staged_smem_bytes(int cmax, int emax, size_t elem, bool smem_tier, int stages);
 template <typename T>
 cudaError_t launch_pull_staged(const Layout& L, const Values<T>& V, const ChunkTable& tab, const VecView<T>& v, T* xw,

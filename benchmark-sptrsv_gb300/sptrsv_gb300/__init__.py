@@ -8,7 +8,7 @@ preparation (Matrix Market / CSC files, triangle extraction, manufactured b).
 """
 from . import matgen, mtx
 from ._lib import (DTYPE_F32, DTYPE_F64, LAYOUT_COL_MAJOR, LAYOUT_ROW_MAJOR, OPT_WARP_AUTO, OPT_WARP_NNZ,
-                   OPT_WARP_RHS, SCHED_AUTO, SCHED_LEVEL_CTA, SCHED_LEVELSET, SCHED_PULL, SCHED_PUSH, SUBSTITUTION_BACKWARD,
+                   OPT_WARP_RHS, SCHED_AUTO, SCHED_LEVELSET, SCHED_PULL, SCHED_PUSH, SUBSTITUTION_BACKWARD,
                    SUBSTITUTION_FORWARD, SptrsvError, load)
 from .solver import SyncFreeSolver, analyser, executor, sptrsv_syncfree_cuda
 
@@ -22,5 +22,5 @@ __all__ = [
     "matgen", "mtx", "load", "sparse_triangular_solve", "SptrsvError", "SyncFreeSolver", "analyser", "executor", "sptrsv_syncfree_cuda",
     "SUBSTITUTION_FORWARD", "SUBSTITUTION_BACKWARD", "OPT_WARP_NNZ", "OPT_WARP_RHS", "OPT_WARP_AUTO",
     "LAYOUT_ROW_MAJOR", "LAYOUT_COL_MAJOR", "DTYPE_F64", "DTYPE_F32", "SCHED_AUTO", "SCHED_PUSH",
-    "SCHED_PULL", "SCHED_LEVELSET", "SCHED_LEVEL_CTA",
+    "SCHED_PULL", "SCHED_LEVELSET",
 ]

@@ -40,7 +40,6 @@ SCHED_AUTO = 0
 SCHED_PUSH = 1
 SCHED_PULL = 2
 SCHED_LEVELSET = 3
-SCHED_LEVEL_CTA = 4
 
 OPTION_SCHEDULE = 0
 OPTION_LANES = 1

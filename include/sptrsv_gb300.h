@@ -71,10 +71,7 @@ typedef enum sptrsv_schedule {
                                  options the caller sets explicitly override the plan */
   SPTRSV_SCHED_PUSH = 1,      /* in-degree counters + atomic partial sums (the reference scheme) */
   SPTRSV_SCHED_PULL = 2,      /* dependency gather with value-as-flag words (deterministic) */
-  SPTRSV_SCHED_LEVELSET = 3,  /* level sets with one grid barrier per level */
-  SPTRSV_SCHED_LEVEL_CTA = 4  /* level sets inside one CTA (a CTA barrier per level, recent values in a
-                                 shared-memory window): deep DAGs with narrow levels, one rhs; other
-                                 requests on this schedule use SPTRSV_SCHED_LEVELSET */
+  SPTRSV_SCHED_LEVELSET = 3   /* level sets with one grid barrier per level */
 } sptrsv_schedule;
 
 /* Tunable options (sptrsv_gb300_set_option / get_option). */
