@@ -89,7 +89,13 @@ def executor(col_ptr, row_idx, val, in_degree, left_sum, m: int, substitution: i
 
 # ------------------------------------------------------------------ handle API
 class SyncFreeSolver:
-    """Analyse once, solve many: a handle of libsptrsv_gb300 bound to torch CUDA tensors."""
+    """Analyse once, solve many: a handle of libsptrsv_gb300 bound to torch CUDA tensors.
+
+    Keyword options map one to one onto ``SPTRSV_OPTION_*``; an option left at
+    None keeps the library default, which with the automatic schedule is the
+    plan chosen from the analysis (``info()`` reports the settings in effect).
+    ``batch=[(col_ptr, row_idx, n, substitution), ...]`` analyses independent
+    systems as one block-diagonal index space solved in one launch."""
 
     def __init__(self, col_ptr=None, row_idx=None, n: int | None = None, substitution: int = 0, *, values=None,
                  batch=None,
