@@ -48,6 +48,7 @@ struct sptrsv_gb300_handle_s {
   int fused_grad = 0;
   int wsync = 0;
   int split = 32;
+  int wsync_batch = 0;   // 0: automatic (2 for short lists, else 1)
   unsigned long long user_set = 0;  // options the caller set explicitly (bit = option id)
   // executor settings chosen from the analysis for SPTRSV_SCHED_AUTO (one rhs)
   struct AutoPlan {
@@ -700,6 +701,11 @@ ExecConfig pick_config(const sptrsv_gb300_handle_s* h, int rhs) {
   c.stages = h->stages_option;
   c.wsync = h->wsync;
   c.split = h->split;
+  // dependencies per lane per lockstep iteration: two when the average list is
+  // short (both usually land late: load them together), one otherwise (the
+  // shortest iteration; earlier entries of a ready-ordered list land early)
+  c.wsync_batch = h->wsync_batch > 0 ? h->wsync_batch
+                                     : ((long long)(h->nnz - h->n) <= 3LL * (long long)h->n ? 2 : 1);
   if (rhs == 1 && h->sched_option == SCHED_AUTO && h->plan.valid) {
     if (planned(h, SPTRSV_OPTION_CHUNK)) c.chunk = h->plan.chunk;
     if (planned(h, SPTRSV_OPTION_BLOCK)) c.block = h->plan.block;
@@ -949,6 +955,10 @@ static int set_option_value(sptrsv_handle_t h, int option, long long value) {
       if (value < 0 || (value > 0 && value < 4) || value > (1 << 20)) return SPTRSV_ERR_INVALID;
       h->split = static_cast<int>(value);
       return SPTRSV_OK;
+    case SPTRSV_OPTION_WSYNC_BATCH:
+      if (!(value == 0 || value == 1 || value == 2 || value == 4)) return SPTRSV_ERR_INVALID;
+      h->wsync_batch = static_cast<int>(value);
+      return SPTRSV_OK;
     default:
       return SPTRSV_ERR_INVALID;
   }
@@ -975,6 +985,7 @@ int sptrsv_gb300_get_option(sptrsv_handle_t h, int option, long long* value) {
     case SPTRSV_OPTION_FUSED_GRAD: *value = h->fused_grad; break;
     case SPTRSV_OPTION_WARP_SYNC: *value = h->wsync; break;
     case SPTRSV_OPTION_SPLIT: *value = h->split; break;
+    case SPTRSV_OPTION_WSYNC_BATCH: *value = h->wsync_batch; break;
     default: return SPTRSV_ERR_INVALID;
   }
   return SPTRSV_OK;
@@ -1559,7 +1570,7 @@ int sptrsv_gb300_tune(sptrsv_handle_t h, const void* d_val, int dtype, int rhs, 
   if (!h->analysed) return SPTRSV_ERR_STATE;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   struct Cand {
-    int sched, order_block, chunk, staged, backoff, ctas, lanes, stages, wsync, block, split;
+    int sched, order_block, chunk, staged, backoff, ctas, lanes, stages, wsync, block, split, batch = 0;
   };
   const int n = h->n;
   const int big = INT_MAX;
@@ -1572,7 +1583,9 @@ int sptrsv_gb300_tune(sptrsv_handle_t h, const void* d_val, int dtype, int rhs, 
     // blocked orders for deep narrow DAGs
     for (int ch : {128, 256}) cands.push_back({SCHED_PULL, big, ch, 0, 128, 1, 1, 2, 1, ch, sp});
     cands.push_back({SCHED_PULL, big, 256, 0, 128, 1, 1, 2, 1, 256, 0});
+    for (int bt : {1, 2, 4}) cands.push_back({SCHED_PULL, big, 256, 0, 128, 1, 1, 2, 1, 256, sp, bt});
     for (int ob : {2048, 8192, 22624}) cands.push_back({SCHED_PULL, ob, ob, 0, 0, 0, 1, 2, 1, 128, sp});
+    for (int bt : {1, 2, 4}) cands.push_back({SCHED_PULL, 22624, 22624, 0, 0, 0, 1, 2, 1, 128, sp, bt});
     // thread-per-unknown executor, level order
     cands.push_back({SCHED_PULL, big, 256, 0, 128, 1, 1, 2, 0, 256, sp});
     cands.push_back({SCHED_LEVELSET, big, 256, 0, 256, 1, 8, 2, 0, 256, sp});
@@ -1608,6 +1621,7 @@ int sptrsv_gb300_tune(sptrsv_handle_t h, const void* d_val, int dtype, int rhs, 
     h->wsync = c.wsync;
     h->block_option = c.block;
     h->split = c.split;
+    h->wsync_batch = c.batch;
     int st = sptrsv_gb300_solve(h, d_val, dtype, rhs, layout, d_b, d_x, stream);
     if (st == SPTRSV_OK) st = check_device(h, s);
     if (st != SPTRSV_OK) continue;  // a candidate that fails (or times out) is skipped
@@ -1647,6 +1661,7 @@ int sptrsv_gb300_tune(sptrsv_handle_t h, const void* d_val, int dtype, int rhs, 
   h->wsync = c.wsync;
   h->block_option = c.block;
   h->split = c.split;
+  h->wsync_batch = c.batch;
   ST_TRY(ensure_layout(h, s));
   ST_TRY(stage_values(h, d_val, dtype, s, false));
   if (best_ms) *best_ms = best;

@@ -202,11 +202,14 @@ __global__ void __launch_bounds__(256) k_pull_vec(ExecArgs<T> a) {
 // warp that it depends on waits to run, so a chain inside a warp (common in
 // blocked orders of narrow DAGs) costs one short iteration per hop. Global
 // waits back off only when no lane of the warp made progress.
-template <typename T, bool EXACT, bool ADJ>
+//
+// U = dependencies a lane loads per lockstep iteration. Small U keeps the
+// iteration short, which is what a hop costs once the last dependency lands;
+// ready-order lists let the earlier dependencies be consumed before that.
+template <typename T, bool EXACT, bool ADJ, int U>
 __global__ void __launch_bounds__(256) k_pull_wsync(ExecArgs<T> a) {
   using F = Flag<T>;
   using Bits = typename F::Bits;
-  constexpr int U = 4;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* s_x = reinterpret_cast<T*>(smem_raw);
   __shared__ unsigned s_chunk;
@@ -357,12 +360,11 @@ __global__ void __launch_bounds__(256) k_pull_wsync(ExecArgs<T> a) {
 // A 1000-entry list then takes about as many lockstep iterations as a
 // 30-entry one, and only its last slice waits on the latest dependencies.
 // Segments without a split list run the one-lane loop (SPLIT = false).
-template <typename T, bool ADJ, bool SPLIT>
+template <typename T, bool ADJ, bool SPLIT, int U>
 __device__ __forceinline__ bool wsync_segment(const ExecArgs<T>& a, T* s_x, int cbase, int walk, int row, int e,
                                               const int e1, unsigned at_or_below) {
   using F = Flag<T>;
   using Bits = typename F::Bits;
-  constexpr int U = 4;
   constexpr unsigned kFull = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const int* __restrict__ lpos = ADJ ? a.out_pos_f : a.dep_pos_f;
@@ -495,7 +497,7 @@ __device__ __forceinline__ bool wsync_segment(const ExecArgs<T>& a, T* s_x, int 
   }
 }
 
-template <typename T, bool ADJ>
+template <typename T, bool ADJ, int U>
 __global__ void __launch_bounds__(256) k_pull_wsync_split(ExecArgs<T> a) {
   using F = Flag<T>;
   using Bits = typename F::Bits;
@@ -530,8 +532,8 @@ __global__ void __launch_bounds__(256) k_pull_wsync_split(ExecArgs<T> a) {
       const int walk = n_walk, lo = n_lo, hi = n_hi, row = n_row;
       const bool split = n_split != 0;  // some unknown of the segment spans several lanes
       if (seg + nwarps < seg1) fetch(seg + nwarps);
-      fail = split ? wsync_segment<T, ADJ, true>(a, s_x, cbase, walk, row, lo, hi, at_or_below)
-                   : wsync_segment<T, ADJ, false>(a, s_x, cbase, walk, row, lo, hi, at_or_below);
+      fail = split ? wsync_segment<T, ADJ, true, U>(a, s_x, cbase, walk, row, lo, hi, at_or_below)
+                   : wsync_segment<T, ADJ, false, U>(a, s_x, cbase, walk, row, lo, hi, at_or_below);
     }
     if (__syncthreads_or(fail)) break;
   }
@@ -1100,10 +1102,18 @@ cudaError_t launch_pull_impl(ExecArgs<T>& a, int rhs, const ExecConfig& cfg, siz
                              cudaStream_t s) {
   const int block = cfg.block;
   if (rhs == 1 && cfg.wsync && !cfg.exact && a.grad == nullptr && a.pc_walk != nullptr)
-    return run(k_pull_wsync_split<T, ADJ>, a, block, smem, num_sms, s);
+    switch (cfg.wsync_batch) {
+      case 1: return run(k_pull_wsync_split<T, ADJ, 1>, a, block, smem, num_sms, s);
+      case 2: return run(k_pull_wsync_split<T, ADJ, 2>, a, block, smem, num_sms, s);
+      default: return run(k_pull_wsync_split<T, ADJ, 4>, a, block, smem, num_sms, s);
+    }
   if (rhs == 1 && cfg.wsync) {
-    if (cfg.exact) return run(k_pull_wsync<T, true, ADJ>, a, block, smem, num_sms, s);
-    return run(k_pull_wsync<T, false, ADJ>, a, block, smem, num_sms, s);
+    if (cfg.exact) return run(k_pull_wsync<T, true, ADJ, 4>, a, block, smem, num_sms, s);
+    switch (cfg.wsync_batch) {
+      case 1: return run(k_pull_wsync<T, false, ADJ, 1>, a, block, smem, num_sms, s);
+      case 2: return run(k_pull_wsync<T, false, ADJ, 2>, a, block, smem, num_sms, s);
+      default: return run(k_pull_wsync<T, false, ADJ, 4>, a, block, smem, num_sms, s);
+    }
   }
   if (rhs == 1) {
     if (cfg.exact) return run(k_pull_vec<T, 1, true, 4, ADJ>, a, block, smem, num_sms, s);

@@ -37,6 +37,7 @@ struct ExecConfig {
   int stages = 2;         // staged: chunk buffers in the producer/consumer ring
   int wsync = 0;          // unstaged one-rhs pull: warp-synchronous lanes (k_pull_wsync)
   int split = 0;          // warp-synchronous, fast arithmetic: split lists longer than this (0: never)
+  int wsync_batch = 4;    // warp-synchronous one rhs, fast arithmetic: dependencies per lane per iteration
 };
 
 // Work units of the staged executor: chunk k covers walk indices

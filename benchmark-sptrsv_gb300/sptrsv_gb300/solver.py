@@ -104,8 +104,8 @@ class SyncFreeSolver:
                  timeout_ms: int | None = None, sync_check: bool | None = None, profile: bool | None = None,
                  block: int | None = None, backoff_ns: int | None = None, ctas_per_sm: int | None = None,
                  staged: bool | None = None, stage_entries: int | None = None, stages: int | None = None,
-                 warp_sync: bool | None = None, split: int | None = None, fused_grad: bool | None = None,
-                 stream=None):
+                 warp_sync: bool | None = None, split: int | None = None, wsync_batch: int | None = None,
+                 fused_grad: bool | None = None, stream=None):
         torch = _torch()
         self._lib = load()
         self.device = torch.device("cuda", torch.cuda.current_device())
@@ -147,6 +147,7 @@ class SyncFreeSolver:
                        (_lib.OPTION_CTAS_PER_SM, ctas_per_sm), (_lib.OPTION_STAGED, staged),
                        (_lib.OPTION_STAGE_ENTRIES, stage_entries), (_lib.OPTION_STAGES, stages),
                        (_lib.OPTION_WARP_SYNC, warp_sync), (_lib.OPTION_SPLIT, split),
+                       (_lib.OPTION_WSYNC_BATCH, wsync_batch),
                        (_lib.OPTION_FUSED_GRAD, fused_grad)):
             if v is not None:
                 self.set_option(opt, int(v))
@@ -311,7 +312,7 @@ class SyncFreeSolver:
         return dval
 
     TUNED_OPTIONS = ("SCHEDULE", "ORDER_BLOCK", "CHUNK", "STAGED", "BACKOFF_NS", "CTAS_PER_SM", "LANES", "STAGES",
-                     "WARP_SYNC", "BLOCK", "SPLIT")
+                     "WARP_SYNC", "BLOCK", "SPLIT", "WSYNC_BATCH")
 
     def tune(self, b, values=None, reps: int = 3) -> dict:
         """Autotune the executor on this right-hand side; returns the chosen options and time."""

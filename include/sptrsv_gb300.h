@@ -100,9 +100,12 @@ typedef enum sptrsv_option {
                                      transposed solve, then one gradient pass over the stored pattern */
   SPTRSV_OPTION_WARP_SYNC = 16,   /* one-rhs pull without staging: 1 = the 32 lanes of a warp advance in
                                      lockstep (fast in-warp dependency chains; blocked orders) */
-  SPTRSV_OPTION_SPLIT = 17        /* warp-synchronous one-rhs pull (not exact): dependency lists longer
+  SPTRSV_OPTION_SPLIT = 17,       /* warp-synchronous one-rhs pull (not exact): dependency lists longer
                                      than this many entries are split over up to 32 lanes (default 32;
                                      0 = one lane per unknown) */
+  SPTRSV_OPTION_WSYNC_BATCH = 18  /* warp-synchronous one-rhs pull (not exact): dependencies a lane loads
+                                     per lockstep iteration, 1, 2 or 4 (0 = automatic: 2 when the lists
+                                     average <= 3 entries, else 1) */
 } sptrsv_option;
 
 typedef struct sptrsv_info {

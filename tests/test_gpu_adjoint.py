@@ -29,7 +29,10 @@ def relerr(x, ref):
                                  dict(staged=False, warp_sync=True, exact=True, order_block=64, chunk=64),
                                  dict(staged=False, warp_sync=True, order_block=128, chunk=128),
                                  dict(staged=False, warp_sync=True, split=4),
-                                 dict(staged=False, warp_sync=True, split=0)],
+                                 dict(staged=False, warp_sync=True, split=0),
+                                 dict(staged=False, warp_sync=True, split=4, wsync_batch=1),
+                                 dict(staged=False, warp_sync=True, split=0, wsync_batch=2, order_block=128,
+                                      chunk=128)],
                          ids=lambda c: "-".join(f"{k}{v}" for k, v in c.items()))
 def test_adjoint_and_gradient_vs_oracle(cuda, name, cfg):
     from oracle import oracle

@@ -105,6 +105,12 @@ def test_split_option_validated(cuda):
     for ok in (0, 4, 64):
         s.set_option(_lib.OPTION_SPLIT, ok)
         assert s.get_option(_lib.OPTION_SPLIT) == ok
+    for bad in (-1, 3, 8):
+        with pytest.raises(SptrsvError):
+            s.set_option(_lib.OPTION_WSYNC_BATCH, bad)
+    for ok in (0, 1, 2, 4):
+        s.set_option(_lib.OPTION_WSYNC_BATCH, ok)
+        assert s.get_option(_lib.OPTION_WSYNC_BATCH) == ok
 
 
 @pytest.mark.parametrize("cfg", [dict(schedule=2), dict(schedule=1)])
