@@ -701,11 +701,7 @@ ExecConfig pick_config(const sptrsv_gb300_handle_s* h, int rhs) {
   c.stages = h->stages_option;
   c.wsync = h->wsync;
   c.split = h->split;
-  // dependencies per lane per lockstep iteration: two when the average list is
-  // short (both usually land late: load them together), one otherwise (the
-  // shortest iteration; earlier entries of a ready-ordered list land early)
-  c.wsync_batch = h->wsync_batch > 0 ? h->wsync_batch
-                                     : ((long long)(h->nnz - h->n) <= 3LL * (long long)h->n ? 2 : 1);
+  c.wsync_batch = h->wsync_batch;  // 0: chosen per solve (solve_typed)
   if (rhs == 1 && h->sched_option == SCHED_AUTO && h->plan.valid) {
     if (planned(h, SPTRSV_OPTION_CHUNK)) c.chunk = h->plan.chunk;
     if (planned(h, SPTRSV_OPTION_BLOCK)) c.block = h->plan.block;
@@ -781,6 +777,15 @@ int solve_typed(sptrsv_gb300_handle_s* h, const Values<T>& V, int rhs, int layou
     if (rhs == 1 && c.wsync && !c.exact && c.split > 0 && longest > c.split && !(adj && adj->grad)) {
       ST_TRY(ensure_pieces(h, adj != nullptr, c.split, c.chunk, s));
       pc = adj ? &h->pc_adj : &h->pc_fwd;
+    }
+    if (c.wsync_batch == 0) {
+      // dependencies per lane per lockstep iteration (measured): one for forward
+      // walks over lists averaging more than 3 entries with one lane per unknown
+      // (the shortest iteration; the earlier entries of a ready-ordered list land
+      // early), two otherwise (short lists, whose entries land together, the
+      // split executor, and the transposed walk)
+      const bool long_avg = (long long)(h->nnz - h->n) > 3LL * (long long)h->n;
+      c.wsync_batch = (!adj && !pc && long_avg) ? 1 : 2;
     }
     CUDA_TRY(launch_pull<T>(h->layout, V, rhs, v, static_cast<T*>(h->xw.p), h->ctl, c, timeout_ns(h), h->num_sms,
                             s, adj, pc));
