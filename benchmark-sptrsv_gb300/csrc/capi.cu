@@ -53,7 +53,7 @@ struct sptrsv_gb300_handle_s {
   // executor settings chosen from the analysis for SPTRSV_SCHED_AUTO (one rhs)
   struct AutoPlan {
     bool valid = false;
-    int order_block = INT_MAX, chunk = 256, block = 256, ctas = 1, backoff = 128, staged = 0, wsync = 1;
+    int order_block = INT_MAX, chunk = 256, block = 256, ctas = 2, backoff = 0, staged = 0, wsync = 1;
     int split_fwd = 0, split_adj = 0;  // split length for the forward / transposed walk (0: none)
     double locality = 0.0;
   } plan;
@@ -1589,6 +1589,11 @@ int sptrsv_gb300_tune(sptrsv_handle_t h, const void* d_val, int dtype, int rhs, 
     for (int ch : {128, 256}) cands.push_back({SCHED_PULL, big, ch, 0, 128, 1, 1, 2, 1, ch, sp});
     cands.push_back({SCHED_PULL, big, 256, 0, 128, 1, 1, 2, 1, 256, 0});
     for (int bt : {1, 2, 4}) cands.push_back({SCHED_PULL, big, 256, 0, 128, 1, 1, 2, 1, 256, sp, bt});
+    for (int ct : {2, 3}) {
+      cands.push_back({SCHED_PULL, big, 256, 0, 0, ct, 1, 2, 1, 256, sp});
+      cands.push_back({SCHED_PULL, big, 256, 0, 0, ct, 1, 2, 1, 256, 0});
+      cands.push_back({SCHED_PULL, big, 128, 0, 0, ct, 1, 2, 1, 128, sp});
+    }
     for (int ob : {2048, 8192, 22624}) cands.push_back({SCHED_PULL, ob, ob, 0, 0, 0, 1, 2, 1, 128, sp});
     for (int bt : {1, 2, 4}) cands.push_back({SCHED_PULL, 22624, 22624, 0, 0, 0, 1, 2, 1, 128, sp, bt});
     // thread-per-unknown executor, level order
