@@ -457,27 +457,32 @@ cudaError_t launch_sort_lists(const int* ptr, const int* pos, const int* src, in
   unsigned *k1 = nullptr, *k2 = nullptr;
   int *v1 = nullptr, *v2 = nullptr;
   void* temp = nullptr;
-  cudaError_t err;
-  if ((err = cudaMallocAsync(reinterpret_cast<void**>(&k1), sizeof(unsigned) * count, s)) != cudaSuccess) return err;
-  if ((err = cudaMallocAsync(reinterpret_cast<void**>(&k2), sizeof(unsigned) * count, s)) != cudaSuccess) return err;
-  if ((err = cudaMallocAsync(reinterpret_cast<void**>(&v1), sizeof(int) * count, s)) != cudaSuccess) return err;
-  if ((err = cudaMallocAsync(reinterpret_cast<void**>(&v2), sizeof(int) * count, s)) != cudaSuccess) return err;
-  if ((err = cudaMallocAsync(&temp, radix_sort_temp_bytes(count), s)) != cudaSuccess) return err;
-  // entries by position of the dependency, then (stable) by owning position
-  k_rank_keys<<<grid_for(count), kThreads, 0, s>>>(pos, count, n, descending ? 1 : 0, k1);
-  if ((err = launch_iota(v1, count, 0, 1, s)) != cudaSuccess) return err;
-  if ((err = radix_sort_pairs(k1, v1, k2, v2, count, bits, temp, s)) != cudaSuccess) return err;
-  if ((err = launch_expand_cols(ptr, n, v1, s)) != cudaSuccess) return err;
-  k_owner_keys<<<grid_for(count), kThreads, 0, s>>>(v1, v2, count, k1);
-  if ((err = radix_sort_pairs(k1, v2, k2, v1, count, bits, temp, s)) != cudaSuccess) return err;
-  if ((err = launch_gather_int(pos, v1, pos_out, count, s)) != cudaSuccess) return err;
-  if ((err = launch_gather_int(src, v1, src_out, count, s)) != cudaSuccess) return err;
-  cudaFreeAsync(k1, s);
-  cudaFreeAsync(k2, s);
-  cudaFreeAsync(v1, s);
-  cudaFreeAsync(v2, s);
-  cudaFreeAsync(temp, s);
-  return cudaGetLastError();
+  auto run = [&]() -> cudaError_t {
+    cudaError_t err;
+    if ((err = cudaMallocAsync(reinterpret_cast<void**>(&k1), sizeof(unsigned) * count, s)) != cudaSuccess) return err;
+    if ((err = cudaMallocAsync(reinterpret_cast<void**>(&k2), sizeof(unsigned) * count, s)) != cudaSuccess) return err;
+    if ((err = cudaMallocAsync(reinterpret_cast<void**>(&v1), sizeof(int) * count, s)) != cudaSuccess) return err;
+    if ((err = cudaMallocAsync(reinterpret_cast<void**>(&v2), sizeof(int) * count, s)) != cudaSuccess) return err;
+    if ((err = cudaMallocAsync(&temp, radix_sort_temp_bytes(count), s)) != cudaSuccess) return err;
+    // entries by position of the dependency, then (stable) by owning position
+    k_rank_keys<<<grid_for(count), kThreads, 0, s>>>(pos, count, n, descending ? 1 : 0, k1);
+    if ((err = launch_iota(v1, count, 0, 1, s)) != cudaSuccess) return err;
+    if ((err = radix_sort_pairs(k1, v1, k2, v2, count, bits, temp, s)) != cudaSuccess) return err;
+    if ((err = launch_expand_cols(ptr, n, v1, s)) != cudaSuccess) return err;
+    k_owner_keys<<<grid_for(count), kThreads, 0, s>>>(v1, v2, count, k1);
+    if ((err = radix_sort_pairs(k1, v2, k2, v1, count, bits, temp, s)) != cudaSuccess) return err;
+    if ((err = launch_gather_int(pos, v1, pos_out, count, s)) != cudaSuccess) return err;
+    if ((err = launch_gather_int(src, v1, src_out, count, s)) != cudaSuccess) return err;
+    return cudaGetLastError();
+  };
+  const cudaError_t err = run();
+  // temporaries are released on every path (stream-ordered after their last use)
+  if (k1) cudaFreeAsync(k1, s);
+  if (k2) cudaFreeAsync(k2, s);
+  if (v1) cudaFreeAsync(v1, s);
+  if (v2) cudaFreeAsync(v2, s);
+  if (temp) cudaFreeAsync(temp, s);
+  return err;
 }
 
 // ------------------------------------------------------------ schedule heuristics
