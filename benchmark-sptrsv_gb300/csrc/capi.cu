@@ -87,6 +87,8 @@ struct sptrsv_gb300_handle_s {
   int max_dep_cnt = 0, max_out_cnt = 0;
   ChunkTable tab_fwd, tab_adj;
   PieceTable pc_fwd, pc_adj;
+  ImportTable imports;
+  int import_option = 1;   // importer warp on blocked layouts (SPTRSV_OPTION_IMPORT)
   // staged values
   Values<double> v64;
   Values<float> v32;
@@ -165,6 +167,13 @@ void free_pieces(PieceTable& t) {
   t = PieceTable();
 }
 
+void free_imports(ImportTable& t) {
+  if (t.ptr) cudaFree(t.ptr);
+  if (t.q) cudaFree(t.q);
+  if (t.dep_slot) cudaFree(t.dep_slot);
+  t = ImportTable();
+}
+
 void free_layout(Layout& L) {
   dev_free(&L.perm);
   dev_free(&L.iperm);
@@ -218,6 +227,7 @@ void free_analysis(sptrsv_gb300_handle_s* h) {
   free_table(h->tab_adj);
   free_pieces(h->pc_fwd);
   free_pieces(h->pc_adj);
+  free_imports(h->imports);
   free_values(h->v64);
   free_values(h->v32);
   h->staged64 = h->staged32 = false;
@@ -301,6 +311,7 @@ int build_layout(sptrsv_gb300_handle_s* h, int block, cudaStream_t s) {
   free_table(h->tab_adj);
   free_pieces(h->pc_fwd);
   free_pieces(h->pc_adj);
+  free_imports(h->imports);
   free_values(h->v64);
   free_values(h->v32);
   h->staged64 = h->staged32 = false;
@@ -550,6 +561,55 @@ int ensure_pieces(sptrsv_gb300_handle_s* h, bool adj, int split, int chunk, cuda
   return build_pieces(h, t, adj ? h->out_cnt_host : h->dep_cnt_host, adj, split, chunk, s);
 }
 
+// Import table of the forward walk for chunks of `chunk` positions (see
+// ImportTable). When a chunk's window and imports do not fit one CTA's shared
+// memory only the sizes are recorded (no device arrays; the caller checks).
+int build_imports(sptrsv_gb300_handle_s* h, int chunk, size_t elem, cudaStream_t s) {
+  free_imports(h->imports);
+  const Layout& L = h->layout;
+  const int n = L.n;
+  const int ndep = L.ndep;
+  std::vector<int> ptr((size_t)n + 1), pos(ndep > 0 ? (size_t)ndep : 1);
+  CUDA_TRY(cudaMemcpyAsync(ptr.data(), L.dep_ptr, sizeof(int) * ((size_t)n + 1), cudaMemcpyDeviceToHost, s));
+  if (ndep > 0)
+    CUDA_TRY(cudaMemcpyAsync(pos.data(), L.dep_pos_f, sizeof(int) * (size_t)ndep, cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  const int nchunks = (n + chunk - 1) / chunk;
+  std::vector<int> cptr((size_t)nchunks + 1, 0), q, slot(ndep > 0 ? (size_t)ndep : 1, -1), ext;
+  int max_imp = 0;
+  for (int c = 0; c < nchunks; ++c) {
+    const int base = c * chunk, end = std::min(n, base + chunk);
+    ext.clear();
+    for (int e = ptr[base]; e < ptr[end]; ++e)
+      if (pos[e] < base) ext.push_back(pos[e]);
+    std::sort(ext.begin(), ext.end());
+    ext.erase(std::unique(ext.begin(), ext.end()), ext.end());
+    for (int e = ptr[base]; e < ptr[end]; ++e) {
+      const int qe = pos[e];
+      slot[e] = qe >= base ? qe - base
+                           : chunk + static_cast<int>(std::lower_bound(ext.begin(), ext.end(), qe) - ext.begin());
+    }
+    q.insert(q.end(), ext.begin(), ext.end());
+    cptr[c + 1] = static_cast<int>(q.size());
+    max_imp = std::max(max_imp, static_cast<int>(ext.size()));
+  }
+  ImportTable& t = h->imports;
+  t.chunk = chunk;
+  t.max_imports = max_imp;
+  if (imported_smem_bytes(chunk, max_imp, elem) > 220 * 1024) return SPTRSV_OK;  // recorded: does not fit
+  CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.ptr), sizeof(int) * cptr.size()));
+  CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.q), sizeof(int) * (q.empty() ? 1 : q.size())));
+  CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.dep_slot), sizeof(int) * slot.size()));
+  CUDA_TRY(cudaMemcpy(t.ptr, cptr.data(), sizeof(int) * cptr.size(), cudaMemcpyHostToDevice));
+  if (!q.empty()) CUDA_TRY(cudaMemcpy(t.q, q.data(), sizeof(int) * q.size(), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(t.dep_slot, slot.data(), sizeof(int) * slot.size(), cudaMemcpyHostToDevice));
+  t.chunk = chunk;
+  t.nchunks = nchunks;
+  t.max_imports = max_imp;
+  h->device_bytes += sizeof(int) * (cptr.size() + q.size() + slot.size());
+  return SPTRSV_OK;
+}
+
 // Largest per-chunk entry budget whose ring of stage buffers (plus the
 // shared-memory tier) fits one CTA's shared memory; 0 if none does.
 constexpr size_t kSmemCap = 220 * 1024;
@@ -770,6 +830,17 @@ int solve_typed(sptrsv_gb300_handle_s* h, const Values<T>& V, int rhs, int layou
     ST_TRY(ensure_table(h, adj != nullptr, c.chunk, emax));
     CUDA_TRY(launch_pull_staged<T>(h->layout, V, adj ? h->tab_adj : h->tab_fwd, v, static_cast<T*>(h->xw.p), h->ctl,
                                    c, timeout_ns(h), h->num_sms, s, adj));
+  } else if (rhs == 1 && c.wsync && !c.exact && !adj && h->import_option && h->layout_block < n &&
+             c.chunk == h->layout_block && c.smem_tier &&
+             !(c.split > 0 && h->max_dep_cnt > c.split) &&
+             (h->imports.chunk == c.chunk || build_imports(h, c.chunk, sizeof(T), s) == SPTRSV_OK) &&
+             h->imports.ptr != nullptr &&
+             imported_smem_bytes(c.chunk, h->imports.max_imports, sizeof(T)) <= 220 * 1024) {
+    // blocked layout: an importer warp per CTA brings the chunk's external dependencies
+    // into shared memory
+    if (c.wsync_batch == 0) c.wsync_batch = (long long)(h->nnz - h->n) > 3LL * (long long)h->n ? 1 : 2;
+    CUDA_TRY(launch_pull_imported<T>(h->layout, V, v, static_cast<T*>(h->xw.p), h->ctl, c, timeout_ns(h),
+                                     h->num_sms, s, h->imports));
   } else {
     const PieceTable* pc = nullptr;
     if (rhs == 1 && planned(h, SPTRSV_OPTION_SPLIT)) c.split = adj ? h->plan.split_adj : h->plan.split_fwd;
@@ -964,6 +1035,9 @@ static int set_option_value(sptrsv_handle_t h, int option, long long value) {
       if (!(value == 0 || value == 1 || value == 2 || value == 4)) return SPTRSV_ERR_INVALID;
       h->wsync_batch = static_cast<int>(value);
       return SPTRSV_OK;
+    case SPTRSV_OPTION_IMPORT:
+      h->import_option = value != 0;
+      return SPTRSV_OK;
     default:
       return SPTRSV_ERR_INVALID;
   }
@@ -991,6 +1065,7 @@ int sptrsv_gb300_get_option(sptrsv_handle_t h, int option, long long* value) {
     case SPTRSV_OPTION_WARP_SYNC: *value = h->wsync; break;
     case SPTRSV_OPTION_SPLIT: *value = h->split; break;
     case SPTRSV_OPTION_WSYNC_BATCH: *value = h->wsync_batch; break;
+    case SPTRSV_OPTION_IMPORT: *value = h->import_option; break;
     default: return SPTRSV_ERR_INVALID;
   }
   return SPTRSV_OK;

@@ -74,6 +74,13 @@ struct ExecArgs {
   const int* pc_cseg;
   const int* pc_cbase;
   const unsigned char* pc_split;  // per segment: 1 if an unknown spans several lanes
+  // imported dependencies (k_pull_wsync_imp): chunk c needs the positions
+  // im_q[im_ptr[c] .. im_ptr[c+1]) from other chunks; dep_slot[e] is the
+  // shared-memory slot of dependency e (in-chunk: position - chunk base;
+  // imported: chunk + import index)
+  const int* im_ptr;
+  const int* im_q;
+  const int* dep_slot;
 };
 
 template <typename T>
@@ -343,6 +350,152 @@ __global__ void __launch_bounds__(256) k_pull_wsync(ExecArgs<T> a) {
           }
         } else {
           nap = a.sleep_min;
+        }
+      }
+    }
+    if (__syncthreads_or(fail)) break;
+  }
+  leave(a.ctl);
+}
+
+// ------------------------------------------------------------------ pull, warp-synchronous, imported dependencies
+// Blocked orders put most of a chunk's dependencies inside the chunk; the few
+// that come from other chunks would make every lockstep iteration of the
+// warps that hold them wait for an L2 round trip. Here one extra warp per CTA
+// imports them: it polls the chunk's external positions (sorted, so roughly
+// in the order they are published) from global memory and copies each value
+// into a shared-memory slot as it lands. The consumer warps then resolve every
+// dependency in shared memory (slot from dep_slot), so their iterations stay
+// short. Fast arithmetic, one rhs, forward walks.
+template <typename T, int U>
+__global__ void __launch_bounds__(288) k_pull_wsync_imp(ExecArgs<T> a) {
+  using F = Flag<T>;
+  using Bits = typename F::Bits;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* s_x = reinterpret_cast<T*>(smem_raw);
+  __shared__ unsigned s_chunk;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int ncw = (blockDim.x >> 5) - 1;  // consumer warps; warp ncw imports
+  const int* __restrict__ lpos = a.dep_pos_f;
+  const T* __restrict__ vals = a.dep_w;
+  for (;;) {
+    const unsigned c = next_chunk(a.ctl, a.nchunks, &s_chunk);
+    if (c >= (unsigned)a.nchunks) break;
+    const int base = static_cast<int>(c) * a.chunk;
+    const int len = min(base + a.chunk, a.n) - base;
+    const int i0 = a.im_ptr[c], nimp = a.im_ptr[c + 1] - i0;
+    for (int i = threadIdx.x; i < len; i += blockDim.x) *reinterpret_cast<Bits*>(&s_x[i]) = F::EMPTY;
+    for (int i = threadIdx.x; i < nimp; i += blockDim.x) *reinterpret_cast<Bits*>(&s_x[a.chunk + i]) = F::EMPTY;
+    __syncthreads();
+    bool fail = false;
+    if (warp == ncw) {
+      // importer: each lane walks its imports in order, one poll at a time
+      WaitBudget wb(a.timeout_ns);
+      unsigned idle = 0u;
+      int i = lane;
+      Bits v = F::EMPTY;
+      if (i < nimp) v = F::load(&a.xw[a.im_q[i0 + i]]);
+      for (;;) {
+        bool progress = false;
+        if (i < nimp) {
+          if (v != F::EMPTY) {
+            F::store_shared(&s_x[a.chunk + i], F::value(v));
+            i += 32;
+            v = i < nimp ? F::load(&a.xw[a.im_q[i0 + i]]) : F::EMPTY;
+            progress = true;
+          } else {
+            v = F::load(&a.xw[a.im_q[i0 + i]]);
+          }
+        }
+        if (__all_sync(0xffffffffu, i >= nimp)) break;
+        if (!__any_sync(0xffffffffu, progress) && ((++idle & 15u) == 0u)) {
+          if (__any_sync(0xffffffffu, !wb.poll(a.ctl, base))) {
+            fail = true;
+            break;
+          }
+        }
+      }
+    } else {
+      int n_row = 0, n_e = 0, n_e1 = 0;
+      auto fetch = [&](int sg) {
+        const int jj = sg * 32 + lane;
+        if (jj < len) {
+          n_row = a.perm[base + jj];
+          n_e = a.dep_ptr[base + jj];
+          n_e1 = a.dep_ptr[base + jj + 1];
+        }
+      };
+      if (warp * 32 < len) fetch(warp);
+      for (int seg = warp; seg * 32 < len && !fail; seg += ncw) {
+        const int j = seg * 32 + lane;
+        bool done = j >= len;
+        const int p = base + j;
+        const int row = n_row;
+        int e = n_e;
+        const int e1 = n_e1;
+        if ((seg + ncw) * 32 < len) fetch(seg + ncw);
+        T acc = T(0);
+        if (!done) acc = a.b[(long long)row * a.b_si] * a.rcp[p];
+        int ls[U];
+        T w[U];
+        Bits bits[U];
+        unsigned todo = 0u;
+        auto load_batch = [&]() {
+          todo = 0u;
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            const int ee = e + u;
+            ls[u] = ee < e1 ? a.dep_slot[ee] : -1;
+            w[u] = ee < e1 ? vals[ee] : T(0);
+          }
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            bits[u] = F::EMPTY;
+            if (ls[u] >= 0) {
+              bits[u] = F::load_shared(&s_x[ls[u]]);
+              todo |= 1u << u;
+            }
+          }
+        };
+        if (!done) load_batch();
+        WaitBudget wb(a.timeout_ns);
+        unsigned idle = 0u;
+        for (;;) {
+          bool progress = false;
+          if (!done) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+              if (!(todo & (1u << u))) continue;
+              if (bits[u] != F::EMPTY) {
+                acc = fma(-w[u], F::value(bits[u]), acc);
+                todo &= ~(1u << u);
+                progress = true;
+              }
+            }
+            if (!todo) {
+              e += U;
+              if (e < e1) {
+                load_batch();
+              } else {
+                F::store_shared(&s_x[j], acc);
+                F::store(&a.xw[p], acc);
+                a.x[(long long)row * a.x_si] = acc;
+                done = true;
+              }
+              progress = true;
+            } else {
+#pragma unroll
+              for (int u = 0; u < U; ++u)
+                if ((todo & (1u << u)) && bits[u] == F::EMPTY) bits[u] = F::load_shared(&s_x[ls[u]]);
+            }
+          }
+          if (__all_sync(0xffffffffu, done)) break;
+          if (!__any_sync(0xffffffffu, progress) && ((++idle & 255u) == 0u)) {
+            if (__any_sync(0xffffffffu, !wb.poll(a.ctl, p))) {
+              fail = true;
+              break;
+            }
+          }
         }
       }
     }
@@ -1150,6 +1303,33 @@ cudaError_t launch_pull_impl(ExecArgs<T>& a, int rhs, const ExecConfig& cfg, siz
 }
 
 template <typename T>
+cudaError_t launch_pull_imported(const Layout& L, const Values<T>& V, const VecView<T>& v, T* xw, DeviceCtl* ctl,
+                                 const ExecConfig& cfg, unsigned long long timeout_ns, int num_sms, cudaStream_t s,
+                                 const ImportTable& im) {
+  if (L.n == 0) return cudaSuccess;
+  ExecArgs<T> a = make_args<T>(L, V, 1, v, im.chunk);
+  a.xw = xw;
+  a.ctl = ctl;
+  a.timeout_ns = timeout_ns;
+  a.ctas_per_sm = cfg.ctas_per_sm;
+  a.im_ptr = im.ptr;
+  a.im_q = im.q;
+  a.dep_slot = im.dep_slot;
+  a.nchunks = im.nchunks;
+  const size_t smem = (size_t)(im.chunk + im.max_imports) * sizeof(T);
+  const int block = cfg.block + 32;
+  switch (cfg.wsync_batch) {
+    case 1: return run(k_pull_wsync_imp<T, 1>, a, block, smem, num_sms, s);
+    case 4: return run(k_pull_wsync_imp<T, 4>, a, block, smem, num_sms, s);
+    default: return run(k_pull_wsync_imp<T, 2>, a, block, smem, num_sms, s);
+  }
+}
+
+size_t imported_smem_bytes(int chunk, int max_imports, size_t elem) {
+  return (size_t)(chunk + max_imports) * elem;
+}
+
+template <typename T>
 cudaError_t launch_pull(const Layout& L, const Values<T>& V, int rhs, const VecView<T>& v, T* xw, DeviceCtl* ctl,
                         const ExecConfig& cfg, unsigned long long timeout_ns, int num_sms, cudaStream_t s,
                         const AdjointArgs<T>* adj, const PieceTable* pc) {
@@ -1376,6 +1556,9 @@ cudaError_t launch_ref_executor(const int* col_ptr, const int* row_idx, const T*
   template cudaError_t launch_pull<T>(const Layout&, const Values<T>&, int, const VecView<T>&, T*, DeviceCtl*,   \
                                       const ExecConfig&, unsigned long long, int, cudaStream_t,                  \
                                       const AdjointArgs<T>*, const PieceTable*);                                 \
+  template cudaError_t launch_pull_imported<T>(const Layout&, const Values<T>&, const VecView<T>&, T*,           \
+                                               DeviceCtl*, const ExecConfig&, unsigned long long, int,           \
+                                               cudaStream_t, const ImportTable&);                                \
   template cudaError_t launch_push<T>(const Layout&, const Values<T>&, int, const VecView<T>&, T*, unsigned*,    \
                                       DeviceCtl*, const ExecConfig&, unsigned long long, int, cudaStream_t);     \
   template cudaError_t launch_levelset<T>(const Layout&, const Values<T>&, int, const VecView<T>&, T*,           \

@@ -68,6 +68,17 @@ struct PieceTable {
   unsigned char* seg_split = nullptr;  // device [nseg] 1 if an unknown of the segment spans several lanes
 };
 
+// Imported dependencies of a forward walk in chunks of `chunk` positions: chunk
+// c reads the positions q[ptr[c] .. ptr[c+1]) (sorted) from other chunks;
+// dep_slot[e] = shared-memory slot of dependency e (in-chunk: its position
+// minus the chunk base; imported: chunk + its index in the chunk's list).
+struct ImportTable {
+  int chunk = 0, nchunks = 0, max_imports = 0;
+  int* ptr = nullptr;       // device [nchunks+1]
+  int* q = nullptr;         // device [total imports]
+  int* dep_slot = nullptr;  // device [ndep]
+};
+
 // Solve-time description of one right-hand-side block. Element (i, k) of b
 // (x) lives at i*si + k*sk.
 template <typename T>
@@ -202,6 +213,12 @@ cudaError_t launch_levelset(const Layout& L, const Values<T>& V, int rhs, const 
                             DeviceCtl* ctl, const ExecConfig& cfg, unsigned long long timeout_ns,
                             cudaStream_t s);
 size_t pull_smem_bytes(int chunk, int rhs, size_t elem);
+size_t imported_smem_bytes(int chunk, int max_imports, size_t elem);
+// warp-synchronous one-rhs forward pull with an importer warp per CTA (blocked layouts)
+template <typename T>
+cudaError_t launch_pull_imported(const Layout& L, const Values<T>& V, const VecView<T>& v, T* xw, DeviceCtl* ctl,
+                                 const ExecConfig& cfg, unsigned long long timeout_ns, int num_sms, cudaStream_t s,
+                                 const ImportTable& im);
 size_t staged_smem_bytes(int cmax, int emax, size_t elem, bool smem_tier, int stages);
 template <typename T>
 cudaError_t launch_pull_staged(const Layout& L, const Values<T>& V, const ChunkTable& tab, const VecView<T>& v, T* xw,

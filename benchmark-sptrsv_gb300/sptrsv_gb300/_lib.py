@@ -60,6 +60,7 @@ OPTION_FUSED_GRAD = 15
 OPTION_WARP_SYNC = 16
 OPTION_SPLIT = 17
 OPTION_WSYNC_BATCH = 18
+OPTION_IMPORT = 19
 
 NOALLOC_MAX_N = 262144  # SPTRSV_NOALLOC_MAX_N
 

@@ -103,9 +103,12 @@ typedef enum sptrsv_option {
   SPTRSV_OPTION_SPLIT = 17,       /* warp-synchronous one-rhs pull (not exact): dependency lists longer
                                      than this many entries are split over up to 32 lanes (default 32;
                                      0 = one lane per unknown) */
-  SPTRSV_OPTION_WSYNC_BATCH = 18  /* warp-synchronous one-rhs pull (not exact): dependencies a lane loads
+  SPTRSV_OPTION_WSYNC_BATCH = 18, /* warp-synchronous one-rhs pull (not exact): dependencies a lane loads
                                      per lockstep iteration, 1, 2 or 4 (0 = automatic: 2 when the lists
                                      average <= 3 entries, else 1) */
+  SPTRSV_OPTION_IMPORT = 19       /* 1 (default): warp-synchronous one-rhs forward pull on a blocked
+                                     layout (chunk = order block) gives each CTA an importer warp that
+                                     copies the chunk's external dependencies into shared memory */
 } sptrsv_option;
 
 typedef struct sptrsv_info {

@@ -63,6 +63,9 @@ CONFIGS = [
     dict(schedule=2, staged=False, warp_sync=True, wsync_batch=2, order_block=64, chunk=64),
     dict(schedule=2, staged=False, warp_sync=True, wsync_batch=1, split=4),
     dict(schedule=2, staged=False, warp_sync=True, wsync_batch=2, split=5, chunk=32, smem_tier=False),
+    dict(schedule=2, staged=False, warp_sync=True, order_block=64, chunk=64, block=64, import_deps=False),
+    dict(schedule=2, staged=False, warp_sync=True, order_block=96, chunk=96, block=64, wsync_batch=1),
+    dict(schedule=2, staged=False, warp_sync=True, order_block=200, chunk=200, block=128, wsync_batch=4),
     dict(schedule=3, lanes=1),
     dict(schedule=3, lanes=8),
 ]
