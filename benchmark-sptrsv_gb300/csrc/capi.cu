@@ -82,6 +82,7 @@ struct sptrsv_gb300_handle_s {
   int* level_ptr_nat = nullptr;
   Layout layout;
   int layout_block = -1;
+  std::vector<int> layout_units;   // blocked layouts: start positions of the units (+ n), else empty
   std::vector<int> dep_cnt_host;   // dependencies per position
   std::vector<int> out_cnt_host;   // dependents per position
   int max_dep_cnt = 0, max_out_cnt = 0;
@@ -168,6 +169,7 @@ void free_pieces(PieceTable& t) {
 }
 
 void free_imports(ImportTable& t) {
+  if (t.start) cudaFree(t.start);
   if (t.ptr) cudaFree(t.ptr);
   if (t.q) cudaFree(t.q);
   if (t.dep_slot) cudaFree(t.dep_slot);
@@ -336,6 +338,7 @@ int build_layout(sptrsv_gb300_handle_s* h, int block, cudaStream_t s) {
   ST_TRY(dev_alloc(h, &L.diag_src, n));
 
   const bool level_order = block >= n;
+  h->layout_units.clear();
   if (n > 0) {
     // natural order rows
     int* rows_nat = nullptr;
@@ -370,6 +373,15 @@ int build_layout(sptrsv_gb300_handle_s* h, int block, cudaStream_t s) {
         const long long max_key = (long long)((max_sys - 1) / block + 1) * h->batch_count;
         if (max_key > 0xFFFFFFFFLL) return SPTRSV_ERR_UNSUPPORTED;
         CUDA_TRY(radix_sort_pairs(keys, rows_lv, keys_sorted, L.perm, n, bits_for(max_key - 1), temp, s));
+        // units of the blocked order (one system's natural block): contiguous
+        // position ranges, the work units of the importer executor
+        std::vector<unsigned> ks(n);
+        CUDA_TRY(cudaMemcpyAsync(ks.data(), keys_sorted, sizeof(unsigned) * (size_t)n, cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(cudaStreamSynchronize(s));
+        h->layout_units.clear();
+        for (int i = 0; i < n; ++i)
+          if (i == 0 || ks[i] != ks[i - 1]) h->layout_units.push_back(i);
+        h->layout_units.push_back(n);
       }
       CUDA_TRY(cudaFreeAsync(keys, s));
       CUDA_TRY(cudaFreeAsync(keys_sorted, s));
@@ -574,11 +586,19 @@ int build_imports(sptrsv_gb300_handle_s* h, int chunk, size_t elem, cudaStream_t
   if (ndep > 0)
     CUDA_TRY(cudaMemcpyAsync(pos.data(), L.dep_pos_f, sizeof(int) * (size_t)ndep, cudaMemcpyDeviceToHost, s));
   CUDA_TRY(cudaStreamSynchronize(s));
-  const int nchunks = (n + chunk - 1) / chunk;
+  // work units: the blocked layout's units (one system's natural block), or
+  // consecutive ranges of `chunk` positions
+  std::vector<int> starts = h->layout_units;
+  if (starts.empty())
+    for (int b = 0; b <= n; b += chunk) starts.push_back(std::min(b, n));
+  if (starts.back() != n) starts.push_back(n);
+  const int nchunks = static_cast<int>(starts.size()) - 1;
+  int width = 1;  // shared-memory window: the longest unit
+  for (int c = 0; c < nchunks; ++c) width = std::max(width, starts[c + 1] - starts[c]);
   std::vector<int> cptr((size_t)nchunks + 1, 0), q, slot(ndep > 0 ? (size_t)ndep : 1, -1), ext;
   int max_imp = 0;
   for (int c = 0; c < nchunks; ++c) {
-    const int base = c * chunk, end = std::min(n, base + chunk);
+    const int base = starts[c], end = starts[c + 1];
     ext.clear();
     for (int e = ptr[base]; e < ptr[end]; ++e)
       if (pos[e] < base) ext.push_back(pos[e]);
@@ -587,7 +607,7 @@ int build_imports(sptrsv_gb300_handle_s* h, int chunk, size_t elem, cudaStream_t
     for (int e = ptr[base]; e < ptr[end]; ++e) {
       const int qe = pos[e];
       slot[e] = qe >= base ? qe - base
-                           : chunk + static_cast<int>(std::lower_bound(ext.begin(), ext.end(), qe) - ext.begin());
+                           : width + static_cast<int>(std::lower_bound(ext.begin(), ext.end(), qe) - ext.begin());
     }
     q.insert(q.end(), ext.begin(), ext.end());
     cptr[c + 1] = static_cast<int>(q.size());
@@ -595,8 +615,11 @@ int build_imports(sptrsv_gb300_handle_s* h, int chunk, size_t elem, cudaStream_t
   }
   ImportTable& t = h->imports;
   t.chunk = chunk;
+  t.width = width;
   t.max_imports = max_imp;
-  if (imported_smem_bytes(chunk, max_imp, elem) > 220 * 1024) return SPTRSV_OK;  // recorded: does not fit
+  if (imported_smem_bytes(width, max_imp, elem) > 220 * 1024) return SPTRSV_OK;  // recorded: does not fit
+  CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.start), sizeof(int) * starts.size()));
+  CUDA_TRY(cudaMemcpy(t.start, starts.data(), sizeof(int) * starts.size(), cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.ptr), sizeof(int) * cptr.size()));
   CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.q), sizeof(int) * (q.empty() ? 1 : q.size())));
   CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.dep_slot), sizeof(int) * slot.size()));
@@ -606,7 +629,7 @@ int build_imports(sptrsv_gb300_handle_s* h, int chunk, size_t elem, cudaStream_t
   t.chunk = chunk;
   t.nchunks = nchunks;
   t.max_imports = max_imp;
-  h->device_bytes += sizeof(int) * (cptr.size() + q.size() + slot.size());
+  h->device_bytes += sizeof(int) * (starts.size() + cptr.size() + q.size() + slot.size());
   return SPTRSV_OK;
 }
 
@@ -835,7 +858,7 @@ int solve_typed(sptrsv_gb300_handle_s* h, const Values<T>& V, int rhs, int layou
              !(c.split > 0 && h->max_dep_cnt > c.split) &&
              (h->imports.chunk == c.chunk || build_imports(h, c.chunk, sizeof(T), s) == SPTRSV_OK) &&
              h->imports.ptr != nullptr &&
-             imported_smem_bytes(c.chunk, h->imports.max_imports, sizeof(T)) <= 220 * 1024) {
+             imported_smem_bytes(h->imports.width, h->imports.max_imports, sizeof(T)) <= 220 * 1024) {
     // blocked layout: an importer warp per CTA brings the chunk's external dependencies
     // into shared memory
     if (c.wsync_batch == 0) c.wsync_batch = (long long)(h->nnz - h->n) > 3LL * (long long)h->n ? 1 : 2;

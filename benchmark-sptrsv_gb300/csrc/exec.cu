@@ -78,6 +78,7 @@ struct ExecArgs {
   // im_q[im_ptr[c] .. im_ptr[c+1]) from other chunks; dep_slot[e] is the
   // shared-memory slot of dependency e (in-chunk: position - chunk base;
   // imported: chunk + import index)
+  const int* im_start;
   const int* im_ptr;
   const int* im_q;
   const int* dep_slot;
@@ -381,8 +382,8 @@ __global__ void __launch_bounds__(288) k_pull_wsync_imp(ExecArgs<T> a) {
   for (;;) {
     const unsigned c = next_chunk(a.ctl, a.nchunks, &s_chunk);
     if (c >= (unsigned)a.nchunks) break;
-    const int base = static_cast<int>(c) * a.chunk;
-    const int len = min(base + a.chunk, a.n) - base;
+    const int base = a.im_start[c];
+    const int len = a.im_start[c + 1] - base;  // <= a.chunk (the window)
     const int i0 = a.im_ptr[c], nimp = a.im_ptr[c + 1] - i0;
     for (int i = threadIdx.x; i < len; i += blockDim.x) *reinterpret_cast<Bits*>(&s_x[i]) = F::EMPTY;
     for (int i = threadIdx.x; i < nimp; i += blockDim.x) *reinterpret_cast<Bits*>(&s_x[a.chunk + i]) = F::EMPTY;
@@ -1307,16 +1308,17 @@ cudaError_t launch_pull_imported(const Layout& L, const Values<T>& V, const VecV
                                  const ExecConfig& cfg, unsigned long long timeout_ns, int num_sms, cudaStream_t s,
                                  const ImportTable& im) {
   if (L.n == 0) return cudaSuccess;
-  ExecArgs<T> a = make_args<T>(L, V, 1, v, im.chunk);
+  ExecArgs<T> a = make_args<T>(L, V, 1, v, im.width);
   a.xw = xw;
   a.ctl = ctl;
   a.timeout_ns = timeout_ns;
   a.ctas_per_sm = cfg.ctas_per_sm;
+  a.im_start = im.start;
   a.im_ptr = im.ptr;
   a.im_q = im.q;
   a.dep_slot = im.dep_slot;
   a.nchunks = im.nchunks;
-  const size_t smem = (size_t)(im.chunk + im.max_imports) * sizeof(T);
+  const size_t smem = (size_t)(im.width + im.max_imports) * sizeof(T);
   const int block = cfg.block + 32;
   switch (cfg.wsync_batch) {
     case 1: return run(k_pull_wsync_imp<T, 1>, a, block, smem, num_sms, s);

@@ -68,12 +68,15 @@ struct PieceTable {
   unsigned char* seg_split = nullptr;  // device [nseg] 1 if an unknown of the segment spans several lanes
 };
 
-// Imported dependencies of a forward walk in chunks of `chunk` positions: chunk
-// c reads the positions q[ptr[c] .. ptr[c+1]) (sorted) from other chunks;
-// dep_slot[e] = shared-memory slot of dependency e (in-chunk: its position
-// minus the chunk base; imported: chunk + its index in the chunk's list).
+// Imported dependencies of a forward walk in work units (the units of a
+// blocked layout, else ranges of `chunk` positions): unit c covers positions
+// [start[c], start[c+1]) and reads the positions q[ptr[c] .. ptr[c+1])
+// (sorted) from other units; dep_slot[e] = shared-memory slot of dependency e
+// (in-unit: its position minus the unit start; imported: width + its index in
+// the unit's list, width = the longest unit).
 struct ImportTable {
-  int chunk = 0, nchunks = 0, max_imports = 0;
+  int chunk = 0, nchunks = 0, width = 0, max_imports = 0;
+  int* start = nullptr;     // device [nchunks+1]
   int* ptr = nullptr;       // device [nchunks+1]
   int* q = nullptr;         // device [total imports]
   int* dep_slot = nullptr;  // device [ndep]

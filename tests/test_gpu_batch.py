@@ -37,7 +37,11 @@ def _solver(systems, **kw):
                                  dict(chunk=40, stage_entries=40, stages=3),
                                  dict(staged=False, warp_sync=True), dict(staged=False, warp_sync=True,
                                                                           order_block=256, chunk=256),
-                                 dict(staged=False, warp_sync=True, split=4)],
+                                 dict(staged=False, warp_sync=True, split=4),
+                                 dict(staged=False, warp_sync=True, order_block=512, chunk=512, block=64,
+                                      import_deps=True),
+                                 dict(staged=False, warp_sync=True, order_block=100, chunk=100, block=128,
+                                      wsync_batch=1)],
                          ids=lambda c: "-".join(f"{k}{v}" for k, v in c.items()) or "default")
 @pytest.mark.parametrize("rhs", [1, 4])
 def test_batch_matches_per_system_oracle(cuda, oracle_port, systems, cfg, rhs):
