@@ -113,7 +113,9 @@ def test_split_option_validated(cuda):
         assert s.get_option(_lib.OPTION_WSYNC_BATCH) == ok
 
 
-@pytest.mark.parametrize("cfg", [dict(schedule=2), dict(schedule=1)])
+@pytest.mark.parametrize("cfg", [dict(schedule=2), dict(schedule=1),
+                                 dict(schedule=2, staged=False, warp_sync=True, import_deps=True,
+                                      order_block=64)])
 def test_wait_budget_expires_cleanly_then_recovers(cuda, cfg):
     """Natural order on the 2-D Laplacian makes single waits last far longer than
     a 1 ms budget: the solve must come back with SPTRSV_ERR_TIMEOUT (every wait
@@ -122,8 +124,9 @@ def test_wait_budget_expires_cleanly_then_recovers(cuda, cfg):
     from sptrsv_gb300 import SptrsvError, SyncFreeSolver, _lib, matgen
     m = matgen.laplace2d_lower(1000)
     b = cuda.from_numpy(m.matvec(np.ones(m.n))).cuda()
-    s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, values=m.val, order_block=1, chunk=64,
-                       timeout_ms=1, **cfg)
+    kw = dict(order_block=1, chunk=64, timeout_ms=1)
+    kw.update(cfg)
+    s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, values=m.val, **kw)
     with pytest.raises(SptrsvError) as ei:
         s.solve(b)
     assert ei.value.status == _lib.ERR_TIMEOUT
