@@ -479,7 +479,9 @@ int ensure_table(sptrsv_gb300_handle_s* h, bool adj, int cmax, int emax) {
 }
 
 // Piece table over a walk (see PieceTable): lists longer than `split` entries
-// are cut into min(32, ceil(len/split)) near-equal consecutive slices.
+// are cut into k = min(32, ceil(len/split)) interleaved slices (piece j takes
+// entries j, j+k, j+2k, ... of the ready-ordered list), so the latest entries
+// spread over all the pieces instead of piling up in the last one.
 int build_pieces(sptrsv_gb300_handle_s* h, PieceTable& t, const std::vector<int>& counts, bool reversed, int split,
                  int chunk, cudaStream_t s) {
   free_pieces(t);
@@ -522,10 +524,10 @@ int build_pieces(sptrsv_gb300_handle_s* h, PieceTable& t, const std::vector<int>
       if (seg_split_host.size() <= sg) seg_split_host.resize(sg + 1, 0);
       seg_split_host[sg] = 1;
     }
-    for (int j = 0; j < k; ++j) {
+    for (int j = 0; j < k; ++j) {  // piece j: entries e0 + j, e0 + j + k, ... (interleaved)
       walk.push_back(i);
-      lo.push_back(static_cast<int>(e0 + c * j / k));
-      hi.push_back(static_cast<int>(e0 + c * (j + 1) / k));
+      lo.push_back(static_cast<int>(e0 + j));
+      hi.push_back(static_cast<int>(e0 + c));
     }
   }
   pad();

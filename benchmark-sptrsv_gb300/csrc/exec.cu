@@ -528,6 +528,7 @@ __device__ __forceinline__ bool wsync_segment(const ExecArgs<T>& a, T* s_x, int 
   bool head = valid;
   int ge = lane, gs = lane;
   unsigned gmask = 0u;
+  int step = 1;  // entries of an unknown split over k lanes interleave: lane j takes j, j+k, j+2k, ...
   if (SPLIT) {
     const int prev = __shfl_up_sync(kFull, walk, 1);
     head = valid && (lane == 0 || prev != walk);
@@ -539,6 +540,7 @@ __device__ __forceinline__ bool wsync_segment(const ExecArgs<T>& a, T* s_x, int 
     gs = valid ? 31 - __clz(heads & at_or_below) : lane;
     // head lanes: the lanes of their unknown (ge >= lane >= 0 there)
     gmask = head ? (ge >= 31 ? kFull : ((2u << ge) - 1u)) & ~((1u << lane) - 1u) : 0u;
+    step = valid ? ge - gs + 1 : 1;
   }
   const int p = ADJ ? last - walk : walk;
   T acc = T(0);
@@ -560,7 +562,7 @@ __device__ __forceinline__ bool wsync_segment(const ExecArgs<T>& a, T* s_x, int 
     todo = 0u;
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-      const int ee = e + u;
+      const int ee = e + u * (SPLIT ? step : 1);
       q[u] = ee < e1 ? lpos[ee] : -1;
       w[u] = ee < e1 ? vals[ee] : T(0);
     }
@@ -595,7 +597,7 @@ __device__ __forceinline__ bool wsync_segment(const ExecArgs<T>& a, T* s_x, int 
         }
       }
       if (!todo) {
-        e += U;
+        e += U * (SPLIT ? step : 1);
         if (e < e1) {
           load_batch();
         } else {

@@ -52,7 +52,9 @@ struct ChunkTable {
 };
 
 // Work units of the split-list warp-synchronous executor: a walk's dependency
-// lists cut into pieces of at most `split` entries (at most 32 per unknown),
+// lists cut into k <= 32 interleaved pieces of about `split` entries (piece j
+// of an unknown covers entries lo, lo + k, lo + 2k, ... below hi, lo = list
+// start + j; k = the number of adjacent lanes holding the unknown),
 // 32 pieces per warp segment with no unknown straddling two segments (padding
 // pieces have walk -1). A chunk holds at most ceil(chunk/32) segments (one
 // per warp when chunk = threads per CTA) and never crosses a multiple of
@@ -61,8 +63,8 @@ struct PieceTable {
   int split = 0, chunk = 0, nseg = 0, nchunks = 0;
   int* walk = nullptr;    // device [nseg*32]
   int* row = nullptr;     // device [nseg*32] row of the unknown (perm of its position; 0 for padding)
-  int* lo = nullptr;      // device [nseg*32] first entry
-  int* hi = nullptr;      // device [nseg*32] end entry
+  int* lo = nullptr;      // device [nseg*32] first entry (list start + piece index)
+  int* hi = nullptr;      // device [nseg*32] end of the list
   int* cseg = nullptr;    // device [nchunks+1] first segment of each chunk
   int* cbase = nullptr;   // device [nchunks] first walk index of each chunk
   unsigned char* seg_split = nullptr;  // device [nseg] 1 if an unknown of the segment spans several lanes
