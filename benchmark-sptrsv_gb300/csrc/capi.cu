@@ -696,7 +696,7 @@ int make_plan(sptrsv_gb300_handle_s* h, const std::vector<int>& row_ptr, cudaStr
     CUDA_TRY(cudaMemcpyAsync(col_ptr.data(), h->csc_ptr, sizeof(int) * ((size_t)n + 1), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
     P.split_fwd = long_share(row_ptr, 32) > 0.05 ? 32 : 0;
-    P.split_adj = long_share(col_ptr, 32) > 0.05 ? 32 : 0;
+    P.split_adj = long_share(col_ptr, 32) > 0.05 ? 8 : 0;  // the reverse walk measured best with short pieces
   }
   if (n > 0 && nl >= 256 && h->batch_count == 1 && nnz > n) {
     const long long width = ((long long)n + nl - 1) / nl;
