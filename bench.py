@@ -20,7 +20,8 @@ Arms:
                    or the reference build where it exists), the four solves of a
                    step run concurrently on four host threads.
 Multi-GPU: every rank solves the same workload independently (replicas);
-the batch workload instead shards its systems over the ranks (nnz-balanced).
+the batch workload instead shards its systems over the ranks (nnz-balanced)
+and the multi_rhs workload its right-hand-side columns (contiguous slices).
 Profiling runs: --scale shrinks the systems, --cases picks a subset, and
 --opt KEY=VALUE fixes a solver option (the autotuner is then skipped).
 
@@ -477,35 +478,65 @@ def run_multi_rhs(args):
     import torch
 
     from oracle import oracle
-    from sptrsv_gb300 import SyncFreeSolver, matgen
+    from sptrsv_gb300 import SyncFreeSolver, matgen, shard
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     m = matgen.system_1m(seed=2)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
     out = {}
     for rhs in (1, 16, 64):
         rng = np.random.default_rng(rhs)
         B = rng.standard_normal((m.n, rhs))
-        ref = oracle.port().solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, B if rhs > 1 else B[:, 0])
-        ref = ref.reshape(m.n, rhs)
-        b = torch.from_numpy(np.ascontiguousarray(B.T)).cuda().t()
-        s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, values=m.val, sync_check=False,
-                           **args.solver_kw)
-        x = s.solve(b)
-        t64 = _timed(lambda: s.solve(b, out=x), args.steps, flush)
-        err64 = float((x.cpu().numpy() - ref).__abs__().max() / np.abs(ref).max())
-        s.set_option(7, 1)
-        xr, iters, est = s.solve_refine(b)
-        s.set_option(7, 0)
-        tmix = _timed(lambda: s.solve_refine(b, out=xr, tol=0.0, max_iter=iters), args.steps, flush)
-        errmix = float((xr.cpu().numpy() - ref).__abs__().max() / np.abs(ref).max())
+        # the right-hand sides shard over ranks as contiguous column slices;
+        # every rank holds the whole triangle and its analysis
+        c0, c1 = shard.rhs_columns(rhs, world, rank)
+        w = c1 - c0
+        t64 = tmix = 0.0
+        err64 = errmix = 0.0
+        iters = 0
+        if w > 0:
+            Bl = B[:, c0:c1]
+            ref = oracle.port().solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution,
+                                      Bl if w > 1 else Bl[:, 0])
+            ref = ref.reshape(m.n, w)
+            b = torch.from_numpy(np.ascontiguousarray(Bl.T)).cuda().t()
+            s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, values=m.val, sync_check=False,
+                               **args.solver_kw)
+            x = s.solve(b)
+            t64 = _timed(lambda: s.solve(b, out=x), args.steps, flush)
+            err64 = float((x.cpu().numpy() - ref).__abs__().max() / np.abs(ref).max())
+            s.set_option(7, 1)
+            xr, iters, est = s.solve_refine(b)
+            s.set_option(7, 0)
+            tmix = _timed(lambda: s.solve_refine(b, out=xr, tol=0.0, max_iter=iters), args.steps, flush)
+            errmix = float((xr.cpu().numpy() - ref).__abs__().max() / np.abs(ref).max())
+            s.close()
+        if dist is not None:
+            # whole-job time = the slowest rank; errors = the worst slice
+            t = torch.tensor([t64, tmix, err64, errmix, iters], dtype=torch.float64, device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            t64, tmix, err64, errmix = (float(v) for v in t.tolist()[:4])
+            iters = int(t[4].item())
         bp = bytes_pass(m.n, m.nnz, rhs)
         out[f"rhs{rhs}"] = {"fp64_ms": round(t64, 4), "mixed_ms": round(tmix, 4), "refine_steps": iters,
                             "speedup_mixed_vs_fp64": round(t64 / tmix, 3), "fp64_fwd_err": err64,
                             "mixed_fwd_err": errmix, "fp64_problem_gbs": round(bp / t64 / 1e6, 2),
                             "mixed_problem_gbs": round(bp / tmix / 1e6, 2)}
-        s.close()
+    if dist is not None:
+        dist.destroy_process_group()
+        if rank != 0:
+            return 0
     line = {"workload": "multi_rhs", "metric": "FP32+FP64-refinement speed-up over plain FP64 (n=1M, rhs=64)",
             "value": out["rhs64"]["speedup_mixed_vs_fp64"], "unit": "x", "higher_is_better": True,
-            "n": m.n, "nnz": m.nnz, "cases": out, "config": {"workload": "n=1M Poisson(9) band 20k, col-major B"}}
+            "n_gpus": world, "n": m.n, "nnz": m.nnz, "cases": out,
+            "config": {"workload": "n=1M Poisson(9) band 20k, col-major B",
+                       "parallelism": f"rhs columns sharded over {world} rank(s)" if world > 1 else "one GPU"}}
     print(json.dumps(line), flush=True)
     return 0
 

@@ -8,7 +8,10 @@ rank derives the same map without communicating. The only collective is the
 host-side gather of per-rank solutions at the end (``gather_solutions``).
 
 A single system does not shard: its dependency chain would need fine-grained
-cross-GPU synchronisation. Those runs are replicas.
+cross-GPU synchronisation. Those runs are replicas. Its right-hand sides do:
+with many columns, every rank holds the same triangle and analysis and solves a
+contiguous slice of the columns (``rhs_columns``); ``gather_columns`` joins the
+slices afterwards.
 """
 from __future__ import annotations
 
@@ -70,4 +73,39 @@ def gather_solutions(local: dict[int, np.ndarray], count: int, group=None) -> li
     missing = [k for k, v in enumerate(out) if v is None]
     if missing:
         raise RuntimeError(f"systems not solved by any rank: {missing[:8]}")
+    return out
+
+
+def rhs_columns(rhs: int, world: int, rank: int) -> tuple[int, int]:
+    """Contiguous slice [start, stop) of ``rhs`` right-hand-side columns owned
+    by ``rank``: the first ``rhs % world`` ranks take one column more, so slice
+    widths differ by at most one. A rank may own no column (start == stop)."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("rank out of range")
+    if rhs < 0:
+        raise ValueError("rhs must be >= 0")
+    base, extra = divmod(rhs, world)
+    start = rank * base + min(rank, extra)
+    return start, start + base + (1 if rank < extra else 0)
+
+
+def gather_columns(local: np.ndarray, rhs: int, group=None) -> np.ndarray:
+    """Joins every rank's n x (its ``rhs_columns`` width) block into the
+    n x rhs solution on all ranks (host memory, after the timed region).
+    Checks that each rank's block has the width its slice asks for."""
+    import torch.distributed as dist
+    world = dist.get_world_size(group)
+    rank = dist.get_rank(group)
+    local = np.asarray(local)
+    if local.ndim != 2:
+        raise ValueError("local block must be n x width")
+    parts: list = [None] * world
+    dist.all_gather_object(parts, (rank, local), group=group)
+    n = local.shape[0]
+    out = np.empty((n, rhs), dtype=local.dtype)
+    for r, blk in parts:
+        a, b = rhs_columns(rhs, world, r)
+        if blk.shape != (n, b - a):
+            raise RuntimeError(f"rank {r} returned a block of shape {blk.shape}, expected {(n, b - a)}")
+        out[:, a:b] = blk
     return out

@@ -36,6 +36,20 @@ def test_assign_edge_cases():
         shard.shard_of([1, 2], 2, 2)
 
 
+def test_rhs_columns_partition():
+    for rhs in (0, 1, 7, 16, 64):
+        for world in (1, 2, 3, 4, 8):
+            cols = [shard.rhs_columns(rhs, world, r) for r in range(world)]
+            assert cols[0][0] == 0 and cols[-1][1] == rhs
+            assert all(cols[r][1] == cols[r + 1][0] for r in range(world - 1))
+            widths = [b - a for a, b in cols]
+            assert max(widths) - min(widths) <= 1
+    with pytest.raises(ValueError):
+        shard.rhs_columns(4, 2, 2)
+    with pytest.raises(ValueError):
+        shard.rhs_columns(-1, 2, 0)
+
+
 def _free_port():
     with socket.socket() as s:
         s.bind(("127.0.0.1", 0))
@@ -59,7 +73,19 @@ def _rank_main(rank, world, port, weights, result_q):
             shard.gather_solutions({0: np.zeros(1)}, len(weights))
         except RuntimeError:
             dup_err = True
-        result_q.put((rank, ok, len(mine), dup_err))
+        # right-hand-side columns: every rank solves its slice of B with the
+        # oracle (stand-in for the device solve) and the slices join to L^-1 B
+        from oracle import oracle
+        from sptrsv_gb300 import matgen
+        m = matgen.poisson_band(200, 4.0, 50, seed=3)
+        B = np.random.default_rng(4).standard_normal((m.n, 7))
+        a, b = shard.rhs_columns(7, world, rank)
+        blk = oracle.port().solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution,
+                                  np.ascontiguousarray(B[:, a:b])).reshape(m.n, b - a)
+        X = shard.gather_columns(blk, 7)
+        full = oracle.port().solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, B).reshape(m.n, 7)
+        cols_ok = bool(np.array_equal(X, full))
+        result_q.put((rank, ok and cols_ok, len(mine), dup_err))
     finally:
         dist.destroy_process_group()
 
