@@ -90,6 +90,8 @@ struct sptrsv_gb300_handle_s {
   PieceTable pc_fwd, pc_adj;
   ImportTable imports;
   int import_option = 1;   // importer warp on blocked layouts (SPTRSV_OPTION_IMPORT)
+  ImportTable pipe;        // unit pipeline tables (ring slots, stages)
+  int pipe_option = 0;     // SPTRSV_OPTION_UNIT_PIPELINE: 0 off, 1 on, else the ring cap
   // staged values
   Values<double> v64;
   Values<float> v32;
@@ -97,10 +99,12 @@ struct sptrsv_gb300_handle_s {
   // workspace
   DevBuf xw, left_sum, counters, r32, d32, stats;
   DevBuf tb, tx;  // row-major staging of column-major blocks of many right-hand sides
+  DevBuf c0;      // unit pipeline: first term b/d of every position
   DeviceCtl* ctl = nullptr;
   int* flags = nullptr;
   int* host_pinned = nullptr;  // 4 ints
   int last_sched = 0;
+  bool last_pipe = false;  // the last one-rhs solve ran the unit pipeline
   size_t device_bytes = 0;
   int profile = 0;
   cudaEvent_t ev_exec[2] = {nullptr, nullptr};
@@ -173,6 +177,9 @@ void free_imports(ImportTable& t) {
   if (t.ptr) cudaFree(t.ptr);
   if (t.q) cudaFree(t.q);
   if (t.dep_slot) cudaFree(t.dep_slot);
+  if (t.ustage) cudaFree(t.ustage);
+  if (t.stab) cudaFree(t.stab);
+  if (t.segs) cudaFree(t.segs);
   t = ImportTable();
 }
 
@@ -230,6 +237,7 @@ void free_analysis(sptrsv_gb300_handle_s* h) {
   free_pieces(h->pc_fwd);
   free_pieces(h->pc_adj);
   free_imports(h->imports);
+  free_imports(h->pipe);
   free_values(h->v64);
   free_values(h->v32);
   h->staged64 = h->staged32 = false;
@@ -314,6 +322,7 @@ int build_layout(sptrsv_gb300_handle_s* h, int block, cudaStream_t s) {
   free_pieces(h->pc_fwd);
   free_pieces(h->pc_adj);
   free_imports(h->imports);
+  free_imports(h->pipe);
   free_values(h->v64);
   free_values(h->v32);
   h->staged64 = h->staged32 = false;
@@ -578,8 +587,13 @@ int ensure_pieces(sptrsv_gb300_handle_s* h, bool adj, int split, int chunk, cuda
 // Import table of the forward walk for chunks of `chunk` positions (see
 // ImportTable). When a chunk's window and imports do not fit one CTA's shared
 // memory only the sizes are recorded (no device arrays; the caller checks).
-int build_imports(sptrsv_gb300_handle_s* h, int chunk, size_t elem, cudaStream_t s) {
-  free_imports(h->imports);
+// ring_cap = 0: the importer kernel's table (a window as wide as the longest
+// unit). ring_cap > 0: the unit pipeline's (ring slots, far dependencies
+// imported, stages of at most pmax positions and emax entries).
+int build_import_table(sptrsv_gb300_handle_s* h, ImportTable& t, int chunk, size_t elem, int ring_cap, int pmax,
+                       int emax, int stages, cudaStream_t s) {
+  free_imports(t);
+  const int smax = std::max(4, pmax / 8);  // segments per stage
   const Layout& L = h->layout;
   const int n = L.n;
   const int ndep = L.ndep;
@@ -597,29 +611,95 @@ int build_imports(sptrsv_gb300_handle_s* h, int chunk, size_t elem, cudaStream_t
   const int nchunks = static_cast<int>(starts.size()) - 1;
   int width = 1;  // shared-memory window: the longest unit
   for (int c = 0; c < nchunks; ++c) width = std::max(width, starts[c + 1] - starts[c]);
-  std::vector<int> cptr((size_t)nchunks + 1, 0), q, slot(ndep > 0 ? (size_t)ndep : 1, -1), ext;
+  int ring = 0;
+  if (ring_cap > 0) {
+    ring = 64;
+    while (ring < width && ring < ring_cap) ring *= 2;
+  }
+  const int win = ring > 0 ? ring : width;  // first import slot
+  // a dependency reads the ring when it is in the unit and (with wrapping) fewer
+  // than ring - 32 positions back
+  auto in_ring = [&](int p, int qe, int base, int len) {
+    return qe >= base && (ring == 0 || len <= ring || p - qe < ring - 32);
+  };
+  std::vector<int> cptr((size_t)nchunks + 1, 0), q, slot((size_t)std::max(ndep, 1) + 16, -1), ext;
+  std::vector<int> ustage, segs, useg;
+  std::vector<int4> stab;  // two per stage: {lo, hi, e0, e1}, {first segment, end segment, 0, 0}
   int max_imp = 0;
+  bool stages_fit = true;
   for (int c = 0; c < nchunks; ++c) {
-    const int base = starts[c], end = starts[c + 1];
+    const int base = starts[c], end = starts[c + 1], len = end - base;
     ext.clear();
-    for (int e = ptr[base]; e < ptr[end]; ++e)
-      if (pos[e] < base) ext.push_back(pos[e]);
+    for (int p = base; p < end; ++p)
+      for (int e = ptr[p]; e < ptr[p + 1]; ++e)
+        if (!in_ring(p, pos[e], base, len)) ext.push_back(pos[e]);
     std::sort(ext.begin(), ext.end());
     ext.erase(std::unique(ext.begin(), ext.end()), ext.end());
-    for (int e = ptr[base]; e < ptr[end]; ++e) {
-      const int qe = pos[e];
-      slot[e] = qe >= base ? qe - base
-                           : width + static_cast<int>(std::lower_bound(ext.begin(), ext.end(), qe) - ext.begin());
-    }
+    for (int p = base; p < end; ++p)
+      for (int e = ptr[p]; e < ptr[p + 1]; ++e) {
+        const int qe = pos[e];
+        slot[e] = in_ring(p, qe, base, len)
+                      ? (ring > 0 ? (qe - base) & (ring - 1) : qe - base)
+                      : win + static_cast<int>(std::lower_bound(ext.begin(), ext.end(), qe) - ext.begin());
+      }
     q.insert(q.end(), ext.begin(), ext.end());
     cptr[c + 1] = static_cast<int>(q.size());
     max_imp = std::max(max_imp, static_cast<int>(ext.size()));
+    if (ring > 0) {
+      // segments: runs of at most 32 consecutive positions (one lane each) whose
+      // lists fit a stage buffer. (Ending runs early at level boundaries was
+      // measured: no faster on 32-wide levels, slower on narrower ones.)
+      useg.clear();
+      int first = base;
+      for (int p = base + 1; p < end; ++p) {
+        if (p - first >= 32 || ptr[p + 1] - ptr[first] > emax) {
+          useg.push_back(first);
+          first = p;
+        }
+      }
+      useg.push_back(first);
+      // stages: runs of whole segments with at most pmax positions, emax list
+      // entries and smax segments
+      ustage.push_back(static_cast<int>(stab.size() / 2));
+      const int sg_base = static_cast<int>(segs.size());
+      const int nsu = static_cast<int>(useg.size());
+      for (int i = 0; i < nsu;) {
+        const int lo = useg[i];
+        int j = i;
+        while (j < nsu) {
+          const int hi = j + 1 < nsu ? useg[j + 1] : end;
+          if (hi - lo > pmax || ptr[hi] - ptr[lo] > emax || j + 1 - i > smax) break;
+          ++j;
+        }
+        if (j == i) {  // one segment's lists exceed a stage buffer
+          stages_fit = false;
+          break;
+        }
+        const int hi = j < nsu ? useg[j] : end;
+        stab.push_back(make_int4(lo, hi, ptr[lo], ptr[hi]));
+        stab.push_back(make_int4(sg_base + i, sg_base + j, 0, 0));
+        i = j;
+      }
+      segs.insert(segs.end(), useg.begin(), useg.end());
+    }
   }
-  ImportTable& t = h->imports;
   t.chunk = chunk;
   t.width = width;
   t.max_imports = max_imp;
-  if (imported_smem_bytes(width, max_imp, elem) > 220 * 1024) return SPTRSV_OK;  // recorded: does not fit
+  t.ring = ring;
+  t.ring_cap = ring_cap;
+  t.pmax = pmax;
+  t.emax = emax;
+  t.stages = stages;
+  t.smax = smax;
+  if (ring > 0) {
+    ustage.push_back(static_cast<int>(stab.size() / 2));
+    segs.push_back(n);
+    if (!stages_fit || unit_smem_bytes(ring, max_imp, pmax, emax, smax, stages, elem) > 220 * 1024)
+      return SPTRSV_OK;  // recorded: does not fit
+  } else if (imported_smem_bytes(width, max_imp, elem) > 220 * 1024) {
+    return SPTRSV_OK;  // recorded: does not fit
+  }
   CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.start), sizeof(int) * starts.size()));
   CUDA_TRY(cudaMemcpy(t.start, starts.data(), sizeof(int) * starts.size(), cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.ptr), sizeof(int) * cptr.size()));
@@ -628,11 +708,26 @@ int build_imports(sptrsv_gb300_handle_s* h, int chunk, size_t elem, cudaStream_t
   CUDA_TRY(cudaMemcpy(t.ptr, cptr.data(), sizeof(int) * cptr.size(), cudaMemcpyHostToDevice));
   if (!q.empty()) CUDA_TRY(cudaMemcpy(t.q, q.data(), sizeof(int) * q.size(), cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMemcpy(t.dep_slot, slot.data(), sizeof(int) * slot.size(), cudaMemcpyHostToDevice));
+  if (ring > 0) {
+    CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.ustage), sizeof(int) * ustage.size()));
+    CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.stab), sizeof(int4) * std::max<size_t>(stab.size(), 2)));
+    segs.resize(segs.size() + 16, n);  // bulk copies read up to 16 bytes past a slice
+    CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&t.segs), sizeof(int) * segs.size()));
+    CUDA_TRY(cudaMemcpy(t.ustage, ustage.data(), sizeof(int) * ustage.size(), cudaMemcpyHostToDevice));
+    if (!stab.empty()) CUDA_TRY(cudaMemcpy(t.stab, stab.data(), sizeof(int4) * stab.size(), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(t.segs, segs.data(), sizeof(int) * segs.size(), cudaMemcpyHostToDevice));
+    t.nstages = static_cast<int>(stab.size() / 2);
+    h->device_bytes += sizeof(int) * (ustage.size() + segs.size()) + sizeof(int4) * stab.size();
+  }
   t.chunk = chunk;
   t.nchunks = nchunks;
   t.max_imports = max_imp;
   h->device_bytes += sizeof(int) * (starts.size() + cptr.size() + q.size() + slot.size());
   return SPTRSV_OK;
+}
+
+int build_imports(sptrsv_gb300_handle_s* h, int chunk, size_t elem, cudaStream_t s) {
+  return build_import_table(h, h->imports, chunk, elem, 0, 0, 0, 0, s);
 }
 
 // Largest per-chunk entry budget whose ring of stage buffers (plus the
@@ -769,6 +864,25 @@ int stage_values(sptrsv_gb300_handle_s* h, const void* d_val, int dtype, cudaStr
   return SPTRSV_OK;
 }
 
+// Unit pipeline tables for this order block (built on first use); true when
+// they exist and the CTA's shared memory holds them for element type T.
+template <typename T>
+bool pipe_ready(sptrsv_gb300_handle_s* h, int chunk, cudaStream_t s) {
+  const int ring_cap = h->pipe_option == 1 ? 8192 : h->pipe_option;
+  const int emax = h->emax_option > 0 ? h->emax_option : 2048;
+  const int pmax = std::min(512, std::max(32, (emax / 4) & ~31));  // at most the kernel's 512
+  const int stages = (h->user_set & (1ull << SPTRSV_OPTION_STAGES)) ? h->stages_option : 3;
+  ImportTable& t = h->pipe;
+  if (t.chunk != chunk || t.ring_cap != ring_cap || t.emax != emax || t.pmax != pmax || t.stages != stages) {
+    if (build_import_table(h, t, chunk, sizeof(T), ring_cap, pmax, emax, stages, s) != SPTRSV_OK) {
+      free_imports(t);
+      return false;
+    }
+  }
+  return t.ustage != nullptr &&
+         unit_smem_bytes(t.ring, t.max_imports, t.pmax, t.emax, t.smax, t.stages, sizeof(T)) <= 220 * 1024;
+}
+
 // Automatic executor settings for a request.
 ExecConfig pick_config(const sptrsv_gb300_handle_s* h, int rhs) {
   ExecConfig c = h->cfg;
@@ -828,6 +942,7 @@ int solve_typed(sptrsv_gb300_handle_s* h, const Values<T>& V, int rhs, int layou
   ExecConfig c = pick_config(h, rhs);
   if (adj) c.sched = SCHED_PULL;  // the transposed solve walks the analysis in reverse with the pull executor
   h->last_sched = c.sched;
+  h->last_pipe = false;
   const size_t elems = (size_t)n * (size_t)rhs;
   if (c.sched == SCHED_PUSH) {
     ST_TRY(ensure_buf(h, h->left_sum, elems * sizeof(T), 1, s));
@@ -855,6 +970,16 @@ int solve_typed(sptrsv_gb300_handle_s* h, const Values<T>& V, int rhs, int layou
     ST_TRY(ensure_table(h, adj != nullptr, c.chunk, emax));
     CUDA_TRY(launch_pull_staged<T>(h->layout, V, adj ? h->tab_adj : h->tab_fwd, v, static_cast<T*>(h->xw.p), h->ctl,
                                    c, timeout_ns(h), h->num_sms, s, adj));
+  } else if (rhs == 1 && c.wsync && !c.exact && !adj && h->pipe_option && h->layout_block < n &&
+             c.chunk == h->layout_block && c.smem_tier && pipe_ready<T>(h, c.chunk, s)) {
+    // blocked layout: one consumer warp per unit reads everything from shared
+    // memory; a loader warp streams the unit's stages, an importer warp its
+    // external dependencies
+    if (c.wsync_batch == 0) c.wsync_batch = 2;
+    ST_TRY(ensure_buf(h, h->c0, ((size_t)n + 16) * sizeof(T), 0, s));
+    CUDA_TRY(launch_pull_unit<T>(h->layout, V, v, static_cast<T*>(h->xw.p), static_cast<T*>(h->c0.p), h->ctl, c,
+                                 timeout_ns(h), h->num_sms, s, h->pipe));
+    h->last_pipe = true;
   } else if (rhs == 1 && c.wsync && !c.exact && !adj && h->import_option && h->layout_block < n &&
              c.chunk == h->layout_block && c.smem_tier &&
              !(c.split > 0 && h->max_dep_cnt > c.split) &&
@@ -970,6 +1095,7 @@ int sptrsv_gb300_destroy(sptrsv_handle_t h) {
   free_buf(h->stats);
   free_buf(h->tb);
   free_buf(h->tx);
+  free_buf(h->c0);
   if (h->ctl) cudaFree(h->ctl);
   if (h->flags) cudaFree(h->flags);
   if (h->host_pinned) cudaFreeHost(h->host_pinned);
@@ -1063,6 +1189,11 @@ static int set_option_value(sptrsv_handle_t h, int option, long long value) {
     case SPTRSV_OPTION_IMPORT:
       h->import_option = value != 0;
       return SPTRSV_OK;
+    case SPTRSV_OPTION_UNIT_PIPELINE:
+      if (!(value == 0 || value == 1 || (value >= 128 && value <= 8192 && (value & (value - 1)) == 0)))
+        return SPTRSV_ERR_INVALID;
+      h->pipe_option = static_cast<int>(value);
+      return SPTRSV_OK;
     default:
       return SPTRSV_ERR_INVALID;
   }
@@ -1091,6 +1222,7 @@ int sptrsv_gb300_get_option(sptrsv_handle_t h, int option, long long* value) {
     case SPTRSV_OPTION_SPLIT: *value = h->split; break;
     case SPTRSV_OPTION_WSYNC_BATCH: *value = h->wsync_batch; break;
     case SPTRSV_OPTION_IMPORT: *value = h->import_option; break;
+    case SPTRSV_OPTION_UNIT_PIPELINE: *value = h->pipe_option; break;
     default: return SPTRSV_ERR_INVALID;
   }
   return SPTRSV_OK;
@@ -1349,6 +1481,7 @@ int sptrsv_gb300_get_info(sptrsv_handle_t h, sptrsv_info* info) {
   info->staged = c.staged;
   info->split = planned(h, SPTRSV_OPTION_SPLIT) ? h->plan.split_fwd : c.split;
   info->locality_permille = static_cast<int>(h->plan.locality * 1000.0 + 0.5);
+  info->unit_pipeline = h->last_pipe ? 1 : 0;
   return h->analysed ? SPTRSV_OK : SPTRSV_ERR_STATE;
 }
 

@@ -111,15 +111,6 @@ __device__ __forceinline__ unsigned group_mask(int G) {
   return ((1u << G) - 1u) << (lane32 & ~(G - 1));
 }
 
-// Claim the next chunk for this CTA (uniform across the CTA).
-__device__ __forceinline__ unsigned next_chunk(DeviceCtl* ctl, unsigned nchunks, unsigned* s_chunk) {
-  if (threadIdx.x == 0) *s_chunk = ctl_failed(ctl) ? nchunks : atomicAdd(&ctl->ticket, 1u);
-  __syncthreads();
-  const unsigned c = *s_chunk;
-  __syncthreads();
-  return c;
-}
-
 template <typename T, bool SHARED>
 __device__ __forceinline__ typename Flag<T>::Bits wait_flag(const T* p, DeviceCtl* ctl, unsigned long long timeout,
                                                             int where, unsigned sleep_min, unsigned sleep_max) {
@@ -417,38 +408,63 @@ __global__ void __launch_bounds__(288) k_pull_wsync_imp(ExecArgs<T> a) {
         }
       }
     } else {
-      int n_row = 0, n_e = 0, n_e1 = 0;
+      // A warp takes every ncw-th segment of the chunk. Its next segment's
+      // scaled right-hand side and first U list entries are loaded while it
+      // works on the current one, and the row and list bounds they need one
+      // segment earlier still, so a segment starts on values that have landed
+      // instead of waiting for two dependent global round trips.
+      int f_row = 0, f_e = 0, f_e1 = 0;           // bounds, two segments ahead
       auto fetch = [&](int sg) {
         const int jj = sg * 32 + lane;
         if (jj < len) {
-          n_row = a.perm[base + jj];
-          n_e = a.dep_ptr[base + jj];
-          n_e1 = a.dep_ptr[base + jj + 1];
+          f_row = a.perm[base + jj];
+          f_e = a.dep_ptr[base + jj];
+          f_e1 = a.dep_ptr[base + jj + 1];
         }
       };
-      if (warp * 32 < len) fetch(warp);
+      int s_row = 0, s_e = 0, s_e1 = 0;           // staged, one segment ahead
+      T s_acc = T(0);
+      int s_ls[U];
+      T s_w[U];
+      auto stage = [&](int sg) {
+        const int jj = sg * 32 + lane;
+        s_row = f_row;
+        s_e = f_e;
+        s_e1 = jj < len ? f_e1 : f_e;
+        s_acc = jj < len ? a.b[(long long)f_row * a.b_si] * a.rcp[base + jj] : T(0);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int ee = s_e + u;
+          s_ls[u] = ee < s_e1 ? a.dep_slot[ee] : -1;
+          s_w[u] = ee < s_e1 ? vals[ee] : T(0);
+        }
+      };
+      if (warp * 32 < len) {
+        fetch(warp);
+        stage(warp);
+        if ((warp + ncw) * 32 < len) fetch(warp + ncw);
+      }
       for (int seg = warp; seg * 32 < len && !fail; seg += ncw) {
         const int j = seg * 32 + lane;
         bool done = j >= len;
         const int p = base + j;
-        const int row = n_row;
-        int e = n_e;
-        const int e1 = n_e1;
-        if ((seg + ncw) * 32 < len) fetch(seg + ncw);
-        T acc = T(0);
-        if (!done) acc = a.b[(long long)row * a.b_si] * a.rcp[p];
+        const int row = s_row;
+        int e = s_e;
+        const int e1 = s_e1;
+        T acc = s_acc;
         int ls[U];
         T w[U];
         Bits bits[U];
         unsigned todo = 0u;
-        auto load_batch = [&]() {
-          todo = 0u;
 #pragma unroll
-          for (int u = 0; u < U; ++u) {
-            const int ee = e + u;
-            ls[u] = ee < e1 ? a.dep_slot[ee] : -1;
-            w[u] = ee < e1 ? vals[ee] : T(0);
-          }
+        for (int u = 0; u < U; ++u) {
+          ls[u] = s_ls[u];
+          w[u] = s_w[u];
+        }
+        if ((seg + ncw) * 32 < len) stage(seg + ncw);
+        if ((seg + 2 * ncw) * 32 < len) fetch(seg + 2 * ncw);
+        auto poll_batch = [&]() {
+          todo = 0u;
 #pragma unroll
           for (int u = 0; u < U; ++u) {
             bits[u] = F::EMPTY;
@@ -458,7 +474,16 @@ __global__ void __launch_bounds__(288) k_pull_wsync_imp(ExecArgs<T> a) {
             }
           }
         };
-        if (!done) load_batch();
+        auto load_batch = [&]() {
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            const int ee = e + u;
+            ls[u] = ee < e1 ? a.dep_slot[ee] : -1;
+            w[u] = ee < e1 ? vals[ee] : T(0);
+          }
+          poll_batch();
+        };
+        if (!done) poll_batch();
         WaitBudget wb(a.timeout_ns);
         unsigned idle = 0u;
         for (;;) {

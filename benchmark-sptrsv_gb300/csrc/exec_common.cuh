@@ -4,6 +4,15 @@
 
 namespace sptrsv {
 
+// Claim the next chunk for this CTA (uniform across the CTA).
+__device__ __forceinline__ unsigned next_chunk(DeviceCtl* ctl, unsigned nchunks, unsigned* s_chunk) {
+  if (threadIdx.x == 0) *s_chunk = ctl_failed(ctl) ? nchunks : atomicAdd(&ctl->ticket, 1u);
+  __syncthreads();
+  const unsigned c = *s_chunk;
+  __syncthreads();
+  return c;
+}
+
 // The last CTA to leave resets the chunk ticket so the next launch starts at 0.
 __device__ __forceinline__ void leave(DeviceCtl* ctl) {
   if (threadIdx.x == 0) {

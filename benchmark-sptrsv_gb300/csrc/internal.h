@@ -76,12 +76,27 @@ struct PieceTable {
 // (sorted) from other units; dep_slot[e] = shared-memory slot of dependency e
 // (in-unit: its position minus the unit start; imported: width + its index in
 // the unit's list, width = the longest unit).
+//
+// The unit pipeline (ring > 0) keeps only a ring of `ring` slots (a power of
+// two) per unit: an in-unit dependency fewer than ring - 32 positions back
+// reads slot (position - unit start) mod ring, and every other dependency,
+// in-unit ones further back included, is imported into slot ring + index.
+// Each unit is cut into segments (runs of at most 32 consecutive positions,
+// one lane each; segment g covers [segs[g], segs[g+1])) and the segments into
+// stages of at most pmax positions, emax list entries and smax segments: unit
+// c owns stages ustage[c] .. ustage[c+1]-1; stage k covers positions
+// [stab[2k].x, stab[2k].y), list entries [stab[2k].z, stab[2k].w) and
+// segments [stab[2k+1].x, stab[2k+1].y).
 struct ImportTable {
   int chunk = 0, nchunks = 0, width = 0, max_imports = 0;
   int* start = nullptr;     // device [nchunks+1]
   int* ptr = nullptr;       // device [nchunks+1]
   int* q = nullptr;         // device [total imports]
-  int* dep_slot = nullptr;  // device [ndep]
+  int* dep_slot = nullptr;  // device [ndep + padding]
+  int ring = 0, ring_cap = 0, pmax = 0, emax = 0, smax = 0, stages = 0, nstages = 0;
+  int* ustage = nullptr;    // device [nchunks+1]
+  int4* stab = nullptr;     // device [2*nstages]
+  int* segs = nullptr;      // device [segments+1 + padding] first position of each segment
 };
 
 // Solve-time description of one right-hand-side block. Element (i, k) of b
@@ -224,6 +239,13 @@ template <typename T>
 cudaError_t launch_pull_imported(const Layout& L, const Values<T>& V, const VecView<T>& v, T* xw, DeviceCtl* ctl,
                                  const ExecConfig& cfg, unsigned long long timeout_ns, int num_sms, cudaStream_t s,
                                  const ImportTable& im);
+// unit pipeline: consumer, importer and bulk-copy loader warp per unit (blocked layouts);
+// c0 = workspace of n + 16 elements for the first terms
+size_t unit_smem_bytes(int ring, int max_imports, int pmax, int emax, int smax, int stages, size_t elem);
+template <typename T>
+cudaError_t launch_pull_unit(const Layout& L, const Values<T>& V, const VecView<T>& v, T* xw, T* c0, DeviceCtl* ctl,
+                             const ExecConfig& cfg, unsigned long long timeout_ns, int num_sms, cudaStream_t s,
+                             const ImportTable& im);
 size_t staged_smem_bytes(int cmax, int emax, size_t elem, bool smem_tier, int stages);
 template <typename T>
 cudaError_t launch_pull_staged(const Layout& L, const Values<T>& V, const ChunkTable& tab, const VecView<T>& v, T* xw,

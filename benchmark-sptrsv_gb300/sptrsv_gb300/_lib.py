@@ -61,6 +61,7 @@ OPTION_WARP_SYNC = 16
 OPTION_SPLIT = 17
 OPTION_WSYNC_BATCH = 18
 OPTION_IMPORT = 19
+OPTION_UNIT_PIPELINE = 20
 
 NOALLOC_MAX_N = 262144  # SPTRSV_NOALLOC_MAX_N
 
@@ -95,6 +96,7 @@ class Info(ctypes.Structure):
         ("staged", ctypes.c_int),
         ("split", ctypes.c_int),
         ("locality_permille", ctypes.c_int),
+        ("unit_pipeline", ctypes.c_int),
     ]
 
 

@@ -105,7 +105,8 @@ class SyncFreeSolver:
                  block: int | None = None, backoff_ns: int | None = None, ctas_per_sm: int | None = None,
                  staged: bool | None = None, stage_entries: int | None = None, stages: int | None = None,
                  warp_sync: bool | None = None, split: int | None = None, wsync_batch: int | None = None,
-                 import_deps: bool | None = None, fused_grad: bool | None = None, stream=None):
+                 import_deps: bool | None = None, unit_pipeline: int | None = None, fused_grad: bool | None = None,
+                 stream=None):
         torch = _torch()
         self._lib = load()
         self.device = torch.device("cuda", torch.cuda.current_device())
@@ -148,6 +149,7 @@ class SyncFreeSolver:
                        (_lib.OPTION_STAGE_ENTRIES, stage_entries), (_lib.OPTION_STAGES, stages),
                        (_lib.OPTION_WARP_SYNC, warp_sync), (_lib.OPTION_SPLIT, split),
                        (_lib.OPTION_WSYNC_BATCH, wsync_batch), (_lib.OPTION_IMPORT, import_deps),
+                       (_lib.OPTION_UNIT_PIPELINE, unit_pipeline),
                        (_lib.OPTION_FUSED_GRAD, fused_grad)):
             if v is not None:
                 self.set_option(opt, int(v))

@@ -106,9 +106,16 @@ typedef enum sptrsv_option {
   SPTRSV_OPTION_WSYNC_BATCH = 18, /* warp-synchronous one-rhs pull (not exact): dependencies a lane loads
                                      per lockstep iteration, 1, 2 or 4 (0 = automatic: 2 when the lists
                                      average <= 3 entries, else 1) */
-  SPTRSV_OPTION_IMPORT = 19       /* 1 (default): warp-synchronous one-rhs forward pull on a blocked
+  SPTRSV_OPTION_IMPORT = 19,      /* 1 (default): warp-synchronous one-rhs forward pull on a blocked
                                      layout (chunk = order block) gives each CTA an importer warp that
                                      copies the chunk's external dependencies into shared memory */
+  SPTRSV_OPTION_UNIT_PIPELINE = 20 /* warp-synchronous one-rhs forward pull on a blocked layout (chunk =
+                                     order block): 1 = one consumer warp per unit reading every operand
+                                     from shared memory, fed by a bulk-copy loader warp (stages of
+                                     SPTRSV_OPTION_STAGE_ENTRIES entries, default 2048, in
+                                     SPTRSV_OPTION_STAGES buffers, default 3) and an importer warp, with
+                                     a ring of up to 8192 value slots per unit; a power of two from 128
+                                     to 8192 = that ring size cap; 0 (default) = off */
 } sptrsv_option;
 
 typedef struct sptrsv_info {
@@ -132,6 +139,7 @@ typedef struct sptrsv_info {
   int staged;           /* 1: TMA-staged chunks */
   int split;            /* split length of the forward walk (0: one lane per unknown) */
   int locality_permille; /* automatic plan: dependencies inside order blocks, per mille */
+  int unit_pipeline;    /* 1: the last one-rhs solve ran the unit pipeline (SPTRSV_OPTION_UNIT_PIPELINE) */
 } sptrsv_info;
 
 typedef struct sptrsv_gb300_handle_s *sptrsv_handle_t;

@@ -111,10 +111,18 @@ def test_split_option_validated(cuda):
     for ok in (0, 1, 2, 4):
         s.set_option(_lib.OPTION_WSYNC_BATCH, ok)
         assert s.get_option(_lib.OPTION_WSYNC_BATCH) == ok
+    for bad in (-1, 2, 64, 100, 16384):
+        with pytest.raises(SptrsvError):
+            s.set_option(_lib.OPTION_UNIT_PIPELINE, bad)
+    for ok in (0, 1, 128, 8192):
+        s.set_option(_lib.OPTION_UNIT_PIPELINE, ok)
+        assert s.get_option(_lib.OPTION_UNIT_PIPELINE) == ok
 
 
 @pytest.mark.parametrize("cfg", [dict(schedule=2), dict(schedule=1),
                                  dict(schedule=2, staged=False, warp_sync=True, import_deps=True,
+                                      order_block=64),
+                                 dict(schedule=2, staged=False, warp_sync=True, unit_pipeline=1,
                                       order_block=64)])
 def test_wait_budget_expires_cleanly_then_recovers(cuda, cfg):
     """Natural order on the 2-D Laplacian makes single waits last far longer than

@@ -66,6 +66,8 @@ CONFIGS = [
     dict(schedule=2, staged=False, warp_sync=True, order_block=64, chunk=64, block=64, import_deps=False),
     dict(schedule=2, staged=False, warp_sync=True, order_block=96, chunk=96, block=64, wsync_batch=1),
     dict(schedule=2, staged=False, warp_sync=True, order_block=200, chunk=200, block=128, wsync_batch=4),
+    dict(schedule=2, staged=False, warp_sync=True, order_block=1000, chunk=1000, block=64, wsync_batch=1),
+    dict(schedule=2, staged=False, warp_sync=True, order_block=777, chunk=777, block=64, wsync_batch=4),
     dict(schedule=3, lanes=1),
     dict(schedule=3, lanes=8),
 ]
@@ -81,6 +83,53 @@ def test_fp64_matches_oracle(cuda, name, cfg):
     # a second solve on the same handle (self-cleaning workspace) gives the same answer
     x2 = s.solve(b_tensor(cuda, g)).cpu().numpy()
     assert relerr(x2, g["x64"]) <= TOL64
+
+
+PIPE_CONFIGS = [
+    dict(order_block=1000, chunk=1000, unit_pipeline=1),
+    dict(order_block=1000, chunk=1000, unit_pipeline=128, stage_entries=256, stages=2),
+    dict(order_block=777, chunk=777, unit_pipeline=256, stage_entries=512, stages=4, wsync_batch=1),
+    dict(order_block=300, chunk=300, unit_pipeline=128, stage_entries=128, wsync_batch=4),
+    dict(order_block=64, chunk=64, unit_pipeline=1),
+]
+
+
+@pytest.mark.parametrize("name", golden_names())
+@pytest.mark.parametrize("cfg", PIPE_CONFIGS, ids=lambda c: "-".join(f"{k}{v}" for k, v in c.items()))
+def test_unit_pipeline_matches_oracle(cuda, name, cfg):
+    """The unit pipeline (one consumer warp per order block, bulk-copy loader,
+    ring of value slots) against the oracle, in FP64 and FP32; with small ring
+    caps and stage buffers it wraps the ring, imports in-unit dependencies that
+    lie too far back, and recycles every stage buffer many times."""
+    g = load_golden(name)
+    s = make_solver(cuda, g, schedule=2, staged=False, warp_sync=True, **cfg)
+    x = s.solve(b_tensor(cuda, g)).cpu().numpy()
+    assert relerr(x, g["x64"]) <= TOL64
+    if int(g["rhs"]) == 1 and int(g["n"]) > cfg["order_block"]:
+        assert s.info()["unit_pipeline"] == 1
+    x2 = s.solve(b_tensor(cuda, g)).cpu().numpy()
+    assert relerr(x2, g["x64"]) <= TOL64
+    x32 = s.solve(b_tensor(cuda, g, np.float32)).cpu().numpy()
+    assert relerr(x32, g["x64"]) <= TOL32
+
+
+@pytest.mark.parametrize("ring,entries", [(128, 256), (1024, 2048), (1, 0)])
+def test_unit_pipeline_mesh_and_band(cuda, oracle_port, ring, entries):
+    """Larger blocked systems through the unit pipeline: a 2-D mesh in blocks of
+    20 mesh rows and a random band whose in-unit dependencies often lie beyond
+    the ring; FP64 results against the oracle."""
+    from sptrsv_gb300 import SyncFreeSolver, matgen
+    for m, ob in ((matgen.laplace2d_lower(100), 2000), (matgen.poisson_band(6000, 5.0, 400, seed=7), 1500),
+                  (matgen.laplace2d_lower(100).transpose(), 2000)):
+        rng = np.random.default_rng(11)
+        bvec = rng.standard_normal(m.n)
+        ref = oracle_port.solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, bvec)
+        s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, values=m.val, schedule=2, staged=False,
+                           warp_sync=True, order_block=ob, chunk=ob, unit_pipeline=ring, stage_entries=entries)
+        x = s.solve(cuda.from_numpy(bvec).cuda()).cpu().numpy()
+        assert relerr(x, ref) <= TOL64
+        assert s.info()["unit_pipeline"] == 1
+        s.close()
 
 
 @pytest.mark.parametrize("name", golden_names())
