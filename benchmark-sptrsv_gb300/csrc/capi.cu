@@ -92,6 +92,7 @@ struct sptrsv_gb300_handle_s {
   int import_option = 1;   // importer warp on blocked layouts (SPTRSV_OPTION_IMPORT)
   ImportTable pipe;        // unit pipeline tables (ring slots, stages)
   int pipe_option = 0;     // SPTRSV_OPTION_UNIT_PIPELINE: 0 off, 1 on, else the ring cap
+  int fused_refine = 1;    // SPTRSV_OPTION_FUSED_REFINE: first refinement step fused into the FP32 pass
   // staged values
   Values<double> v64;
   Values<float> v32;
@@ -1194,6 +1195,9 @@ static int set_option_value(sptrsv_handle_t h, int option, long long value) {
         return SPTRSV_ERR_INVALID;
       h->pipe_option = static_cast<int>(value);
       return SPTRSV_OK;
+    case SPTRSV_OPTION_FUSED_REFINE:
+      h->fused_refine = value != 0;
+      return SPTRSV_OK;
     default:
       return SPTRSV_ERR_INVALID;
   }
@@ -1223,6 +1227,7 @@ int sptrsv_gb300_get_option(sptrsv_handle_t h, int option, long long* value) {
     case SPTRSV_OPTION_WSYNC_BATCH: *value = h->wsync_batch; break;
     case SPTRSV_OPTION_IMPORT: *value = h->import_option; break;
     case SPTRSV_OPTION_UNIT_PIPELINE: *value = h->pipe_option; break;
+    case SPTRSV_OPTION_FUSED_REFINE: *value = h->fused_refine; break;
     default: return SPTRSV_ERR_INVALID;
   }
   return SPTRSV_OK;
@@ -1607,35 +1612,81 @@ int sptrsv_gb300_solve_refine(sptrsv_handle_t h, const double* d_val, int rhs, i
   const long long count = (long long)h->n * rhs;
   ST_TRY(ensure_buf(h, h->r32, sizeof(float) * count, 0, s));
   ST_TRY(ensure_buf(h, h->d32, sizeof(float) * count, 0, s));
-  ST_TRY(ensure_buf(h, h->stats, 2 * sizeof(unsigned long long), 1, s));
+  ST_TRY(ensure_buf(h, h->stats, 4 * sizeof(unsigned long long), 1, s));
   const long long si = layout == SPTRSV_LAYOUT_ROW_MAJOR ? rhs : 1;
   const long long sk = layout == SPTRSV_LAYOUT_ROW_MAJOR ? 1 : h->n;
   float* r32 = static_cast<float*>(h->r32.p);
   float* d32 = static_cast<float*>(h->d32.p);
   auto* stats = static_cast<unsigned long long*>(h->stats.p);
   const bool checked = tol > 0.0;
-  // X_0 = FP32 solve of (float) B
-  CUDA_TRY(launch_cast_d2f(d_b, r32, count, s));
-  ST_TRY(solve_typed<float>(h, h->v32, rhs, layout, r32, d32, s, nullptr, false));
-  CUDA_TRY(cudaMemsetAsync(stats, 0, 2 * sizeof(unsigned long long), s));
-  CUDA_TRY(launch_update(d_x, d32, count, stats, true, s));
   double prev = 0.0, xmax = 0.0, estimate = NAN;
-  unsigned long long host_stats[2] = {0, 0};
-  if (checked) {
-    CUDA_TRY(cudaMemcpyAsync(host_stats, stats, sizeof(host_stats), cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(cudaStreamSynchronize(s));
-    std::memcpy(&prev, &host_stats[1], sizeof(double));
-    xmax = prev;
-  }
-  int it = 0;
+  unsigned long long host_stats[3] = {0, 0, 0};
+  int it = 0, first = 1;
   bool converged = false;
-  for (it = 1; it <= max_iter; ++it) {
+  ExecConfig fc = pick_config(h, rhs);
+  if (h->fused_refine && fc.sched == SCHED_PULL && !fc.exact && rhs <= 64) {
+    // X_0, the FP64 residual and the first FP32 correction in one pass: X = X_0 + D_1
+    if (rhs == 1 && fc.wsync_batch == 0) fc.wsync_batch = (long long)(h->nnz - h->n) > 3LL * (long long)h->n ? 1 : 2;
+    // level order: one CTA of 256 threads per SM up to 4 right-hand sides, three
+    // beyond (measured on the 1M-row band and power-law systems; the pass reads
+    // more per dependency than a plain solve, and fewer polling warps paid)
+    if (h->sched_option == SCHED_AUTO && planned(h, SPTRSV_OPTION_CTAS_PER_SM) && h->layout_block >= h->n)
+      fc.ctas_per_sm = rhs <= 4 ? 1 : 3;
+    ST_TRY(ensure_buf(h, h->xw, sizeof(unsigned long long) * count, 0, s));
+    CUDA_TRY(cudaMemsetAsync(h->xw.p, 0xFF, sizeof(unsigned long long) * count, s));
+    CUDA_TRY(cudaMemsetAsync(stats, 0, 3 * sizeof(unsigned long long), s));
+    h->last_sched = SCHED_PULL;
+    h->last_pipe = false;
+    if (h->profile) {
+      if (!h->ev_exec[0]) {
+        CUDA_TRY(cudaEventCreate(&h->ev_exec[0]));
+        CUDA_TRY(cudaEventCreate(&h->ev_exec[1]));
+      }
+      CUDA_TRY(cudaEventRecord(h->ev_exec[0], s));
+    }
+    CUDA_TRY(launch_refine_fused(h->layout, h->v32, h->v64, rhs, d_b, d_x, si, sk,
+                                 static_cast<unsigned long long*>(h->xw.p), stats, h->ctl, fc, timeout_ns(h),
+                                 h->num_sms, s));
+    if (h->profile) {
+      CUDA_TRY(cudaEventRecord(h->ev_exec[1], s));
+      h->ev_recorded = true;
+    }
+    first = 2;
+    it = 1;
+    if (checked) {
+      CUDA_TRY(cudaMemcpyAsync(host_stats, stats, sizeof(host_stats), cudaMemcpyDeviceToHost, s));
+      CUDA_TRY(cudaStreamSynchronize(s));
+      double dmax = 0.0, x0max = 0.0;
+      std::memcpy(&dmax, &host_stats[0], sizeof(double));
+      std::memcpy(&xmax, &host_stats[1], sizeof(double));
+      std::memcpy(&x0max, &host_stats[2], sizeof(double));
+      // D_0 = X_0, D_1 = the fused correction
+      estimate = (x0max > 0.0 && xmax > 0.0) ? dmax * (dmax / x0max) / xmax : (dmax == 0.0 ? 0.0 : INFINITY);
+      converged = estimate <= tol;
+      prev = dmax;
+    }
+  } else {
+    // X_0 = FP32 solve of (float) B
+    CUDA_TRY(launch_cast_d2f(d_b, r32, count, s));
+    ST_TRY(solve_typed<float>(h, h->v32, rhs, layout, r32, d32, s, nullptr, false));
+    CUDA_TRY(cudaMemsetAsync(stats, 0, 2 * sizeof(unsigned long long), s));
+    CUDA_TRY(launch_update(d_x, d32, count, stats, true, s));
+    if (checked) {
+      CUDA_TRY(cudaMemcpyAsync(host_stats, stats, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+      CUDA_TRY(cudaStreamSynchronize(s));
+      std::memcpy(&prev, &host_stats[1], sizeof(double));
+      xmax = prev;
+    }
+  }
+  int steps = first - 1;  // refinement steps done
+  for (it = first; !converged && it <= max_iter; ++it) {
     CUDA_TRY(launch_residual(h->layout, h->v64, rhs, d_b, d_x, si, sk, r32, s));
     ST_TRY(solve_typed<float>(h, h->v32, rhs, layout, r32, d32, s, nullptr, false));
     CUDA_TRY(cudaMemsetAsync(stats, 0, 2 * sizeof(unsigned long long), s));
     CUDA_TRY(launch_update(d_x, d32, count, stats, false, s));
+    steps = it;
     if (!checked) continue;
-    CUDA_TRY(cudaMemcpyAsync(host_stats, stats, sizeof(host_stats), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaMemcpyAsync(host_stats, stats, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
     double dmax = 0.0;
     std::memcpy(&dmax, &host_stats[0], sizeof(double));
@@ -1647,7 +1698,7 @@ int sptrsv_gb300_solve_refine(sptrsv_handle_t h, const double* d_val, int rhs, i
     }
     prev = dmax;
   }
-  if (iters) *iters = it > max_iter ? max_iter : it;
+  if (iters) *iters = steps;
   if (est) *est = estimate;
   if (h->sync_check || checked) ST_TRY(check_device(h, s));
   if (checked && !converged) return SPTRSV_ERR_NOT_CONVERGED;

@@ -1,0 +1,329 @@
+// Fused first refinement step: one pass over the dependency DAG that solves
+// in FP32, forms the FP64 residual and solves the FP32 correction together.
+//
+// Mixed-precision refinement solves L x0 = b in FP32, forms r = b - L x0 in
+// FP64 and solves L d = r in FP32, then x = x0 + d. All three walk the same
+// DAG, and at position p everything they need is final as soon as the
+// dependencies of p are: x0_j and d_j of every dependency j, and x0_p itself.
+// So one sync-free pass does all three. With w = L(p,j)/L(p,p) (FP32 and FP64
+// copies, ready order) and rho = r/L(p,p):
+//
+//   x0_p  = b_p/d_p - sum_j w32_j x0_j                     (FP32)
+//   rho_p = b_p/d_p - x0_p - sum_j w64_j x0_j              (FP64, x0_j exact in FP64)
+//   d_p   = RN32(rho_p) - sum_j w32_j d_j                  (FP32)
+//   x_p   = x0_p + d_p                                     (FP64)
+//
+// Position p publishes the pair (x0_p, d_p) as one 64-bit value-as-flag word
+// (low half x0, high half d; all ones = not yet published), so a dependency
+// costs one poll, exactly as in a single solve. These are the separate
+// passes' operations on the same operands: the FP32 solves and the FP64
+// residual round exactly as they do there, only the residual is scaled by
+// 1/L(p,p) before it is rounded to FP32.
+//
+// Lanes and lockstep as in the warp-synchronous many-rhs executor: G lanes per
+// unknown (32/G unknowns per warp), each lane covering RPL right-hand sides,
+// UD dependencies loaded per batch; a group moves to its next batch once all
+// its lanes consumed the current one. In-chunk dependencies resolve through
+// shared memory when the chunk's words fit. Every wait is bounded.
+//
+// stats (non-negative doubles as ordered bit patterns, max over the pass):
+// [0] max |d|, [1] max |x|, [2] max |x0| -- the refinement's stopping estimate.
+#include "exec_common.cuh"
+#include "internal.h"
+
+namespace sptrsv {
+
+namespace {
+
+constexpr unsigned long long kPairEmpty = 0xFFFFFFFFFFFFFFFFull;
+constexpr unsigned long long kPairNaN = 0x7FC000007FC00000ull;
+
+struct RefineArgs {
+  int n, rhs, chunk, nchunks, smem_tier, ctas_per_sm;
+  const int* perm;
+  const int* dep_ptr;
+  const int* dep_pos_f;
+  const float* w32;
+  const double* w64;
+  const float* rcp32;
+  const double* rcp64;
+  const double* b;
+  double* x;
+  long long b_si, b_sk, x_si, x_sk;
+  unsigned long long* xw;     // [n * rhs] (x0, d) pairs, position-major
+  unsigned long long* stats;  // [3]
+  DeviceCtl* ctl;
+  unsigned long long timeout_ns;
+  unsigned sleep_min, sleep_max;  // backoff of global polls (ns)
+};
+
+__device__ __forceinline__ unsigned long long pack_pair(float x0, float d) {
+  const unsigned long long v = (static_cast<unsigned long long>(__float_as_uint(d)) << 32) |
+                               static_cast<unsigned long long>(__float_as_uint(x0));
+  return v == kPairEmpty ? kPairNaN : v;
+}
+__device__ __forceinline__ float pair_x0(unsigned long long v) {
+  return __uint_as_float(static_cast<unsigned>(v & 0xFFFFFFFFull));
+}
+__device__ __forceinline__ float pair_d(unsigned long long v) { return __uint_as_float(static_cast<unsigned>(v >> 32)); }
+
+// Exact FP32 -> FP64 widening from the IEEE 754 bit fields (sign kept,
+// exponent re-biased from 127 to 1023, 23-bit fraction shifted into the top of
+// the 52-bit one), on the integer pipe: FP64 instructions are scarce on this
+// GPU, and the fused pass widens every FP32 value it reads. Subnormal, infinite
+// and NaN inputs take the hardware conversion.
+__device__ __forceinline__ double widen(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned ex = (u >> 23) & 0xFFu, man = u & 0x7FFFFFu;
+  if (ex == 0xFFu || (ex == 0u && man != 0u)) return static_cast<double>(f);
+  const unsigned hi = (u & 0x80000000u) | (ex != 0u ? (ex + 896u) << 20 : 0u) | (man >> 3);
+  return __hiloint2double(static_cast<int>(hi), static_cast<int>(man << 29));
+}
+
+__device__ __forceinline__ unsigned long long ld_shared_u64(const unsigned long long* p) {
+  return *reinterpret_cast<const volatile unsigned long long*>(p);
+}
+__device__ __forceinline__ void st_shared_u64(unsigned long long* p, unsigned long long v) {
+  *reinterpret_cast<volatile unsigned long long*>(p) = v;
+}
+
+__device__ __forceinline__ void stats_max(unsigned long long* p, float v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0)
+    atomicMax(p, static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(v))));
+}
+
+template <int G, int RPL, int UD>
+__global__ void __launch_bounds__(256) k_pull_refine1(RefineArgs a) {
+  using Bits = unsigned long long;
+  constexpr int P = 32 / G;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Bits* s_x = reinterpret_cast<Bits*>(smem_raw);
+  __shared__ unsigned s_chunk;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int gi = lane / G, gl = lane % G;
+  const unsigned gmask = G >= 32 ? 0xffffffffu : ((1u << G) - 1u) << (lane & ~(G - 1));
+  const int rhs = a.rhs;
+  // stopping-estimate maxima, kept in FP32 (the estimate needs no more)
+  float mx_d = 0.f, mx_x = 0.f, mx_x0 = 0.f;
+  for (;;) {
+    const unsigned c = next_chunk(a.ctl, a.nchunks, &s_chunk);
+    if (c >= (unsigned)a.nchunks) break;
+    const int base = static_cast<int>(c) * a.chunk;
+    const int len = min(base + a.chunk, a.n) - base;
+    if (a.smem_tier)
+      for (long long i = threadIdx.x; i < (long long)len * rhs; i += blockDim.x) s_x[i] = kPairEmpty;
+    __syncthreads();
+    bool fail = false;
+    for (int seg = warp; seg * P < len && !fail; seg += nwarps) {
+      const int j = seg * P + gi;
+      bool done = j >= len;  // group-uniform
+      const int p = base + j;
+      int row = 0, e = 0, e1 = 0;
+      float acc0[RPL], accd[RPL];
+      double res[RPL];
+#pragma unroll
+      for (int r = 0; r < RPL; ++r) {
+        acc0[r] = 0.f;
+        accd[r] = 0.f;
+        res[r] = 0.0;
+      }
+      if (!done) {
+        row = a.perm[p];
+        e = a.dep_ptr[p];
+        e1 = a.dep_ptr[p + 1];
+        const float s32 = a.rcp32[p];
+        const double s64 = a.rcp64[p];
+#pragma unroll
+        for (int r = 0; r < RPL; ++r) {
+          const int k = gl + r * G;
+          if (k < rhs) {
+            const double bv = a.b[(long long)row * a.b_si + (long long)k * a.b_sk];
+            acc0[r] = static_cast<float>(bv) * s32;
+            res[r] = bv * s64;
+          }
+        }
+      }
+      int q[UD], sl[UD];
+      float w32[UD];
+      double w64[UD];
+      Bits bits[UD][RPL];
+      unsigned todo = 0u;
+      auto load_batch = [&]() {
+        todo = 0u;
+#pragma unroll
+        for (int u = 0; u < UD; ++u) {
+          const bool in = e + u < e1;
+          q[u] = in ? a.dep_pos_f[e + u] : -1;
+          w32[u] = in ? a.w32[e + u] : 0.f;
+          w64[u] = in ? a.w64[e + u] : 0.0;
+          sl[u] = (q[u] >= 0 && a.smem_tier && q[u] >= base) ? q[u] - base : -1;
+#pragma unroll
+          for (int r = 0; r < RPL; ++r) {
+            const int k = gl + r * G;
+            bits[u][r] = kPairEmpty;
+            if (q[u] >= 0 && k < rhs) {
+              bits[u][r] = sl[u] >= 0 ? ld_shared_u64(&s_x[(long long)sl[u] * rhs + k])
+                                      : ld_relaxed_u64(&a.xw[(long long)q[u] * rhs + k]);
+              todo |= 1u << (u * RPL + r);
+            }
+          }
+        }
+      };
+      if (!done) load_batch();
+      WaitBudget wb(a.timeout_ns);
+      unsigned nap = a.sleep_min, idle = 0u;
+      for (;;) {
+        bool progress = false, global_wait = false;
+        if (!done) {
+#pragma unroll
+          for (int r = 0; r < RPL; ++r)
+#pragma unroll
+            for (int u = 0; u < UD; ++u) {
+              const unsigned bit = 1u << (u * RPL + r);
+              if (!(todo & bit)) continue;
+              if (bits[u][r] != kPairEmpty) {
+                const float xj = pair_x0(bits[u][r]);
+                acc0[r] = fmaf(-w32[u], xj, acc0[r]);
+                res[r] = fma(-w64[u], widen(xj), res[r]);
+                accd[r] = fmaf(-w32[u], pair_d(bits[u][r]), accd[r]);
+                todo &= ~bit;
+                progress = true;
+              } else if (sl[u] < 0) {
+                global_wait = true;
+              }
+            }
+        }
+        const unsigned clear = __ballot_sync(0xffffffffu, done || todo == 0u);
+        const bool group_clear = (clear & gmask) == gmask;
+        if (!done) {
+          if (group_clear) {
+            e += UD;
+            if (e < e1) {
+              load_batch();
+            } else {
+#pragma unroll
+              for (int r = 0; r < RPL; ++r) {
+                const int k = gl + r * G;
+                if (k < rhs) {
+                  const float x0 = acc0[r];
+                  const double x0w = widen(x0);
+                  const float d = static_cast<float>(res[r] - x0w) + accd[r];
+                  const Bits v = pack_pair(x0, d);
+                  if (a.smem_tier) st_shared_u64(&s_x[(long long)j * rhs + k], v);
+                  st_relaxed_u64(&a.xw[(long long)p * rhs + k], v);
+                  a.x[(long long)row * a.x_si + (long long)k * a.x_sk] = x0w + widen(d);
+                  mx_d = fmaxf(mx_d, fabsf(d));
+                  mx_x = fmaxf(mx_x, fabsf(x0 + d));
+                  mx_x0 = fmaxf(mx_x0, fabsf(x0));
+                }
+              }
+              done = true;
+            }
+            progress = true;
+          } else {
+#pragma unroll
+            for (int u = 0; u < UD; ++u)
+#pragma unroll
+              for (int r = 0; r < RPL; ++r) {
+                const int k = gl + r * G;
+                if ((todo & (1u << (u * RPL + r))) && bits[u][r] == kPairEmpty)
+                  bits[u][r] = sl[u] >= 0 ? ld_shared_u64(&s_x[(long long)sl[u] * rhs + k])
+                                          : ld_relaxed_u64(&a.xw[(long long)q[u] * rhs + k]);
+              }
+          }
+        }
+        if (__all_sync(0xffffffffu, done)) break;
+        const bool any_progress = __any_sync(0xffffffffu, progress);
+        const bool any_global = __any_sync(0xffffffffu, global_wait);
+        __syncwarp();
+        if (!any_progress) {
+          if (any_global && a.sleep_max) {
+            __nanosleep(nap);
+            nap = nap * 2u < a.sleep_max ? nap * 2u : a.sleep_max;
+          }
+          if ((any_global || (++idle & 255u) == 0u) && !wb.poll(a.ctl, p)) fail = true;
+          if (__any_sync(0xffffffffu, fail)) {
+            fail = true;
+            break;
+          }
+        } else {
+          nap = a.sleep_min;
+        }
+      }
+    }
+    if (__syncthreads_or(fail)) break;
+  }
+  stats_max(&a.stats[0], mx_d);
+  stats_max(&a.stats[1], mx_x);
+  stats_max(&a.stats[2], mx_x0);
+  leave(a.ctl);
+}
+
+template <int G, int RPL, int UD>
+cudaError_t run_refine1(const RefineArgs& a, int block, size_t smem, int num_sms, cudaStream_t s) {
+  auto kernel = k_pull_refine1<G, RPL, UD>;
+  if (smem > 48 * 1024) {
+    const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
+  if (per_sm < 1) per_sm = 1;
+  if (a.ctas_per_sm > 0 && per_sm > a.ctas_per_sm) per_sm = a.ctas_per_sm;
+  long long grid = (long long)num_sms * per_sm;
+  if (grid > a.nchunks) grid = a.nchunks;
+  if (grid < 1) grid = 1;
+  kernel<<<static_cast<int>(grid), block, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_refine_fused(const Layout& L, const Values<float>& v32, const Values<double>& v64, int rhs,
+                                const double* b, double* x, long long si, long long sk, unsigned long long* xw,
+                                unsigned long long* stats, DeviceCtl* ctl, const ExecConfig& cfg,
+                                unsigned long long timeout_ns, int num_sms, cudaStream_t s) {
+  if (L.n == 0) return cudaSuccess;
+  if (rhs < 1 || rhs > 64) return cudaErrorInvalidValue;
+  RefineArgs a{};
+  a.n = L.n;
+  a.rhs = rhs;
+  a.chunk = cfg.chunk > 0 ? cfg.chunk : 256;
+  a.nchunks = (L.n + a.chunk - 1) / a.chunk;
+  a.ctas_per_sm = cfg.ctas_per_sm;
+  a.perm = L.perm;
+  a.dep_ptr = L.dep_ptr;
+  a.dep_pos_f = L.dep_pos_f;
+  a.w32 = v32.dep_w;
+  a.w64 = v64.dep_w;
+  a.rcp32 = v32.rcp;
+  a.rcp64 = v64.rcp;
+  a.b = b;
+  a.x = x;
+  a.b_si = a.x_si = si;
+  a.b_sk = a.x_sk = sk;
+  a.xw = xw;
+  a.stats = stats;
+  a.ctl = ctl;
+  a.timeout_ns = timeout_ns;
+  a.sleep_min = cfg.sleep_max ? 16u : 0u;
+  a.sleep_max = cfg.sleep_max;
+  size_t smem = 0;
+  if (cfg.smem_tier) {
+    smem = (size_t)a.chunk * (size_t)rhs * sizeof(unsigned long long);
+    if (smem <= 200 * 1024) a.smem_tier = 1;
+    else smem = 0;
+  }
+  const int block = cfg.block;
+  const int ud = cfg.wsync_batch == 1 ? 1 : 2;
+  if (rhs == 1) return ud == 1 ? run_refine1<1, 1, 1>(a, block, smem, num_sms, s)
+                               : run_refine1<1, 1, 2>(a, block, smem, num_sms, s);
+  if (rhs <= 4) return run_refine1<4, 1, 2>(a, block, smem, num_sms, s);
+  if (rhs <= 8) return run_refine1<8, 1, 2>(a, block, smem, num_sms, s);
+  if (rhs <= 16) return run_refine1<16, 1, 2>(a, block, smem, num_sms, s);
+  if (rhs <= 32) return run_refine1<32, 1, 2>(a, block, smem, num_sms, s);
+  return run_refine1<32, 2, 2>(a, block, smem, num_sms, s);
+}
+
+}  // namespace sptrsv

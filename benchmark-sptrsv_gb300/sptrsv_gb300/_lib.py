@@ -62,6 +62,7 @@ OPTION_SPLIT = 17
 OPTION_WSYNC_BATCH = 18
 OPTION_IMPORT = 19
 OPTION_UNIT_PIPELINE = 20
+OPTION_FUSED_REFINE = 21
 
 NOALLOC_MAX_N = 262144  # SPTRSV_NOALLOC_MAX_N
 

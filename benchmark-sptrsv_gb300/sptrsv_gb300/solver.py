@@ -106,7 +106,7 @@ class SyncFreeSolver:
                  staged: bool | None = None, stage_entries: int | None = None, stages: int | None = None,
                  warp_sync: bool | None = None, split: int | None = None, wsync_batch: int | None = None,
                  import_deps: bool | None = None, unit_pipeline: int | None = None, fused_grad: bool | None = None,
-                 stream=None):
+                 fused_refine: bool | None = None, stream=None):
         torch = _torch()
         self._lib = load()
         self.device = torch.device("cuda", torch.cuda.current_device())
@@ -150,7 +150,7 @@ class SyncFreeSolver:
                        (_lib.OPTION_WARP_SYNC, warp_sync), (_lib.OPTION_SPLIT, split),
                        (_lib.OPTION_WSYNC_BATCH, wsync_batch), (_lib.OPTION_IMPORT, import_deps),
                        (_lib.OPTION_UNIT_PIPELINE, unit_pipeline),
-                       (_lib.OPTION_FUSED_GRAD, fused_grad)):
+                       (_lib.OPTION_FUSED_GRAD, fused_grad), (_lib.OPTION_FUSED_REFINE, fused_refine)):
             if v is not None:
                 self.set_option(opt, int(v))
         self._stream = stream
@@ -236,7 +236,9 @@ class SyncFreeSolver:
 
     def solve_refine(self, b, values=None, *, tol: float = 1e-12, max_iter: int = 10, out=None):
         """FP32 storage/solve + FP64-residual iterative refinement (b float64). Returns
-        (x, iterations, estimated relative forward error)."""
+        (x, iterations, estimated relative forward error). With the default
+        ``fused_refine`` the first FP32 solve, FP64 residual and FP32 correction run
+        as one pass over the dependency DAG."""
         torch = _torch()
         b2, layout = self._layout_of(b)
         if b2.dtype != torch.float64:

@@ -109,13 +109,17 @@ typedef enum sptrsv_option {
   SPTRSV_OPTION_IMPORT = 19,      /* 1 (default): warp-synchronous one-rhs forward pull on a blocked
                                      layout (chunk = order block) gives each CTA an importer warp that
                                      copies the chunk's external dependencies into shared memory */
-  SPTRSV_OPTION_UNIT_PIPELINE = 20 /* warp-synchronous one-rhs forward pull on a blocked layout (chunk =
+  SPTRSV_OPTION_UNIT_PIPELINE = 20, /* warp-synchronous one-rhs forward pull on a blocked layout (chunk =
                                      order block): 1 = one consumer warp per unit reading every operand
                                      from shared memory, fed by a bulk-copy loader warp (stages of
                                      SPTRSV_OPTION_STAGE_ENTRIES entries, default 2048, in
                                      SPTRSV_OPTION_STAGES buffers, default 3) and an importer warp, with
                                      a ring of up to 8192 value slots per unit; a power of two from 128
                                      to 8192 = that ring size cap; 0 (default) = off */
+  SPTRSV_OPTION_FUSED_REFINE = 21 /* sptrsv_gb300_solve_refine: 1 (default) = the FP32 solve, the FP64
+                                     residual and the FP32 correction of the first refinement step run
+                                     as one pass over the dependency DAG (pull schedules, rhs <= 64);
+                                     0 = separate passes */
 } sptrsv_option;
 
 typedef struct sptrsv_info {
@@ -246,7 +250,11 @@ int sptrsv_gb300_solve(sptrsv_handle_t handle, const void *d_val, int dtype, int
  * accumulation, accuracy recovered by iterative refinement in which only the
  * residual R = B - L X (from the FP64 values) and the update X += D run in
  * FP64. b and x are FP64 (layout as in sptrsv_gb300_solve); d_val is FP64 (or
- * NULL for the staged FP64 values). Stops when the estimated relative forward
+ * NULL for the staged FP64 values). With SPTRSV_OPTION_FUSED_REFINE (default)
+ * the first solve and the first correction share one sync-free pass: each
+ * unknown publishes its FP32 value and its FP32 correction together, so the
+ * step costs one walk of the dependency chain instead of two; further steps
+ * run as separate residual, solve and update passes. Stops when the estimated relative forward
  * error ||D_k||^2 / (||D_{k-1}|| ||X||) (max norms; D_0 = X_0) is at most
  * `tol`, after at least one refinement step and at most `max_iter`; tol <= 0
  * runs exactly max_iter steps without reading anything back (asynchronous,

@@ -19,13 +19,14 @@ def relerr(x, ref):
 
 
 @pytest.mark.parametrize("name", golden_names())
-@pytest.mark.parametrize("schedule", [1, 2, 3])
-def test_refined_forward_error(cuda, name, schedule):
+@pytest.mark.parametrize("schedule,fused", [(0, True), (0, False), (1, True), (2, True), (2, False), (3, True)])
+def test_refined_forward_error(cuda, name, schedule, fused):
     from sptrsv_gb300 import SyncFreeSolver
     g = load_golden(name)
     n, rhs = int(g["n"]), int(g["rhs"])
     sub = 0 if int(g["lower"]) else 1
-    s = SyncFreeSolver(g["col_ptr"], g["row_idx"], n, sub, values=g["val"], schedule=schedule)
+    s = SyncFreeSolver(g["col_ptr"], g["row_idx"], n, sub, values=g["val"], schedule=schedule,
+                       fused_refine=fused)
     b = cuda.from_numpy(g["b"].reshape(n, rhs)).cuda()
     x, iters, est = s.solve_refine(b)
     assert 1 <= iters <= 4
@@ -58,3 +59,67 @@ def test_refine_reports_non_convergence(cuda):
     with pytest.raises(SptrsvError) as ei:
         s.solve_refine(b, tol=1e-300, max_iter=1)
     assert ei.value.status == _lib.ERR_NOT_CONVERGED
+
+
+def _fused_cases():
+    from sptrsv_gb300 import matgen
+    return {
+        "band_fwd": lambda: matgen.poisson_band(30_000, 9.0, 3000, seed=11),
+        "band_bwd": lambda: matgen.poisson_band(30_000, 9.0, 3000, seed=12, lower=False),
+        "powerlaw_fwd": lambda: matgen.system_powerlaw_4m(seed=1, n=60_000, target_nnz=600_000),
+        "powerlaw_bwd": lambda: matgen.system_powerlaw_4m(seed=1, n=60_000, target_nnz=600_000).transpose(),
+        # deep and narrow: the automatic plan picks a blocked layout
+        "laplace_fwd": lambda: matgen.laplace2d_lower(300),
+        "laplace_bwd": lambda: matgen.laplace2d_lower(300).transpose(),
+    }
+
+
+@pytest.mark.parametrize("case", list(_fused_cases()))
+@pytest.mark.parametrize("rhs", [1, 3, 16, 64])
+def test_fused_first_step_against_oracle(cuda, oracle_port, case, rhs):
+    """The fused pass (FP32 solve, FP64 residual and FP32 correction in one walk of
+    the DAG) reaches the 1e-10 forward error in its single step on these diagonally
+    dominant systems, like the separate passes do, for row- and column-major blocks."""
+    from sptrsv_gb300 import SyncFreeSolver
+    m = _fused_cases()[case]()
+    B = np.random.default_rng(rhs).standard_normal((m.n, rhs))
+    ref = oracle_port.solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, B)
+    results = {}
+    for fused in (True, False):
+        s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, values=m.val, fused_refine=fused)
+        for layout in ("row", "col"):
+            b = cuda.from_numpy(B).cuda()
+            if layout == "col":
+                b = cuda.from_numpy(np.ascontiguousarray(B.T)).cuda().t()
+            x, iters, est = s.solve_refine(b, tol=1e-12)
+            assert relerr(x.cpu().numpy(), ref) <= TOL_FWD, (fused, layout)
+            assert 1 <= iters <= 3 and est <= 1e-12
+            # fixed-step mode: no read-back, same result after the same number of steps
+            x2, it2, _ = s.solve_refine(b, tol=0.0, max_iter=iters)
+            assert it2 == iters
+            assert relerr(x2.cpu().numpy(), ref) <= TOL_FWD
+            results[(fused, layout)] = (x.cpu().numpy(), iters)
+        s.close()
+    assert results[(True, "row")][1] == 1
+    # the fused step and the separate passes agree to well below the tolerance
+    assert relerr(results[(True, "row")][0], results[(False, "row")][0]) <= TOL_FWD
+
+
+def test_fused_refine_more_steps_and_option(cuda, oracle_port):
+    """max_iter > 1 continues with separate passes after the fused step; the option
+    round-trips and 0 selects the separate passes."""
+    from sptrsv_gb300 import SyncFreeSolver, _lib, matgen
+    m = matgen.poisson_band(8000, 8.0, 800, seed=13)
+    B = np.random.default_rng(3).standard_normal((m.n, 2))
+    ref = oracle_port.solve(m.col_ptr, m.row_idx, m.val, m.n, 0, B)
+    s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, 0, values=m.val)
+    assert s.get_option(_lib.OPTION_FUSED_REFINE) == 1
+    b = cuda.from_numpy(B).cuda()
+    for steps in (1, 2, 3):
+        x, it, _ = s.solve_refine(b, tol=0.0, max_iter=steps)
+        assert it == steps
+        assert relerr(x.cpu().numpy(), ref) <= TOL_FWD
+    s.set_option(_lib.OPTION_FUSED_REFINE, 0)
+    assert s.get_option(_lib.OPTION_FUSED_REFINE) == 0
+    x, it, _ = s.solve_refine(b)
+    assert relerr(x.cpu().numpy(), ref) <= TOL_FWD
