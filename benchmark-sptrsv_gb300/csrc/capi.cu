@@ -1624,7 +1624,14 @@ int sptrsv_gb300_solve_refine(sptrsv_handle_t h, const double* d_val, int rhs, i
   int it = 0, first = 1;
   bool converged = false;
   ExecConfig fc = pick_config(h, rhs);
-  if (h->fused_refine && fc.sched == SCHED_PULL && !fc.exact && rhs <= 64) {
+  bool fuse = h->fused_refine && fc.sched == SCHED_PULL && !fc.exact && rhs <= 64;
+  if (fuse && rhs == 1) {
+    // the fused pass gives every unknown one lane: where the plain solve would
+    // spread long lists over lanes (split executor), separate passes are faster
+    const int split = planned(h, SPTRSV_OPTION_SPLIT) ? h->plan.split_fwd : fc.split;
+    if (split > 0 && h->max_dep_cnt > split) fuse = false;
+  }
+  if (fuse) {
     // X_0, the FP64 residual and the first FP32 correction in one pass: X = X_0 + D_1
     if (rhs == 1 && fc.wsync_batch == 0) fc.wsync_batch = (long long)(h->nnz - h->n) > 3LL * (long long)h->n ? 1 : 2;
     // level order: one CTA of 256 threads per SM up to 4 right-hand sides, three

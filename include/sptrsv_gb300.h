@@ -118,8 +118,9 @@ typedef enum sptrsv_option {
                                      to 8192 = that ring size cap; 0 (default) = off */
   SPTRSV_OPTION_FUSED_REFINE = 21 /* sptrsv_gb300_solve_refine: 1 (default) = the FP32 solve, the FP64
                                      residual and the FP32 correction of the first refinement step run
-                                     as one pass over the dependency DAG (pull schedules, rhs <= 64);
-                                     0 = separate passes */
+                                     as one pass over the dependency DAG (pull schedules, rhs <= 64,
+                                     and for one rhs only where no dependency list is split over
+                                     lanes); 0 = separate passes */
 } sptrsv_option;
 
 typedef struct sptrsv_info {
