@@ -270,6 +270,29 @@ def reference_scheme_ms(cases, dev, reps: int = 3) -> dict:
     return out
 
 
+def hop_latency(dev, n: int = 8192, reps: int = 9) -> dict:
+    """Per-hop latency of this library's executor, measured on a chain (unknown j
+    feeds j+1 only, n levels): one unknown per chunk puts every hop through global
+    memory (publish, L2, poll by another CTA); one chunk for the whole chain puts
+    every hop through the CTA's shared memory. nlevels x t_hop is the floor of a
+    solve whose hops all take that path."""
+    import torch
+
+    from sptrsv_gb300 import SyncFreeSolver, matgen
+    m = matgen.chain(n)
+    b = torch.from_numpy(m.matvec(np.ones(n))).to(dev)
+    out = {}
+    for name, chunk in (("global", 1), ("smem", n)):
+        s = SyncFreeSolver(m.col_ptr, m.row_idx, n, 0, values=m.val, schedule=2, staged=False, warp_sync=True,
+                           order_block=2**31 - 1, chunk=chunk, sync_check=False)
+        x = s.solve(b)
+        ms = _timed(lambda: s.solve(b, out=x), reps)
+        s.check()
+        out[name] = 1e3 * ms / n
+        s.close()
+    return out
+
+
 def run_gpu(args, world, rank, local):
     import torch
 
@@ -400,6 +423,9 @@ def run_gpu(args, world, rank, local):
     # bounded waits, through the kernel-level C-ABI surface
     ref_scheme = reference_scheme_ms(cases, dev) if not args.no_ref_scheme else {}
 
+    # latency floor: nlevels x the per-hop latency of the path the schedule's hops take
+    # (global memory in level order, shared memory inside the blocks of a blocked order)
+    hop = hop_latency(dev)
     # roofline of the dominant kernel (the executor on the case with the largest share)
     peak, peak_kind = read_peaks()
     dom = max(cases, key=lambda c: statistics.mean(exec_ms[c["name"]]))
@@ -418,6 +444,11 @@ def run_gpu(args, world, rank, local):
             "us_per_level": round(1e3 * ems / max(info[c["name"]]["nlevels"], 1), 3),
             "max_abs_err": errs[c["name"]], "analysis_ms": round(info[c["name"]]["analysis_ms"], 2),
         }
+        blocked = info[c["name"]]["order_block"] < c["m"].n
+        floor_ms = info[c["name"]]["nlevels"] * hop["smem" if blocked else "global"] * 1e-3
+        details[c["name"]]["latency_floor_ms"] = round(floor_ms, 4)
+        details[c["name"]]["floor_path"] = "shared memory (blocked order)" if blocked else "global memory (level order)"
+        details[c["name"]]["exec_over_floor"] = round(ems / floor_ms, 2) if floor_ms > 0 else None
         if c["name"] in ref_scheme:
             details[c["name"]]["reference_scheme_ms"] = round(ref_scheme[c["name"]], 4)
             details[c["name"]]["speedup_vs_reference_scheme"] = round(ref_scheme[c["name"]] / ms, 2)
@@ -438,6 +469,11 @@ def run_gpu(args, world, rank, local):
                      "traffic_unit": "bytes per launch (DRAM read + write)",
                      "traffic_source": TRAFFIC_SOURCE if traffic_bytes(dom) else None,
                      "kernel": f"executor on {dom['name']}", "peak_source": peak_kind},
+        "latency_floor": {"t_hop_global_us": round(hop["global"], 4), "t_hop_smem_us": round(hop["smem"], 4),
+                          "floor_ms_per_step": round(sum(d["latency_floor_ms"] for d in details.values()), 4),
+                          "how": "chain of 8,192 unknowns: one unknown per chunk (every hop through global "
+                                 "memory) and one chunk for the chain (every hop through shared memory); "
+                                 "floor = nlevels x t_hop of the path the case's schedule uses"},
         "cpu_baseline": cpu,
         "e2e": {"value": round(e2e_val, 3), "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": round(e2e_step, 4)},
