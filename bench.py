@@ -617,6 +617,15 @@ def run_batch(args):
     xr, iters, est = s.solve_refine(b)
     s.set_option(7, 0)
     t_mixed = _timed(lambda: s.solve_refine(b, out=xr, tol=0.0, max_iter=iters), args.steps, flush)
+    # the same refinement captured once in a CUDA graph and replayed
+    xg = torch.empty_like(xr)
+    graph = s.graph(b, xg, kind=1, count=iters)
+    graph.replay()
+    s.check()
+    t_graph = _timed(graph.replay, args.steps, flush)
+    s.check()
+    graph_err = float((xg - xr).abs().max() / xr.abs().max())
+    graph.close()
     x64 = s.solve(b)
     t_b64 = _timed(lambda: s.solve(b, out=x64), args.steps, flush)
     # per-system plain FP64 launches (one handle per system, one launch each)
@@ -641,9 +650,9 @@ def run_batch(args):
         err = max(err, float(np.abs(xr_h[off[k]:off[k + 1]] - ref).max() / np.abs(ref).max()))
     if dist is not None:
         # whole-job time = the slowest rank
-        t = torch.tensor([t_mixed, t_b64, t_per], dtype=torch.float64, device="cuda")
+        t = torch.tensor([t_mixed, t_b64, t_per, t_graph], dtype=torch.float64, device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_mixed, t_b64, t_per = (float(v) for v in t.tolist())
+        t_mixed, t_b64, t_per, t_graph = (float(v) for v in t.tolist())
         tot = torch.tensor([ntot, nnz], dtype=torch.float64, device="cuda")
         dist.all_reduce(tot)
         ntot, nnz = (int(v) for v in tot.tolist())
@@ -659,7 +668,9 @@ def run_batch(args):
             "n_gpus": world, "scaling": "strong" if world > 1 else None,
             "systems": nsys, "n_total": ntot, "nnz_total": nnz, "rhs": rhs,
             "nlevels_batch": s.info()["nlevels"], "tuned": tuned,
-            "mixed_batched_ms": round(t_mixed, 3), "refine_steps": iters, "fp64_batched_ms": round(t_b64, 3),
+            "mixed_batched_ms": round(t_mixed, 3), "refine_steps": iters,
+            "mixed_graph_replay_ms": round(t_graph, 3), "graph_vs_direct_rel_diff": graph_err,
+            "fp64_batched_ms": round(t_b64, 3),
             "fp64_per_system_launches_ms": round(t_per, 3),
             "speedup_vs_per_system_fp64": round(t_per / t_mixed, 2),
             "speedup_vs_batched_fp64": round(t_b64 / t_mixed, 3),
