@@ -123,3 +123,21 @@ def test_fused_refine_more_steps_and_option(cuda, oracle_port):
     assert s.get_option(_lib.OPTION_FUSED_REFINE) == 0
     x, it, _ = s.solve_refine(b)
     assert relerr(x.cpu().numpy(), ref) <= TOL_FWD
+
+
+@pytest.mark.parametrize("case", ["one", "diagonal", "chain", "dense64", "star"])
+def test_fused_refine_edge_structures(cuda, oracle_port, case):
+    """Edge structures through the fused pass: a single unknown, no dependencies at
+    all, a chain (one unknown per level), a dense triangle (one long list per row)
+    and a star (one unknown feeding all others)."""
+    from sptrsv_gb300 import SyncFreeSolver, matgen
+    m = {"one": lambda: matgen.diagonal(1), "diagonal": lambda: matgen.diagonal(5000),
+         "chain": lambda: matgen.chain(3000), "dense64": lambda: matgen.dense_lower(64),
+         "star": lambda: matgen.star(4000)}[case]()
+    for rhs in (1, 5):
+        B = np.random.default_rng(rhs).standard_normal((m.n, rhs))
+        ref = oracle_port.solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, B)
+        s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, values=m.val, fused_refine=True)
+        x, iters, est = s.solve_refine(cuda.from_numpy(B).cuda())
+        assert relerr(x.cpu().numpy(), ref) <= TOL_FWD, (case, rhs)
+        s.close()
