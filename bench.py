@@ -192,12 +192,31 @@ def run_reference(args, world, rank):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD, "rhs": 1, "l2": "inputs > L2 for the power-law system; CPU arm"},
         "cpu_baseline": {"value": round(value, 4), "unit": "GB/s", "cores": threads, "kind": kind,
-                         "sample": sample},
+                         "sample": sample, "host": host_info()},
         "e2e": {"value": round(value, 4), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "max_abs_err_vs_ones": err,
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def host_info() -> dict:
+    """The host the CPU arms ran on: architecture, logical cores, CPU model
+    (/proc/cpuinfo 'model name', or the Arm implementer/part codes)."""
+    import platform
+    model = ""
+    try:
+        fields = {}
+        for ln in open("/proc/cpuinfo"):
+            if ":" in ln:
+                k, v = ln.split(":", 1)
+                fields.setdefault(k.strip(), v.strip())
+        model = fields.get("model name") or (
+            f"implementer {fields.get('CPU implementer', '?')} part {fields.get('CPU part', '?')}"
+            if "CPU part" in fields else "")
+    except OSError:
+        pass
+    return {"machine": platform.machine(), "nproc": os.cpu_count(), "cpu_model": model or platform.processor()}
 
 
 def cpu_baseline_sample(cases):
@@ -219,7 +238,8 @@ def cpu_baseline_sample(cases):
             tot_bytes += bytes_pass(m.n, m.nnz)
             solves += 1
     return {"value": round(tot_bytes / tot_s / 1e9, 4), "unit": "GB/s", "cores": 1, "kind": kind,
-            "sample": f"{solves} serial FP64 solves over the 4 workload systems (~4 s each), 1 thread"}
+            "sample": f"{solves} serial FP64 solves over the 4 workload systems (~4 s each), 1 thread",
+            "host": host_info()}
 
 
 # ------------------------------------------------------------------ GPU arm
