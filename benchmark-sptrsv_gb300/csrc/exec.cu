@@ -567,6 +567,9 @@ __device__ __forceinline__ bool wsync_segment(const ExecArgs<T>& a, T* s_x, int 
     gmask = head ? (ge >= 31 ? kFull : ((2u << ge) - 1u)) & ~((1u << lane) - 1u) : 0u;
     step = valid ? ge - gs + 1 : 1;
   }
+  // the widest unknown of the segment bounds the suffix-sum rounds (most split
+  // lists span a few lanes, so usually one or two rounds instead of five)
+  const unsigned span = SPLIT ? __reduce_max_sync(kFull, static_cast<unsigned>(step)) : 1u;
   const int p = ADJ ? last - walk : walk;
   T acc = T(0);
   if (head) acc = a.b[(long long)row * a.b_si] * a.rcp[p];
@@ -647,9 +650,9 @@ __device__ __forceinline__ bool wsync_segment(const ExecArgs<T>& a, T* s_x, int 
       if (__any_sync(kFull, ready)) {
         T xi = acc;
 #pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
+        for (unsigned off = 1; off < span; off <<= 1) {
           const T t = __shfl_down_sync(kFull, xi, off);
-          if (lane + off <= ge) xi += t;
+          if (lane + static_cast<int>(off) <= ge) xi += t;
         }
         if (ready) {
           publish(xi);
