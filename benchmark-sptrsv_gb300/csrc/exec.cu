@@ -326,11 +326,15 @@ __global__ void __launch_bounds__(256) k_pull_wsync(ExecArgs<T> a) {
                 bits[u] = ls[u] >= 0 ? F::load_shared(&s_x[ls[u]]) : F::load(&a.xw[q[u]]);
           }
         }
-        if (__all_sync(0xffffffffu, done)) break;
-        const bool any_progress = __any_sync(0xffffffffu, progress);
-        const bool any_global = __any_sync(0xffffffffu, global_wait);
-        __syncwarp();
-        if (!any_progress) {
+        // no lane consumed anything: nothing was published, so the completion
+        // vote is skipped
+        if (__any_sync(0xffffffffu, progress)) {
+          if (__all_sync(0xffffffffu, done)) break;
+          __syncwarp();
+          nap = a.sleep_min;
+        } else {
+          const bool any_global = __any_sync(0xffffffffu, global_wait);
+          __syncwarp();
           if (any_global && a.sleep_max) {
             __nanosleep(nap);
             nap = nap * 2u < a.sleep_max ? nap * 2u : a.sleep_max;
@@ -340,8 +344,6 @@ __global__ void __launch_bounds__(256) k_pull_wsync(ExecArgs<T> a) {
             fail = true;
             break;
           }
-        } else {
-          nap = a.sleep_min;
         }
       }
     }
@@ -607,6 +609,7 @@ __device__ __forceinline__ bool wsync_segment(const ExecArgs<T>& a, T* s_x, int 
   };
   bool sdone = !valid;  // slice consumed (one-lane unknowns publish at the same moment)
   bool done = !valid;   // unknown published
+  if (__all_sync(kFull, done)) return false;
   if (!sdone) load_batch();
   WaitBudget wb(a.timeout_ns);
   unsigned nap = a.sleep_min, idle = 0u;
@@ -643,31 +646,35 @@ __device__ __forceinline__ bool wsync_segment(const ExecArgs<T>& a, T* s_x, int 
             bits[u] = ls[u] >= 0 ? F::load_shared(&s_x[ls[u]]) : F::load(&a.xw[q[u]]);
       }
     }
-    if (SPLIT) {
-      // publish every unknown whose slices are all in
-      const unsigned sd = __ballot_sync(kFull, sdone);
-      const bool ready = head && !done && (sd & gmask) == gmask;
-      if (__any_sync(kFull, ready)) {
-        T xi = acc;
-#pragma unroll
-        for (unsigned off = 1; off < span; off <<= 1) {
-          const T t = __shfl_down_sync(kFull, xi, off);
-          if (lane + static_cast<int>(off) <= ge) xi += t;
-        }
-        if (ready) {
-          publish(xi);
-          done = true;
-          progress = true;
-        }
-        const unsigned pub = __ballot_sync(kFull, head && done);
-        if (valid && !head) done = (pub >> gs) & 1u;
-      }
-    }
-    if (__all_sync(kFull, done)) return false;
+    // Nothing consumed in the warp means no slice finished and nothing was
+    // published, so the completion checks (and their warp votes) are skipped.
     const bool any_progress = __any_sync(kFull, progress);
-    const bool any_global = __any_sync(kFull, global_wait);
-    __syncwarp();
-    if (!any_progress) {
+    if (any_progress) {
+      if (SPLIT) {
+        // publish every unknown whose slices are all in
+        const unsigned sd = __ballot_sync(kFull, sdone);
+        const bool ready = head && !done && (sd & gmask) == gmask;
+        if (__any_sync(kFull, ready)) {
+          T xi = acc;
+#pragma unroll
+          for (unsigned off = 1; off < span; off <<= 1) {
+            const T t = __shfl_down_sync(kFull, xi, off);
+            if (lane + static_cast<int>(off) <= ge) xi += t;
+          }
+          if (ready) {
+            publish(xi);
+            done = true;
+          }
+          const unsigned pub = __ballot_sync(kFull, head && done);
+          if (valid && !head) done = (pub >> gs) & 1u;
+        }
+      }
+      if (__all_sync(kFull, done)) return false;
+      __syncwarp();
+      nap = a.sleep_min;
+    } else {
+      const bool any_global = __any_sync(kFull, global_wait);
+      __syncwarp();
       if (any_global && a.sleep_max) {
         __nanosleep(nap);
         nap = nap * 2u < a.sleep_max ? nap * 2u : a.sleep_max;
@@ -675,8 +682,6 @@ __device__ __forceinline__ bool wsync_segment(const ExecArgs<T>& a, T* s_x, int 
       bool fail = false;
       if ((any_global || (++idle & 255u) == 0u) && !wb.poll(a.ctl, p)) fail = true;
       if (__any_sync(kFull, fail)) return true;
-    } else {
-      nap = a.sleep_min;
     }
   }
 }
@@ -864,11 +869,15 @@ __global__ void __launch_bounds__(256) k_pull_wsync_multi(ExecArgs<T> a) {
               }
           }
         }
-        if (__all_sync(0xffffffffu, done)) break;
-        const bool any_progress = __any_sync(0xffffffffu, progress);
-        const bool any_global = __any_sync(0xffffffffu, global_wait);
-        __syncwarp();
-        if (!any_progress) {
+        // no lane consumed anything: nothing was published, so the completion
+        // vote is skipped
+        if (__any_sync(0xffffffffu, progress)) {
+          if (__all_sync(0xffffffffu, done)) break;
+          __syncwarp();
+          nap = a.sleep_min;
+        } else {
+          const bool any_global = __any_sync(0xffffffffu, global_wait);
+          __syncwarp();
           if (any_global && a.sleep_max) {
             __nanosleep(nap);
             nap = nap * 2u < a.sleep_max ? nap * 2u : a.sleep_max;
@@ -878,8 +887,6 @@ __global__ void __launch_bounds__(256) k_pull_wsync_multi(ExecArgs<T> a) {
             fail = true;
             break;
           }
-        } else {
-          nap = a.sleep_min;
         }
       }
     }
