@@ -233,11 +233,15 @@ __global__ void __launch_bounds__(256) k_pull_refine1(RefineArgs a) {
               }
           }
         }
-        if (__all_sync(0xffffffffu, done)) break;
-        const bool any_progress = __any_sync(0xffffffffu, progress);
-        const bool any_global = __any_sync(0xffffffffu, global_wait);
-        __syncwarp();
-        if (!any_progress) {
+        // no lane consumed anything: nothing was published, so the completion
+        // vote is skipped
+        if (__any_sync(0xffffffffu, progress)) {
+          if (__all_sync(0xffffffffu, done)) break;
+          __syncwarp();
+          nap = a.sleep_min;
+        } else {
+          const bool any_global = __any_sync(0xffffffffu, global_wait);
+          __syncwarp();
           if (any_global && a.sleep_max) {
             __nanosleep(nap);
             nap = nap * 2u < a.sleep_max ? nap * 2u : a.sleep_max;
@@ -247,8 +251,6 @@ __global__ void __launch_bounds__(256) k_pull_refine1(RefineArgs a) {
             fail = true;
             break;
           }
-        } else {
-          nap = a.sleep_min;
         }
       }
     }
