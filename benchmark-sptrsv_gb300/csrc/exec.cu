@@ -517,12 +517,13 @@ __global__ void __launch_bounds__(288) k_pull_wsync_imp(ExecArgs<T> a) {
                 if ((todo & (1u << u)) && bits[u] == F::EMPTY) bits[u] = F::load_shared(&s_x[ls[u]]);
             }
           }
-          if (__all_sync(0xffffffffu, done)) break;
-          if (!__any_sync(0xffffffffu, progress) && ((++idle & 255u) == 0u)) {
-            if (__any_sync(0xffffffffu, !wb.poll(a.ctl, p))) {
-              fail = true;
-              break;
-            }
+          // no lane consumed anything: nothing was published, so the
+          // completion vote is skipped
+          if (__any_sync(0xffffffffu, progress)) {
+            if (__all_sync(0xffffffffu, done)) break;
+          } else if (((++idle & 255u) == 0u) && __any_sync(0xffffffffu, !wb.poll(a.ctl, p))) {
+            fail = true;
+            break;
           }
         }
       }
