@@ -1894,7 +1894,7 @@ int sptrsv_gb300_tune(sptrsv_handle_t h, const void* d_val, int dtype, int rhs, 
   } else {
     // chunk 0 = one unknown per lane group
     for (int bo : {64, 512}) cands.push_back({SCHED_PULL, big, 0, 0, bo, 0, 1, 2, 1, 256, sp});
-    cands.push_back({SCHED_PULL, big, 0, 0, 0, 1, 1, 2, 1, 256, sp});
+    for (int ct : {1, 2, 3}) cands.push_back({SCHED_PULL, big, 0, 0, 0, ct, 1, 2, 1, 256, sp});
     for (int ob : {1024, 4096, 16384}) cands.push_back({SCHED_PULL, ob, ob, 0, 0, 0, 1, 2, 1, 256, sp});
     cands.push_back({SCHED_PULL, big, 0, 0, 256, 0, 1, 2, 0, 256, sp});
     cands.push_back({SCHED_LEVELSET, big, 256, 0, 256, 1, 8, 2, 0, 256, sp});
