@@ -57,3 +57,15 @@ def test_invalid_arguments_rejected_on_host(built_lib):
 def test_build_targets_sm103a_only():
     import build as pkg_build
     assert pkg_build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def test_option_constants_match_header():
+    """Every SPTRSV_OPTION_* value in the header has the same number in the binding."""
+    import re
+    from sptrsv_gb300 import _lib
+    text = (ROOT / "include" / "sptrsv_gb300.h").read_text()
+    opts = {m.group(1): int(m.group(2)) for m in re.finditer(r"SPTRSV_OPTION_([A-Z_]+)\s*=\s*(\d+)", text)}
+    assert len(opts) >= 20
+    for name, value in opts.items():
+        assert getattr(_lib, f"OPTION_{name}") == value, name
+    assert sorted(opts.values()) == list(range(len(opts)))
