@@ -15,10 +15,11 @@
 //
 // Position p publishes the pair (x0_p, d_p) as one 64-bit value-as-flag word
 // (low half x0, high half d; all ones = not yet published), so a dependency
-// costs one poll, exactly as in a single solve. These are the separate
-// passes' operations on the same operands: the FP32 solves and the FP64
-// residual round exactly as they do there, only the residual is scaled by
-// 1/L(p,p) before it is rounded to FP32.
+// costs one poll, exactly as in a single solve. The FP32 recurrences are the
+// separate passes' arithmetic; the residual is formed in FP64 from the scaled
+// FP64 weights the FP64 solve uses (so it is r/L(p,p), with the scaling
+// rounded into the weights), which moves it only at the FP64 rounding level,
+// far below the FP32 error it corrects.
 //
 // Lanes and lockstep as in the warp-synchronous many-rhs executor: G lanes per
 // unknown (32/G unknowns per warp), each lane covering RPL right-hand sides,
@@ -26,8 +27,9 @@
 // its lanes consumed the current one. In-chunk dependencies resolve through
 // shared memory when the chunk's words fit. Every wait is bounded.
 //
-// stats (non-negative doubles as ordered bit patterns, max over the pass):
-// [0] max |d|, [1] max |x|, [2] max |x0| -- the refinement's stopping estimate.
+// stats (non-negative doubles as ordered bit patterns, max over the pass,
+// taken in FP32): [0] max |d|, [1] max |x|, [2] max |x0| -- the refinement's
+// stopping estimate.
 #include "exec_common.cuh"
 #include "internal.h"
 
