@@ -557,10 +557,11 @@ __device__ __forceinline__ bool wsync_segment(const ExecArgs<T>& a, T* s_x, int 
   int ge = lane, gs = lane;
   unsigned gmask = 0u;
   int step = 1;  // entries of an unknown split over k lanes interleave: lane j takes j, j+k, j+2k, ...
+  unsigned heads = 0u;  // split segments: first lane of every unknown (warp-uniform)
   if (SPLIT) {
     const int prev = __shfl_up_sync(kFull, walk, 1);
     head = valid && (lane == 0 || prev != walk);
-    const unsigned heads = __ballot_sync(kFull, head);
+    heads = __ballot_sync(kFull, head);
     const unsigned valids = __ballot_sync(kFull, valid);
     // this lane's group: from its head (at or below) to the lane before the next head
     const unsigned above = heads & ~at_or_below;
@@ -610,6 +611,7 @@ __device__ __forceinline__ bool wsync_segment(const ExecArgs<T>& a, T* s_x, int 
   };
   bool sdone = !valid;  // slice consumed (one-lane unknowns publish at the same moment)
   bool done = !valid;   // unknown published
+  unsigned published = 0u;  // split segments: heads of the unknowns published so far (warp-uniform)
   if (__all_sync(kFull, done)) return false;
   if (!sdone) load_batch();
   WaitBudget wb(a.timeout_ns);
@@ -652,25 +654,34 @@ __device__ __forceinline__ bool wsync_segment(const ExecArgs<T>& a, T* s_x, int 
     const bool any_progress = __any_sync(kFull, progress);
     if (any_progress) {
       if (SPLIT) {
-        // publish every unknown whose slices are all in
-        const unsigned sd = __ballot_sync(kFull, sdone);
-        const bool ready = head && !done && (sd & gmask) == gmask;
-        if (__any_sync(kFull, ready)) {
+        // publish every unknown whose slices are all in. Which unknowns are
+        // complete follows from one ballot, worked out identically by every
+        // lane: a segmented OR from each unknown's last lane down to its head
+        // marks the unknowns that still have a lane with its slice pending.
+        const unsigned pending = ~__ballot_sync(kFull, sdone);
+        unsigned v = pending, f = (heads >> 1) | 0x80000000u;  // f: last lane of an unknown
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const unsigned open = ~f;
+          v |= (v >> d) & open;
+          f |= (f >> d) & open;
+        }
+        const unsigned ready = heads & ~v & ~published;
+        if (ready) {
           T xi = acc;
 #pragma unroll
           for (unsigned off = 1; off < span; off <<= 1) {
             const T t = __shfl_down_sync(kFull, xi, off);
             if (lane + static_cast<int>(off) <= ge) xi += t;
           }
-          if (ready) {
-            publish(xi);
-            done = true;
-          }
-          const unsigned pub = __ballot_sync(kFull, head && done);
-          if (valid && !head) done = (pub >> gs) & 1u;
+          if ((ready >> lane) & 1u) publish(xi);
+          published |= ready;
+          if (valid) done = (published >> gs) & 1u;
         }
+        if (published == heads) return false;
+      } else if (__all_sync(kFull, done)) {
+        return false;
       }
-      if (__all_sync(kFull, done)) return false;
       __syncwarp();
       nap = a.sleep_min;
     } else {
