@@ -244,9 +244,9 @@ def cpu_baseline_sample(cases):
 
 # ------------------------------------------------------------------ GPU arm
 # DRAM bytes per stored entry of the split-list executor on the power-law
-# backward system: ncu capture of the 1/4-size case (155.9 MB for 9,474,199
+# backward system: ncu capture of the 1/4-size case (156.0 MB for 9,474,199
 # stored entries; traffic grows with the stored entries), scaled to a launch.
-TRAFFIC_PER_ENTRY = {"powerlaw_bwd": (145.506304e6 + 10.404864e6) / 9474199}
+TRAFFIC_PER_ENTRY = {"powerlaw_bwd": (145.447680e6 + 10.590208e6) / 9474199}
 TRAFFIC_SOURCE = ("ncu --set full capture of k_pull_wsync_split on powerlaw_bwd at 1/4 size, scaled by stored "
                   "entries (profiles/k_pull_wsync_split_powerlaw_bwd.md)")
 
