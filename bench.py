@@ -190,7 +190,8 @@ def run_reference(args, world, rank):
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "GB/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD, "rhs": 1, "l2": "inputs > L2 for the power-law system; CPU arm"},
+        "config": {"workload": WORKLOAD if args.scale == 1.0 else f"{WORKLOAD}, sizes x{args.scale}", "rhs": 1,
+                   "l2": "inputs > L2 for the power-law system; CPU arm"},
         "cpu_baseline": {"value": round(value, 4), "unit": "GB/s", "cores": threads, "kind": kind,
                          "sample": sample, "host": host_info()},
         "e2e": {"value": round(value, 4), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
