@@ -13,10 +13,10 @@ from ._lib import (DTYPE_F32, DTYPE_F64, LAYOUT_COL_MAJOR, LAYOUT_ROW_MAJOR, OPT
 from .solver import SyncFreeSolver, analyser, executor, sptrsv_syncfree_cuda
 
 
-def sparse_triangular_solve(solver, values, b):
+def sparse_triangular_solve(solver, values, b, recompute=False):
     """Differentiable x = op(L)^-1 b (see sptrsv_gb300.autograd)."""
     from .autograd import sparse_triangular_solve as _f
-    return _f(solver, values, b)
+    return _f(solver, values, b, recompute)
 
 __all__ = [
     "matgen", "mtx", "load", "sparse_triangular_solve", "SptrsvError", "SyncFreeSolver", "analyser", "executor", "sptrsv_syncfree_cuda",
