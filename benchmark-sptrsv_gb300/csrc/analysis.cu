@@ -36,15 +36,19 @@ __global__ void k_validate_ptr(const int* __restrict__ col_ptr, int n, int nnz, 
   }
 }
 
-// One thread per column. Requires monotone, in-range column pointers.
-__global__ void k_validate_rows(const int* __restrict__ col_ptr, const int* __restrict__ row_idx, int n,
+// One thread per column. A column whose pointers are not an in-range,
+// non-decreasing pair is flagged SF_BAD_PTR and its rows are not read, so the
+// kernel is safe on any column-pointer array (nnz = length of row_idx).
+__global__ void k_validate_rows(const int* __restrict__ col_ptr, const int* __restrict__ row_idx, int n, int nnz,
                                 SysDesc sd, int* flags) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += stride) {
     const int substitution = dir_of(sd, c);
     const int beg = col_ptr[c], end = col_ptr[c + 1];
     int f = 0;
-    if (beg == end) {
+    if (beg < 0 || end < beg || end > nnz) {
+      f |= SF_BAD_PTR;
+    } else if (beg == end) {
       f |= SF_MISSING_DIAG;
     } else {
       int prev = -1;
@@ -72,10 +76,10 @@ cudaError_t launch_validate_ptr(const int* col_ptr, int n, int nnz, int* flags, 
   k_validate_ptr<<<grid_for((long long)n + 1), kThreads, 0, s>>>(col_ptr, n, nnz, flags);
   return cudaGetLastError();
 }
-cudaError_t launch_validate_rows(const int* col_ptr, const int* row_idx, int n, const SysDesc& sd, int* flags,
-                                 cudaStream_t s) {
+cudaError_t launch_validate_rows(const int* col_ptr, const int* row_idx, int n, int nnz, const SysDesc& sd,
+                                 int* flags, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
-  k_validate_rows<<<grid_for(n), kThreads, 0, s>>>(col_ptr, row_idx, n, sd, flags);
+  k_validate_rows<<<grid_for(n), kThreads, 0, s>>>(col_ptr, row_idx, n, nnz, sd, flags);
   return cudaGetLastError();
 }
 
@@ -158,15 +162,22 @@ cudaError_t launch_nat_rows(const SysDesc& sd, int n, int* rows_nat, cudaStream_
 // ------------------------------------------------------------ in-degree analyser
 // inDeg[row] += 1 for every stored entry, diagonal included
 // (reference: SpTRSV_cuda/sptrsv_syncfree_cuda.h:8-19). The caller zeroes inDeg.
-__global__ void k_in_degree(const int* __restrict__ row_idx, int nnz, int* in_degree) {
+// A row index outside [0, m) is skipped (never written) and, when `bad` is
+// given, raises SF_ROW_RANGE there.
+__global__ void k_in_degree(const int* __restrict__ row_idx, int m, int nnz, int* in_degree, int* bad) {
   const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nnz; e += stride)
-    atomicAdd(&in_degree[row_idx[e]], 1);
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nnz; e += stride) {
+    const int r = row_idx[e];
+    if (static_cast<unsigned>(r) < static_cast<unsigned>(m)) {
+      atomicAdd(&in_degree[r], 1);
+    } else if (bad) {
+      atomicOr(bad, SF_ROW_RANGE);
+    }
+  }
 }
-cudaError_t launch_in_degree(const int* row_idx, int m, int nnz, int* in_degree, cudaStream_t s) {
-  (void)m;
+cudaError_t launch_in_degree(const int* row_idx, int m, int nnz, int* in_degree, cudaStream_t s, int* bad) {
   if (nnz == 0) return cudaSuccess;
-  k_in_degree<<<grid_for(nnz), kThreads, 0, s>>>(row_idx, nnz, in_degree);
+  k_in_degree<<<grid_for(nnz), kThreads, 0, s>>>(row_idx, m, nnz, in_degree, bad);
   return cudaGetLastError();
 }
 

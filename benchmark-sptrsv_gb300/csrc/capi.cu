@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <new>
 #include <vector>
@@ -1021,21 +1022,31 @@ int solve_typed(sptrsv_gb300_handle_s* h, const Values<T>& V, int rhs, int layou
   return SPTRSV_OK;
 }
 
+// Control blocks (ticket, done counter, error code) of the kernel-level
+// executor, one per (device, stream): calls on one stream are ordered by the
+// stream, and calls on different streams, from any host threads, never share
+// a block. A block is allocated at the first call on its stream and kept
+// until exit (a later stream that reuses the handle value reuses the block,
+// which is as safe: the block is idle between calls on that stream).
 std::mutex g_raw_mutex;
-DeviceCtl* g_raw_ctl[64] = {nullptr};
+std::map<std::pair<int, cudaStream_t>, DeviceCtl*> g_raw_ctl;
 
-int raw_ctl(DeviceCtl** out) {
+int raw_ctl(cudaStream_t s, DeviceCtl** out) {
   int dev = 0;
   CUDA_TRY(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 64) return SPTRSV_ERR_INVALID;
   std::lock_guard<std::mutex> lock(g_raw_mutex);
-  if (!g_raw_ctl[dev]) {
-    DeviceCtl* c = nullptr;
-    CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&c), sizeof(DeviceCtl)));
-    CUDA_TRY(cudaMemset(c, 0, sizeof(DeviceCtl)));
-    g_raw_ctl[dev] = c;
+  DeviceCtl*& c = g_raw_ctl[std::make_pair(dev, s)];
+  if (!c) {
+    DeviceCtl* fresh = nullptr;
+    if (cudaMalloc(reinterpret_cast<void**>(&fresh), sizeof(DeviceCtl)) != cudaSuccess) {
+      cudaGetLastError();
+      g_raw_ctl.erase(std::make_pair(dev, s));
+      return SPTRSV_ERR_OOM;
+    }
+    CUDA_TRY(cudaMemset(fresh, 0, sizeof(DeviceCtl)));
+    c = fresh;
   }
-  *out = g_raw_ctl[dev];
+  *out = c;
   return SPTRSV_OK;
 }
 
@@ -1254,7 +1265,7 @@ int analyse_core(sptrsv_handle_t h, const int* d_colPtr, const int* d_rowIdx, cu
   int f = 0;
   ST_TRY(read_flags(h, s, &f));
   if (f) return SPTRSV_ERR_BAD_STRUCTURE;
-  CUDA_TRY(launch_validate_rows(d_colPtr, d_rowIdx, n, sd0, h->flags, s));
+  CUDA_TRY(launch_validate_rows(d_colPtr, d_rowIdx, n, nnz, sd0, h->flags, s));
   ST_TRY(read_flags(h, s, &f));
   if (f) return SPTRSV_ERR_BAD_STRUCTURE;
 
@@ -2003,15 +2014,17 @@ int sptrsv_gb300_executor(const int* d_cscColPtr, const int* d_cscRowIdx, const 
     return SPTRSV_ERR_INVALID;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   DeviceCtl* ctl = nullptr;
-  ST_TRY(raw_ctl(&ctl));
+  ST_TRY(raw_ctl(s, &ctl));
   CUDA_TRY(launch_ref_executor<double>(d_cscColPtr, d_cscRowIdx, d_cscVal, d_graphInDegree, d_left_sum, m,
                                        substitution, rhs, opt, d_b, d_x, ctl, 1000000000ull, s));
-  CUDA_TRY(cudaStreamSynchronize(s));
   int code = 0;
-  CUDA_TRY(cudaMemcpy(&code, &ctl->code, sizeof(int), cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpyAsync(&code, &ctl->code, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
   if (code != DEV_OK) {
-    CUDA_TRY(cudaMemset(ctl, 0, sizeof(DeviceCtl)));
-    return SPTRSV_ERR_TIMEOUT;
+    // the kernel resets its ticket and done words on exit; clear the error code
+    CUDA_TRY(cudaMemsetAsync(ctl, 0, sizeof(DeviceCtl), s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    return code == DEV_BAD_INPUT ? SPTRSV_ERR_BAD_STRUCTURE : SPTRSV_ERR_TIMEOUT;
   }
   return SPTRSV_OK;
 }

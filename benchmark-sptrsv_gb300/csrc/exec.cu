@@ -1515,13 +1515,24 @@ cudaError_t launch_grad_values(const int* csc_row, const int* csc_col, int nnz, 
 // dependency order (SpTRSV_cuda/sptrsv_syncfree_cuda.h:110-172, :290-407).
 // in_degree counts down from the analysed in-degree; a column is ready when
 // its count reaches 1. The caller zeroes left_sum and restores in_degree
-// between solves, as with the reference.
+// between solves, as with the reference. A row index outside [0, m) is never
+// written through: the column's warp records DEV_BAD_INPUT and every warp
+// stops at its next ticket. With `gate` set and *gate non-zero (structural
+// flags raised earlier in the stream) nothing is solved and DEV_BAD_INPUT is
+// recorded.
+__device__ __forceinline__ void raise_bad_input(DeviceCtl* ctl, int where) {
+  if (atomicCAS(&ctl->code, DEV_OK, DEV_BAD_INPUT) == DEV_OK) ctl->where = where;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(128) k_ref_exec(const int* __restrict__ col_ptr, const int* __restrict__ row_idx,
                                                   const T* __restrict__ val, int* in_degree, T* left_sum, int m,
                                                   int substitution, int rhs, int opt, const T* __restrict__ b, T* x,
-                                                  DeviceCtl* ctl, unsigned long long timeout_ns) {
+                                                  DeviceCtl* ctl, unsigned long long timeout_ns,
+                                                  const int* __restrict__ gate) {
   const int lane = threadIdx.x & 31;
+  if (gate && *gate != 0 && blockIdx.x == 0 && threadIdx.x == 0) raise_bad_input(ctl, -1);
+  if (gate && *gate != 0) m = 0;   // every warp skips the loop and joins the exit count
   for (;;) {
     int id = 0;
     if (lane == 0) id = ctl_failed(ctl) ? m : static_cast<int>(atomicAdd(&ctl->ticket, 1u));
@@ -1547,6 +1558,14 @@ __global__ void __launch_bounds__(128) k_ref_exec(const int* __restrict__ col_pt
     // Lanes over right-hand sides (RHS mode) or over entries (NNZ mode); AUTO
     // follows the reference's rule (sptrsv_syncfree_cuda.h:262).
     const bool rhs_mode = rhs > 1 && (opt == 2 || (opt == 3 && (len <= rhs || rhs > 16) && len < 2048));
+    // rows outside [0, m) would write past the counters and partial sums
+    bool bad_row = false;
+    for (int e = s0 + lane; e < s1; e += 32)
+      bad_row |= static_cast<unsigned>(row_idx[e]) >= static_cast<unsigned>(m);
+    if (__any_sync(0xffffffffu, bad_row)) {
+      if (lane == 0) raise_bad_input(ctl, col);
+      break;
+    }
     for (int k = lane; k < rhs; k += 32) {
       const long long p = (long long)col * rhs + k;
       x[p] = (b[p] - Flag<T>::value(Flag<T>::load(&left_sum[p]))) * coef;
@@ -1588,7 +1607,7 @@ __global__ void __launch_bounds__(128) k_ref_exec(const int* __restrict__ col_pt
 template <typename T>
 cudaError_t launch_ref_executor(const int* col_ptr, const int* row_idx, const T* val, int* in_degree, T* left_sum,
                                 int m, int substitution, int rhs, int opt, const T* b, T* x, DeviceCtl* ctl,
-                                unsigned long long timeout_ns, cudaStream_t s) {
+                                unsigned long long timeout_ns, cudaStream_t s, const int* gate) {
   if (m == 0) return cudaSuccess;
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
@@ -1599,7 +1618,7 @@ cudaError_t launch_ref_executor(const int* col_ptr, const int* row_idx, const T*
   const long long need = ((long long)m + 3) / 4;
   if (grid > need) grid = need;
   k_ref_exec<T><<<(int)grid, 128, 0, s>>>(col_ptr, row_idx, val, in_degree, left_sum, m, substitution, rhs, opt, b,
-                                          x, ctl, timeout_ns);
+                                          x, ctl, timeout_ns, gate);
   return cudaGetLastError();
 }
 
@@ -1617,7 +1636,8 @@ cudaError_t launch_ref_executor(const int* col_ptr, const int* row_idx, const T*
   template cudaError_t launch_grad_values<T>(const int*, const int*, int, int, const T*, const T*, long long,     \
                                              long long, T*, cudaStream_t);                                       \
   template cudaError_t launch_ref_executor<T>(const int*, const int*, const T*, int*, T*, int, int, int, int,    \
-                                              const T*, T*, DeviceCtl*, unsigned long long, cudaStream_t);
+                                              const T*, T*, DeviceCtl*, unsigned long long, cudaStream_t,        \
+                                              const int*);
 SPTRSV_INSTANTIATE(double)
 SPTRSV_INSTANTIATE(float)
 

@@ -164,8 +164,10 @@ struct SysDesc {
 
 // ---------------------------------------------------------------- analysis
 cudaError_t launch_validate_ptr(const int* col_ptr, int n, int nnz, int* flags, cudaStream_t s);
-cudaError_t launch_validate_rows(const int* col_ptr, const int* row_idx, int n, const SysDesc& sd, int* flags,
-                                 cudaStream_t s);
+// safe on any column pointers: a column with an out-of-range or decreasing pair is
+// flagged SF_BAD_PTR and its rows are not read (nnz = length of row_idx)
+cudaError_t launch_validate_rows(const int* col_ptr, const int* row_idx, int n, int nnz, const SysDesc& sd,
+                                 int* flags, cudaStream_t s);
 // batch: merge per-system CSC arrays (local indices, concatenated) into one
 // block-diagonal CSC and fill the per-unknown system/direction arrays
 cudaError_t launch_batch_merge(const int* col_ptr_cat, const int* row_idx_cat, int count, const int* sys_off,
@@ -173,7 +175,9 @@ cudaError_t launch_batch_merge(const int* col_ptr_cat, const int* row_idx_cat, i
                                unsigned char* dir, int* sys_of, int* flags, cudaStream_t s);
 // natural execution order: forward systems ascending, backward systems descending
 cudaError_t launch_nat_rows(const SysDesc& sd, int n, int* rows_nat, cudaStream_t s);
-cudaError_t launch_in_degree(const int* row_idx, int m, int nnz, int* in_degree, cudaStream_t s);
+// rows outside [0, m) are skipped; with `bad` set they also raise SF_ROW_RANGE there
+cudaError_t launch_in_degree(const int* row_idx, int m, int nnz, int* in_degree, cudaStream_t s,
+                             int* bad = nullptr);
 // exclusive scan of `count` ints; out may alias in; out[count] receives the total when with_total.
 cudaError_t exclusive_scan_int(const int* in, int* out, int count, bool with_total, cudaStream_t s);
 size_t radix_sort_temp_bytes(int count);
@@ -276,10 +280,14 @@ cudaError_t launch_update(double* x, const float* d, long long count, unsigned l
                           cudaStream_t s);
 
 // Kernel-level surface of the reference: in-degree countdown counters owned by
-// the caller, natural column order, one warp per column.
+// the caller, natural column order, one warp per column. A row index outside
+// [0, m) is never written through: the kernel records DEV_BAD_INPUT and stops.
+// With `gate` set, the kernel does nothing but record DEV_BAD_INPUT when
+// *gate is non-zero (structural flags found by validation earlier in the stream).
 template <typename T>
 cudaError_t launch_ref_executor(const int* col_ptr, const int* row_idx, const T* val, int* in_degree,
                                 T* left_sum, int m, int substitution, int rhs, int opt, const T* b, T* x,
-                                DeviceCtl* ctl, unsigned long long timeout_ns, cudaStream_t s);
+                                DeviceCtl* ctl, unsigned long long timeout_ns, cudaStream_t s,
+                                const int* gate = nullptr);
 
 }  // namespace sptrsv

@@ -10,6 +10,10 @@
 //
 // Limits and rules:
 //  * at most kNoAllocMaxN unknowns, one right-hand side, FP64;
+//  * the structure is validated on the device in the same stream before the
+//    solve (column pointers, row range, order, diagonal placement, triangle);
+//    malformed input returns SPTRSV_ERR_BAD_STRUCTURE and nothing past the
+//    scratch array is ever written;
 //  * the first call on a device looks up the array's device address
 //    (cudaGetSymbolAddress, once per device, with that device current); make
 //    that first call before any stream capture;
@@ -26,12 +30,14 @@ namespace sptrsv {
 namespace {
 
 constexpr int kNoAllocMaxN = SPTRSV_NOALLOC_MAX_N;
-constexpr size_t kCtlBytes = 256;
+constexpr size_t kCtlBytes = 256;     // DeviceCtl, then the structural flags word at kFlagsOffset
+constexpr size_t kFlagsOffset = 128;
+static_assert(sizeof(DeviceCtl) <= kFlagsOffset, "control block overlaps the flags word");
 constexpr size_t kCounterBytes = sizeof(int) * (size_t)kNoAllocMaxN;
 constexpr size_t kSumBytes = sizeof(double) * (size_t)kNoAllocMaxN;
 constexpr size_t kScratchBytes = kCtlBytes + kCounterBytes + kSumBytes;
 
-// [control block | in-degree counters | partial sums]
+// [control block, flags | in-degree counters | partial sums]
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 std::mutex g_setup_mutex;
@@ -70,20 +76,28 @@ extern "C" int sptrsv_gb300_solve_noalloc(const int* d_colPtr, const int* d_rowI
   const int st = scratch_for_current_device(&scratch);
   if (st != SPTRSV_OK) return st;
   auto* ctl = reinterpret_cast<DeviceCtl*>(scratch);
+  auto* flags = reinterpret_cast<int*>(scratch + kFlagsOffset);
   auto* counters = reinterpret_cast<int*>(scratch + kCtlBytes);
   auto* left_sum = reinterpret_cast<double*>(scratch + kCtlBytes + kCounterBytes);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  // clear what must start at zero: control words (ticket, error code), partial sums;
-  // the in-degree counters are rebuilt by the analyser below
-  if (cudaMemsetAsync(ctl, 0, sizeof(DeviceCtl), s) != cudaSuccess ||
+  // clear what must start at zero: control words (ticket, error code) and the
+  // flags word, partial sums, in-degree counters (rebuilt by the analyser)
+  if (cudaMemsetAsync(scratch, 0, kCtlBytes, s) != cudaSuccess ||
       cudaMemsetAsync(left_sum, 0, sizeof(double) * (size_t)n, s) != cudaSuccess ||
       cudaMemsetAsync(counters, 0, sizeof(int) * (size_t)n, s) != cudaSuccess) {
     cudaGetLastError();
     return SPTRSV_ERR_CUDA;
   }
-  if (launch_in_degree(d_rowIdx, n, nnz, counters, s) != cudaSuccess ||
+  // validation, analyser and executor in one stream: the executor does nothing
+  // but record DEV_BAD_INPUT when validation raised a flag, and the analyser
+  // skips rows outside [0, n), so malformed input never writes past the array
+  SysDesc sd;
+  sd.substitution = substitution;
+  if (launch_validate_ptr(d_colPtr, n, nnz, flags, s) != cudaSuccess ||
+      launch_validate_rows(d_colPtr, d_rowIdx, n, nnz, sd, flags, s) != cudaSuccess ||
+      launch_in_degree(d_rowIdx, n, nnz, counters, s, flags) != cudaSuccess ||
       launch_ref_executor<double>(d_colPtr, d_rowIdx, d_val, counters, left_sum, n, substitution, 1,
-                                  SPTRSV_OPT_WARP_AUTO, d_b, d_x, ctl, 1000000000ull, s) != cudaSuccess) {
+                                  SPTRSV_OPT_WARP_AUTO, d_b, d_x, ctl, 1000000000ull, s, flags) != cudaSuccess) {
     cudaGetLastError();
     return SPTRSV_ERR_CUDA;
   }
@@ -93,5 +107,6 @@ extern "C" int sptrsv_gb300_solve_noalloc(const int* d_colPtr, const int* d_rowI
     cudaGetLastError();
     return SPTRSV_ERR_CUDA;
   }
-  return code == DEV_OK ? SPTRSV_OK : SPTRSV_ERR_TIMEOUT;
+  if (code == DEV_OK) return SPTRSV_OK;
+  return code == DEV_BAD_INPUT ? SPTRSV_ERR_BAD_STRUCTURE : SPTRSV_ERR_TIMEOUT;
 }

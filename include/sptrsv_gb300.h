@@ -189,7 +189,14 @@ int sptrsv_gb300_syncfree_host(const int *cscColPtrTR, const int *cscRowIdxTR, c
  *                         d_left_sum (n*rhs, zero on entry). Like the reference,
  *                         the caller restores d_graphInDegree and zeroes
  *                         d_left_sum before the next call. Synchronises and
- *                         reports SPTRSV_ERR_TIMEOUT if a wait ran out.
+ *                         reports SPTRSV_ERR_TIMEOUT if a wait ran out, and
+ *                         SPTRSV_ERR_BAD_STRUCTURE (nothing written past the
+ *                         caller's arrays) if a row index lies outside [0, m).
+ *                         The ticket and error words live in a small device
+ *                         block the library keeps per (device, stream): calls
+ *                         on one stream are ordered by it, calls on different
+ *                         streams (from any host threads) are independent.
+ * sptrsv_gb300_analyser   skips (never writes) row indices outside [0, m).
  * ------------------------------------------------------------------------- */
 int sptrsv_gb300_analyser(const int *d_cscRowIdx, int m, int nnz, int *d_graphInDegree, void *stream);
 int sptrsv_gb300_executor(const int *d_cscColPtr, const int *d_cscRowIdx, const double *d_cscVal,
@@ -313,7 +320,10 @@ int sptrsv_gb300_tune(sptrsv_handle_t handle, const void *d_val, int dtype, int 
  * sums, control words) in a fixed device array inside the library, sized for
  * at most SPTRSV_NOALLOC_MAX_N unknowns (about 3 MB, held by every GPU that
  * loads the library until the process exits). Larger n returns
- * SPTRSV_ERR_UNSUPPORTED. The first call on a device looks up the array's
+ * SPTRSV_ERR_UNSUPPORTED. The structure is validated on the device before the
+ * solve, in the same stream; malformed input (column pointers, a row index
+ * outside [0, n), unsorted rows, a misplaced or missing diagonal, the wrong
+ * triangle) returns SPTRSV_ERR_BAD_STRUCTURE and writes nothing past the array. The first call on a device looks up the array's
  * address (once per device); make it before any stream capture. All calls
  * share the array and each clears it before use, so calls whose GPU work
  * overlaps race: serialise them. Synchronises `stream`; returns

@@ -8,11 +8,13 @@ Two implementations with one interface:
   * ``port``: liboracle.so, the C restatement in sptrsv_oracle.c (always built);
   * ``ref``:  libsptrsv_ref.so, the reference's own serial sources compiled in
     place by ``make ref`` (only where the reference checkout exists; the GPU
-    host does not have it).
+    host does not have it). The checkout's root directory comes from the
+    environment variable SPTRSV_REFERENCE_DIR.
 """
 from __future__ import annotations
 
 import ctypes
+import os
 import subprocess
 from pathlib import Path
 
@@ -21,7 +23,15 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 PORT_LIB = HERE / "_build" / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libsptrsv_ref.so"
-REF_SOURCES = Path("/root/reference/SpTRSV_cuda")
+
+
+def ref_sources() -> Path | None:
+    """SpTRSV_cuda/ of the reference checkout named by SPTRSV_REFERENCE_DIR, if present."""
+    root = os.environ.get("SPTRSV_REFERENCE_DIR")
+    if not root:
+        return None
+    src = Path(root) / "SpTRSV_cuda"
+    return src if src.exists() else None
 
 FORWARD = 0
 BACKWARD = 1
@@ -30,8 +40,9 @@ BACKWARD = 1
 def build(ref: bool = True) -> None:
     """Compile the port (always) and the reference build (when its sources are present)."""
     subprocess.run(["make", "-s", "-C", str(HERE), "port"], check=True)
-    if ref and REF_SOURCES.exists():
-        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={REF_SOURCES}"], check=True)
+    src = ref_sources()
+    if ref and src is not None:
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={src}"], check=True)
 
 
 def _p(a):
@@ -146,7 +157,7 @@ def port() -> _Impl:
 def ref() -> _Impl | None:
     """The reference's own serial code, or None where it was not built."""
     if "ref" not in _CACHE:
-        if not REF_LIB.exists() and REF_SOURCES.exists():
+        if not REF_LIB.exists() and ref_sources() is not None:
             build(ref=True)
         if not REF_LIB.exists():
             return None

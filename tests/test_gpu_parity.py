@@ -290,3 +290,86 @@ def test_full_size_properties_laplace(cuda, oracle_port):
         x = s.solve(cuda.from_numpy(b).cuda()).cpu().numpy()
         assert np.array_equal(x.view(np.uint64), ref.view(np.uint64))
         assert s.info()["nlevels"] == 2 * 1414 - 1
+
+
+def test_kernel_level_executor_two_threads_two_streams(cuda, oracle_port):
+    """Two host threads, each on its own stream, run the kernel-level analyser and
+    executor at the same time on different systems: the library keeps one control
+    block (ticket, done and error words) per stream, so neither call disturbs the other."""
+    import threading
+
+    from sptrsv_gb300 import analyser, executor, matgen
+    systems = [matgen.poisson_band(30_000, 6.0, 3000, seed=41, lower=True),
+               matgen.poisson_band(24_000, 9.0, 1500, seed=42, lower=False)]
+    refs, outs, errors = [], [None, None], []
+    for k, m in enumerate(systems):
+        b = np.random.default_rng(k).standard_normal(m.n)
+        refs.append((b, oracle_port.solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, b)))
+
+    def run(k):
+        try:
+            m = systems[k]
+            stream = cuda.cuda.Stream()
+            with cuda.cuda.stream(stream):
+                cp = cuda.from_numpy(m.col_ptr).cuda()
+                ri = cuda.from_numpy(m.row_idx).cuda()
+                va = cuda.from_numpy(m.val).cuda()
+                b = cuda.from_numpy(refs[k][0]).cuda()
+                deg0 = cuda.empty(m.n, dtype=cuda.int32, device="cuda")
+                analyser(ri, m.n, m.nnz, deg0, stream=stream)
+                res = []
+                for _ in range(6):
+                    deg = deg0.clone()
+                    left = cuda.zeros(m.n, dtype=cuda.float64, device="cuda")
+                    x = cuda.zeros(m.n, dtype=cuda.float64, device="cuda")
+                    executor(cp, ri, va, deg, left, m.n, m.substitution, 1, 3, b, x, stream=stream)
+                    res.append(x.cpu().numpy())
+                outs[k] = res
+        except Exception as exc:  # noqa: BLE001 - reported by the main thread
+            errors.append(exc)
+
+    threads = [threading.Thread(target=run, args=(k,)) for k in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    for k in range(2):
+        for x in outs[k]:
+            assert relerr(x, refs[k][1]) <= TOL64
+
+
+def test_kernel_level_executor_rejects_row_out_of_range(cuda, oracle_port):
+    """A row index >= m makes the kernel-level executor return BAD_STRUCTURE without
+    writing through it. The counters and partial sums are allocated twice as long, so
+    the planted row stays inside them even if the guard failed; their tails must stay
+    untouched."""
+    from sptrsv_gb300 import _lib, analyser, matgen
+    m = matgen.poisson_band(5000, 5.0, 400, seed=43, lower=True)
+    row_idx = m.row_idx.copy()
+    col = 1000
+    row_idx[m.col_ptr[col + 1] - 1] = m.n + 7     # last (largest) row of the column
+    cp = cuda.from_numpy(m.col_ptr).cuda()
+    ri = cuda.from_numpy(row_idx).cuda()
+    va = cuda.from_numpy(m.val).cuda()
+    deg = cuda.zeros(2 * m.n, dtype=cuda.int32, device="cuda")
+    analyser(cuda.from_numpy(m.row_idx).cuda(), m.n, m.nnz, deg)
+    left = cuda.zeros(2 * m.n, dtype=cuda.float64, device="cuda")
+    b = cuda.ones(m.n, dtype=cuda.float64, device="cuda")
+    x = cuda.zeros(m.n, dtype=cuda.float64, device="cuda")
+    import ctypes
+    stream = ctypes.c_void_p(int(cuda.cuda.current_stream().cuda_stream))
+    p = lambda t: ctypes.c_void_p(int(t.data_ptr()))  # noqa: E731
+    rc = _lib.load().sptrsv_gb300_executor(p(cp), p(ri), p(va), p(deg), p(left), m.n, 0, 1, 3, p(b), p(x), stream)
+    assert rc == _lib.ERR_BAD_STRUCTURE
+    assert int(deg[m.n:].abs().sum()) == 0
+    assert float(left[m.n:].abs().sum()) == 0.0
+    # the per-stream control block is usable again after the error
+    deg2 = cuda.empty(m.n, dtype=cuda.int32, device="cuda")
+    analyser(cuda.from_numpy(m.row_idx).cuda(), m.n, m.nnz, deg2)
+    left2 = cuda.zeros(m.n, dtype=cuda.float64, device="cuda")
+    rc = _lib.load().sptrsv_gb300_executor(p(cp), p(cuda.from_numpy(m.row_idx).cuda()), p(va), p(deg2), p(left2),
+                                           m.n, 0, 1, 3, p(b), p(x), stream)
+    assert rc == 0
+    ref = oracle_port.solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, np.ones(m.n))
+    assert relerr(x.cpu().numpy(), ref) <= TOL64
