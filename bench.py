@@ -87,6 +87,15 @@ def make_cases(scale: float = 1.0, only=None):
     return cases
 
 
+def workload_config(args, world: int) -> dict:
+    """The `config` of both arms' JSON lines (identical, so the lines compare)."""
+    return {"workload": WORKLOAD if args.scale == 1.0 else f"{WORKLOAD}, sizes x{args.scale}", "rhs": 1,
+            "dtype": "f64", "parallelism": f"replicas x{world}" if world > 1 else "one device",
+            "mode": "replicas" if world > 1 else "single",
+            "l2": "GPU arm: flushed (256 MiB write) before every solve and before every end-to-end step, "
+                  "outside the timed events; CPU arm: inputs larger than the host caches for the power-law system"}
+
+
 def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -190,8 +199,7 @@ def run_reference(args, world, rank):
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "GB/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD if args.scale == 1.0 else f"{WORKLOAD}, sizes x{args.scale}", "rhs": 1,
-                   "l2": "inputs > L2 for the power-law system; CPU arm"},
+        "config": workload_config(args, world),
         "cpu_baseline": {"value": round(value, 4), "unit": "GB/s", "cores": threads, "kind": kind,
                          "sample": sample, "host": host_info()},
         "e2e": {"value": round(value, 4), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -412,6 +420,7 @@ def run_gpu(args, world, rank, local):
     e2e_order = by_size[0::2] + by_size[1::2][::-1]
     e2e_ms = []
     for it in range(args.warmup + args.steps):
+        flush.fill_(it & 0xFF)   # cold L2, as in the device-timed loop (outside the timed region)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         arrived = []
@@ -478,17 +487,18 @@ def run_gpu(args, world, rank, local):
             details[c["name"]]["reference_scheme_ms"] = round(ref_scheme[c["name"]], 4)
             details[c["name"]]["speedup_vs_reference_scheme"] = round(ref_scheme[c["name"]] / ms, 2)
     if rank != 0:
+        if pg:
+            pg.destroy_process_group()
         return 0
     cpu = cpu_baseline_sample(cases) if (world == 1 and not args.no_cpu_baseline) else None
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(step_ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generators, x_true = 1)",
-        "config": {"workload": WORKLOAD if args.scale == 1.0 else f"{WORKLOAD}, sizes x{args.scale}", "rhs": 1,
-                   "parallelism": f"replicas x{world}",
-                   "l2": "flushed (256 MiB write) before every solve, outside the timed events",
-                   "solver": args.solver_kw or ("defaults" if args.no_tune else "autotuned per system"),
+        "config": workload_config(args, world),
+        "solver": {"settings": args.solver_kw or ("defaults" if args.no_tune else "autotuned per system"),
                    "tuned": tuned},
+        "per_rank_value": round(total_bytes / (step_ms * 1e-3) / 1e9, 3),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 3), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 5), "traffic": traffic_bytes(dom),
                      "traffic_unit": "bytes per launch (DRAM read + write)",
@@ -512,6 +522,24 @@ def run_gpu(args, world, rank, local):
                                           "atomic partial sums), restated with ticket order and bounded waits, "
                                           "same systems, L2 not flushed"} if ref_scheme else None),
     }
+    if world == 1 and not args.no_extras and args.scale == 1.0 and not args.cases:
+        # the rest of the metric, measured after the headline's timed region:
+        # 10k system beside the CPU serial executor, many right-hand sides with
+        # mixed precision, the 512-system batch, forward + adjoint
+        from sptrsv_gb300 import matgen
+        for c in cases:
+            c["solver"].close()
+        del cases, solvers
+        torch.cuda.empty_cache()
+        ex_args = argparse.Namespace(**vars(args))
+        ex_args.steps = min(args.steps, 10)
+        m1 = matgen.system_1m(seed=2)
+        t0 = time.perf_counter()
+        line["system_10k"] = measure_system_10k(ex_args, dev)
+        line["multi_rhs"] = measure_multi_rhs(ex_args, dev, m=m1)
+        line["batch"] = measure_batch(ex_args, dev)
+        line["adjoint"] = measure_adjoint(ex_args, dev, m=m1)
+        line["extras_wall_s"] = round(time.perf_counter() - t0, 1)
     print(json.dumps(line), flush=True)
     if pg:
         pg.destroy_process_group()
@@ -519,6 +547,9 @@ def run_gpu(args, world, rank, local):
 
 
 # ------------------------------------------------------------------ other workloads
+# Each returns a dict; `--workload X` prints it as a line of its own, and the
+# default run attaches all four to its line (one GPU, after the timed region
+# of the headline workload).
 def _timed(fn, reps, flush=None):
     import torch
     ts = []
@@ -535,22 +566,69 @@ def _timed(fn, reps, flush=None):
     return statistics.median(ts)
 
 
-def run_multi_rhs(args):
+def _relerr(x, ref) -> float:
+    x = np.asarray(x, dtype=np.float64).ravel()
+    ref = np.asarray(ref, dtype=np.float64).ravel()
+    return float(np.max(np.abs(x - ref)) / max(float(np.max(np.abs(ref))), 1e-300))
+
+
+def measure_system_10k(args, dev) -> dict:
+    """10k-row Poisson(8) band system, FP64, rhs 1: the serial executor on one host core
+    beside the GPU solve (automatic plan), both against the oracle."""
+    import torch
+
+    from oracle import oracle
+    from sptrsv_gb300 import SyncFreeSolver, matgen
+    m = matgen.system_10k()
+    b = m.matvec(np.ones(m.n))
+    imp = oracle.ref() or oracle.port()
+    deg = imp.analyser(m.row_idx, m.n)
+    ts = []
+    for _ in range(max(args.steps, 20)):
+        t0 = time.perf_counter()
+        ref = imp.executor(m.col_ptr, m.row_idx, m.val, deg, m.n, 0, 1, b)
+        ts.append(1e3 * (time.perf_counter() - t0))
+    cpu_ms = statistics.median(ts)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, 0, values=m.val, sync_check=False)
+    bd = torch.from_numpy(b).to(dev)
+    x = s.solve(bd)
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    time.sleep(0.2)
+    # enough repetitions (~0.1 s) for the clock sampler to see the solves
+    gpu_ms = _timed(lambda: s.solve(bd, out=x), max(args.steps, 500), flush)
+    clk = clocks.stop()
+    s.check()
+    err = _relerr(x.cpu().numpy(), ref)
+    ex = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, 0, values=m.val, schedule=2, exact=True)
+    bit_equal = bool(np.array_equal(ex.solve(bd).cpu().numpy().view(np.uint64), ref.view(np.uint64)))
+    ex.close()
+    nl = s.info()["nlevels"]
+    s.close()
+    bp = bytes_pass(m.n, m.nnz)
+    return {"workload": "n=10,000 Poisson(8) band 2000, FP64, rhs=1, forward", "n": m.n, "nnz": m.nnz,
+            "nlevels": nl, "gpu_ms": round(gpu_ms, 4), "gpu_gbs": round(bp / gpu_ms / 1e6, 3),
+            "cpu_serial_ms": round(cpu_ms, 4), "cpu_serial_gbs": round(bp / cpu_ms / 1e6, 3),
+            "cpu_kind": "reference" if imp.kind == "ref" else "port", "cpu_cores": 1,
+            "speedup_gpu_vs_cpu_serial": round(cpu_ms / gpu_ms, 2), "fwd_err_vs_oracle": err,
+            "exact_mode_bit_identical": bit_equal, "l2": "flushed before every GPU solve", "clocks": clk}
+
+
+def measure_multi_rhs(args, dev, m=None, world=1, rank=0, dist=None) -> dict:
+    """n = 1M band system, rhs in {1, 16, 64}, column-major B ~ N(0,1): plain FP64
+    vs FP32 storage/solve + FP64-residual refinement, both against the oracle."""
     import torch
 
     from oracle import oracle
     from sptrsv_gb300 import SyncFreeSolver, matgen, shard
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    m = matgen.system_1m(seed=2)
-    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    if m is None:
+        m = matgen.system_1m(seed=2)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
     out = {}
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    time.sleep(0.2)
     for rhs in (1, 16, 64):
         rng = np.random.default_rng(rhs)
         B = rng.standard_normal((m.n, rhs))
@@ -566,55 +644,46 @@ def run_multi_rhs(args):
             ref = oracle.port().solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution,
                                       Bl if w > 1 else Bl[:, 0])
             ref = ref.reshape(m.n, w)
-            b = torch.from_numpy(np.ascontiguousarray(Bl.T)).cuda().t()
+            b = torch.from_numpy(np.ascontiguousarray(Bl.T)).to(dev).t()
             s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, values=m.val, sync_check=False,
                                **args.solver_kw)
             x = s.solve(b)
             t64 = _timed(lambda: s.solve(b, out=x), args.steps, flush)
-            err64 = float((x.cpu().numpy() - ref).__abs__().max() / np.abs(ref).max())
+            s.check()
+            err64 = _relerr(x.cpu().numpy(), ref)
             s.set_option(7, 1)
             xr, iters, est = s.solve_refine(b)
             s.set_option(7, 0)
             tmix = _timed(lambda: s.solve_refine(b, out=xr, tol=0.0, max_iter=iters), args.steps, flush)
-            errmix = float((xr.cpu().numpy() - ref).__abs__().max() / np.abs(ref).max())
+            s.check()
+            errmix = _relerr(xr.cpu().numpy(), ref)
             s.close()
         if dist is not None:
             # whole-job time = the slowest rank; errors = the worst slice
-            t = torch.tensor([t64, tmix, err64, errmix, iters], dtype=torch.float64, device="cuda")
+            t = torch.tensor([t64, tmix, err64, errmix, iters], dtype=torch.float64, device=dev)
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             t64, tmix, err64, errmix = (float(v) for v in t.tolist()[:4])
             iters = int(t[4].item())
         bp = bytes_pass(m.n, m.nnz, rhs)
         out[f"rhs{rhs}"] = {"fp64_ms": round(t64, 4), "mixed_ms": round(tmix, 4), "refine_steps": iters,
-                            "speedup_mixed_vs_fp64": round(t64 / tmix, 3), "fp64_fwd_err": err64,
-                            "mixed_fwd_err": errmix, "fp64_problem_gbs": round(bp / t64 / 1e6, 2),
-                            "mixed_problem_gbs": round(bp / tmix / 1e6, 2)}
-    if dist is not None:
-        dist.destroy_process_group()
-        if rank != 0:
-            return 0
-    line = {"workload": "multi_rhs", "metric": "FP32+FP64-refinement speed-up over plain FP64 (n=1M, rhs=64)",
-            "value": out["rhs64"]["speedup_mixed_vs_fp64"], "unit": "x", "higher_is_better": True,
-            "n_gpus": world, "n": m.n, "nnz": m.nnz, "cases": out,
-            "config": {"workload": "n=1M Poisson(9) band 20k, col-major B",
-                       "parallelism": f"rhs columns sharded over {world} rank(s)" if world > 1 else "one GPU"}}
-    print(json.dumps(line), flush=True)
-    return 0
+                            "speedup_mixed_vs_fp64": round(t64 / tmix, 3), "fp64_fwd_err_vs_oracle": err64,
+                            "mixed_fwd_err_vs_oracle": errmix, "fp64_problem_gbs": round(bp / t64 / 1e6, 2),
+                            "mixed_problem_gbs": round(bp / tmix / 1e6, 2),
+                            "fp64_solves_per_s": round(1e3 / t64, 1)}
+    clk = clocks.stop()
+    return {"workload": "n=1M Poisson(9) band 20k, rhs 1/16/64, column-major B ~ N(0,1)", "n": m.n, "nnz": m.nnz,
+            "cases": out, "l2": "flushed before every solve", "clocks": clk,
+            "parallelism": f"rhs columns sharded over {world} rank(s)" if world > 1 else "one GPU"}
 
 
-def run_batch(args):
+def measure_batch(args, dev, world=1, rank=0, dist=None) -> dict:
+    """512 independent systems (even lower, odd upper), rhs 4: one batched launch
+    sequence (FP32 + FP64 refinement; plain FP64) vs 512 per-system FP64 launches;
+    every system's slice against its own oracle solve."""
     import torch
 
     from oracle import oracle
     from sptrsv_gb300 import SyncFreeSolver, matgen, shard
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     t0 = time.perf_counter()
     systems_all = matgen.batch_uneven(count=args.batch_count, seed=3)
     # independent systems shard over ranks with no exchange (nnz-balanced assignment)
@@ -631,95 +700,106 @@ def run_batch(args):
     s = SyncFreeSolver(batch=[(m.col_ptr, m.row_idx, m.n, m.substitution) for m in systems], values=vals,
                        sync_check=False, **args.solver_kw)
     tan = time.perf_counter() - t0
-    b = torch.from_numpy(np.concatenate(bs)).cuda()
+    b = torch.from_numpy(np.concatenate(bs)).to(dev)
     tuned = None
+    t0 = time.perf_counter()
     if not args.no_tune and not args.solver_kw:
         s.set_option(7, 1)
-        tuned = s.tune(b, values=torch.from_numpy(vals).cuda(), reps=2)
+        tuned = s.tune(b, values=torch.from_numpy(vals).to(dev), reps=2)
         s.set_option(7, 0)
-    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    ttune = time.perf_counter() - t0
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
     s.set_option(7, 1)
     xr, iters, est = s.solve_refine(b)
     s.set_option(7, 0)
-    t_mixed = _timed(lambda: s.solve_refine(b, out=xr, tol=0.0, max_iter=iters), args.steps, flush)
-    # the same refinement captured once in a CUDA graph and replayed
-    xg = torch.empty_like(xr)
-    graph = s.graph(b, xg, kind=1, count=iters)
-    graph.replay()
-    s.check()
-    t_graph = _timed(graph.replay, args.steps, flush)
-    s.check()
-    graph_err = float((xg - xr).abs().max() / xr.abs().max())
-    graph.close()
     x64 = s.solve(b)
-    t_b64 = _timed(lambda: s.solve(b, out=x64), args.steps, flush)
     # per-system plain FP64 launches (one handle per system, one launch each)
     hs = [SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, values=m.val, sync_check=False,
                          **args.solver_kw) for m in systems]
-    bd = [torch.from_numpy(bb).cuda() for bb in bs]
+    bd = [torch.from_numpy(bb).to(dev) for bb in bs]
     xd = [torch.empty_like(bb) for bb in bd]
 
     def per_system():
         for h, bb, xx in zip(hs, bd, xd):
             h.solve(bb, out=xx)
     per_system()
+    xg = torch.empty_like(xr)
+    graph = s.graph(b, xg, kind=1, count=iters)
+    graph.replay()
+    s.check()
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    time.sleep(0.2)
+    t_mixed = _timed(lambda: s.solve_refine(b, out=xr, tol=0.0, max_iter=iters), args.steps, flush)
+    t_graph = _timed(graph.replay, args.steps, flush)
+    t_b64 = _timed(lambda: s.solve(b, out=x64), args.steps, flush)
     t_per = _timed(per_system, max(3, args.steps // 3), flush)
-    # forward error vs the per-system FP64 oracle on a sample of systems
-    xr_h = xr.cpu().numpy()
+    clk = clocks.stop()
+    s.check()
+    graph_err = float((xg - xr).abs().max() / xr.abs().max())
+    graph.close()
+    # forward error of every system against its own FP64 oracle solve
+    xr_h, x64_h = xr.cpu().numpy(), x64.cpu().numpy()
+    xd_h = [xx.cpu().numpy() for xx in xd]
     off = s.offsets
-    sample = list(range(0, len(systems), max(1, len(systems) // 16)))
-    err = 0.0
-    for k in sample:
-        m = systems[k]
-        ref = oracle.port().solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, bs[k])
-        err = max(err, float(np.abs(xr_h[off[k]:off[k + 1]] - ref).max() / np.abs(ref).max()))
+    err_mixed = err64 = err_per = 0.0
+    imp = oracle.port()
+    for k, m in enumerate(systems):
+        ref = imp.solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, bs[k])
+        err_mixed = max(err_mixed, _relerr(xr_h[off[k]:off[k + 1]], ref))
+        err64 = max(err64, _relerr(x64_h[off[k]:off[k + 1]], ref))
+        err_per = max(err_per, _relerr(xd_h[k], ref))
+    nlevels = s.info()["nlevels"]
+    for h in hs:
+        h.close()
+    s.close()
     if dist is not None:
         # whole-job time = the slowest rank
-        t = torch.tensor([t_mixed, t_b64, t_per, t_graph], dtype=torch.float64, device="cuda")
+        t = torch.tensor([t_mixed, t_b64, t_per, t_graph], dtype=torch.float64, device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         t_mixed, t_b64, t_per, t_graph = (float(v) for v in t.tolist())
-        tot = torch.tensor([ntot, nnz], dtype=torch.float64, device="cuda")
+        tot = torch.tensor([ntot, nnz], dtype=torch.float64, device=dev)
         dist.all_reduce(tot)
         ntot, nnz = (int(v) for v in tot.tolist())
-        e = torch.tensor([err], dtype=torch.float64, device="cuda")
+        e = torch.tensor([err_mixed, err64, err_per], dtype=torch.float64, device=dev)
         dist.all_reduce(e, op=dist.ReduceOp.MAX)
-        err = float(e.item())
-        dist.destroy_process_group()
-        if rank != 0:
-            return 0
+        err_mixed, err64, err_per = (float(v) for v in e.tolist())
     nsys = len(systems_all)
-    line = {"workload": "batch", "metric": "batched solves/s (FP32+FP64 refinement, one persistent launch per pass)",
-            "value": round(nsys / (t_mixed * 1e-3), 2), "unit": "systems/s", "higher_is_better": True,
-            "n_gpus": world, "scaling": "strong" if world > 1 else None,
-            "systems": nsys, "n_total": ntot, "nnz_total": nnz, "rhs": rhs,
-            "nlevels_batch": s.info()["nlevels"], "tuned": tuned,
-            "mixed_batched_ms": round(t_mixed, 3), "refine_steps": iters,
+    return {"workload": f"{nsys} systems (half lower, half upper), n log-uniform 1k-200k, rhs=4",
+            "metric": "batched solves/s (FP32+FP64 refinement, one persistent launch per pass)",
+            "value": round(nsys / (t_mixed * 1e-3), 2), "unit": "systems/s",
+            "systems": nsys, "n_total": ntot, "nnz_total": nnz, "rhs": rhs, "nlevels_batch": nlevels,
+            "tuned": tuned, "mixed_batched_ms": round(t_mixed, 3), "refine_steps": iters,
             "mixed_graph_replay_ms": round(t_graph, 3), "graph_vs_direct_rel_diff": graph_err,
-            "fp64_batched_ms": round(t_b64, 3),
+            "fp64_batched_ms": round(t_b64, 3), "fp64_batched_solves_per_s": round(nsys / (t_b64 * 1e-3), 2),
             "fp64_per_system_launches_ms": round(t_per, 3),
             "speedup_vs_per_system_fp64": round(t_per / t_mixed, 2),
             "speedup_vs_batched_fp64": round(t_b64 / t_mixed, 3),
-            "fwd_err_vs_oracle_sampled": err, "sampled_systems": len(sample),
-            "generate_s": round(tgen, 1), "analyse_s": round(tan, 2),
-            "config": {"workload": f"{nsys} systems, rhs=4, FP32+FP64 refinement",
-                       "parallelism": f"systems sharded over {world} rank(s), nnz-balanced" if world > 1
-                       else "one GPU"}}
-    print(json.dumps(line), flush=True)
-    return 0
+            "fwd_err_vs_oracle_mixed": err_mixed, "fwd_err_vs_oracle_fp64_batched": err64,
+            "fwd_err_vs_oracle_fp64_per_system": err_per, "checked_systems": len(systems),
+            "generate_s": round(tgen, 1), "analyse_s": round(tan, 2), "tune_s": round(ttune, 1),
+            "l2": "flushed before every timed call", "clocks": clk,
+            "parallelism": f"systems sharded over {world} rank(s), nnz-balanced" if world > 1 else "one GPU"}
 
 
-def run_adjoint(args):
+def measure_adjoint(args, dev, m=None) -> dict:
+    """The 1M band system, rhs 8, FP64, loss = sum(w * x): forward + adjoint with the
+    value gradient over the forward time; gradients against the oracle gradient."""
     import torch
 
+    from oracle import oracle
     from sptrsv_gb300 import SyncFreeSolver, matgen, sparse_triangular_solve
-    m = matgen.system_1m(seed=2)
+    if m is None:
+        m = matgen.system_1m(seed=2)
     rhs = 8
     rng = np.random.default_rng(4)
-    B = torch.from_numpy(rng.standard_normal((m.n, rhs))).cuda()
-    W = torch.from_numpy(rng.standard_normal((m.n, rhs))).cuda()
+    Bh = rng.standard_normal((m.n, rhs))
+    Wh = rng.standard_normal((m.n, rhs))
+    B = torch.from_numpy(Bh).to(dev)
+    W = torch.from_numpy(Wh).to(dev)
     s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, sync_check=False, **args.solver_kw)
-    val = torch.from_numpy(m.val).cuda()
-    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    val = torch.from_numpy(m.val).to(dev)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
 
     def fwd():
         with torch.no_grad():
@@ -730,20 +810,63 @@ def run_adjoint(args):
         bb = B.detach().requires_grad_(True)
         x = sparse_triangular_solve(s, v, bb)
         (W * x).sum().backward()
-        return v.grad, bb.grad
+        return x, v.grad, bb.grad
     fwd()
-    fwd_bwd()
+    x, gv, gb = fwd_bwd()
+    s.check()
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    time.sleep(0.2)
     t_f = _timed(fwd, args.steps, flush)
     t_fb = _timed(fwd_bwd, args.steps, flush)
     s.set_option(15, 1)
     fwd_bwd()
     t_fb_fused = _timed(fwd_bwd, args.steps, flush)
     s.set_option(15, 0)
-    line = {"workload": "adjoint", "metric": "(forward + adjoint with value gradient) / forward time",
+    clk = clocks.stop()
+    s.check()
+    x_ref = oracle.port().solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, Bh)
+    lam_ref, dval_ref = oracle.adjoint_gradient(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, x_ref, Wh)
+    errs = {"x": _relerr(x.detach().cpu().numpy(), x_ref), "grad_b": _relerr(gb.cpu().numpy(), lam_ref),
+            "grad_values": _relerr(gv.cpu().numpy(), dval_ref)}
+    s.close()
+    return {"workload": "n=1M Poisson(9) band 20k, rhs=8, FP64, loss=sum(w*x)",
+            "metric": "(forward + adjoint with value gradient) / forward time",
             "value": round(t_fb / t_f, 3), "unit": "ratio", "higher_is_better": False,
             "forward_ms": round(t_f, 3), "forward_backward_ms": round(t_fb, 3),
             "forward_backward_fused_in_solve_ms": round(t_fb_fused, 3), "n": m.n, "nnz": m.nnz, "rhs": rhs,
-            "config": {"workload": "n=1M Poisson(9) band 20k, rhs=8, FP64, loss=sum(w*x)"}}
+            "err_vs_oracle": errs, "l2": "flushed before every timed call", "clocks": clk}
+
+
+def _dist_setup(dev, world):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    dist.init_process_group("nccl", device_id=dev)
+    return dist
+
+
+def run_workload(args, world, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if args.workload == "system_10k":
+        if rank != 0:
+            return 0
+        line = measure_system_10k(args, dev)
+    elif args.workload == "adjoint":
+        if rank != 0:
+            return 0
+        line = measure_adjoint(args, dev)
+    else:
+        dist = _dist_setup(dev, world)
+        fn = measure_multi_rhs if args.workload == "multi_rhs" else measure_batch
+        line = fn(args, dev, world=world, rank=rank, dist=dist)
+        if dist is not None:
+            dist.destroy_process_group()
+            if rank != 0:
+                return 0
+    line = {"workload_name": args.workload, "n_gpus": world, **line}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -762,7 +885,11 @@ def main(argv=None) -> int:
     ap.add_argument("--lanes", type=int, default=None)
     ap.add_argument("--chunk", type=int, default=None)
     ap.add_argument("--order-block", type=int, default=None)
-    ap.add_argument("--workload", choices=["deep_wide", "multi_rhs", "batch", "adjoint"], default="deep_wide")
+    ap.add_argument("--workload", choices=["deep_wide", "system_10k", "multi_rhs", "batch", "adjoint"],
+                    default="deep_wide")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default workload only: skip the 10k, multi-rhs, batch and adjoint measurements "
+                         "attached to its line")
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--scale", type=float, default=1.0,
                     help="size factor of the deep/wide systems (1.0 = the benchmark sizes; smaller for profiling)")
@@ -792,12 +919,8 @@ def main(argv=None) -> int:
     world, rank, local = dist_env()
     if args.impl == "reference":
         return run_reference(args, world, rank)
-    if args.workload == "multi_rhs":
-        return run_multi_rhs(args)
-    if args.workload == "batch":
-        return run_batch(args)
-    if args.workload == "adjoint":
-        return run_adjoint(args)
+    if args.workload != "deep_wide":
+        return run_workload(args, world, rank, local)
     return run_gpu(args, world, rank, local)
 
 

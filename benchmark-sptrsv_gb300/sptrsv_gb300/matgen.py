@@ -63,8 +63,6 @@ def _assemble_sorted(n: int, off_col: np.ndarray, off_row: np.ndarray, off_val: 
     per_col = np.bincount(off_col, minlength=n).astype(np.int64)
     col_ptr = np.zeros(n + 1, dtype=np.int64)
     np.cumsum(per_col + 1, out=col_ptr[1:])
-    first_off = np.zeros(n, dtype=np.int64)
-    np.cumsum(per_col[:-1], out=first_off[1:])
     nnz = int(col_ptr[-1])
     row_idx = np.empty(nnz, dtype=np.int32)
     val = np.empty(nnz, dtype=np.float64)
@@ -72,9 +70,11 @@ def _assemble_sorted(n: int, off_col: np.ndarray, off_row: np.ndarray, off_val: 
     row_idx[dpos] = np.arange(n, dtype=np.int32)
     val[dpos] = diag
     if off_col.shape[0]:
-        pos = col_ptr[off_col] + 1 + (np.arange(off_col.shape[0], dtype=np.int64) - first_off[off_col])
-        row_idx[pos] = off_row
-        val[pos] = off_val
+        # the off-diagonals fill every slot after each column's diagonal, in order
+        off = np.ones(nnz, dtype=bool)
+        off[dpos] = False
+        row_idx[off] = off_row
+        val[off] = off_val
     return CscTriangle(n, col_ptr.astype(np.int32), row_idx, val, True)
 
 
@@ -98,10 +98,10 @@ def banded_random_lower(n: int, counts: np.ndarray, band: int, seed_or_rng, lowe
         base[1:] = cs[seg_end[:-1]]
     total_w = cs[seg_end] - base if n else base
     col = np.repeat(j, k)
-    first = seg_end - k                               # first draw of each column
-    within = np.arange(col.shape[0], dtype=np.int64) - np.repeat(np.cumsum(k) - k, k)
-    u = (cs[first[col] + within] - base[col]) / total_w[col]
-    span = avail[col]
+    draw = np.ones(cs.shape[0], dtype=bool)           # every partial sum but the closing ones
+    draw[seg_end] = False
+    u = (cs[draw] - np.repeat(base, k)) / np.repeat(total_w, k)
+    span = np.repeat(avail, k)
     row = col + 1 + np.minimum((u * span).astype(np.int64), span - 1)
     if row.shape[0] > 1:
         keep = np.ones(row.shape[0], dtype=bool)
