@@ -1,9 +1,13 @@
 """Input preparation with the reference's semantics.
 
 * ``read_mtx``: a Matrix Market coordinate file (real / integer / pattern /
-  complex-real-part, general / symmetric / skew-symmetric) to CSR, with
-  symmetric storage expanded and duplicates summed (the reader of
-  SpTRSV_cuda/mmio_highlevel.h:8-134 and :137-296, restated).
+  complex-real-part) to CSR, as the reader of SpTRSV_cuda/mmio_highlevel.h:8-134
+  and :137-296 builds it: symmetric and hermitian storage expanded (the mirror
+  entry gets the same value), every other symmetry kind -- skew-symmetric
+  included -- read as stored. Two deliberate differences, neither of which
+  changes a solve: rows come out with ascending columns (the reference keeps
+  file order; the triangle's CSC is sorted by both), and duplicate entries are
+  summed (the reference keeps both copies, and its solvers add both).
 * ``extract_triangle``: the reference's -forward / -backward preparation
   (SpTRSV_cuda/main.cu:153-218): keep the strictly lower (forward) or strictly
   upper (backward) part of A, give every kept entry a value rand()%10+1 (here:
@@ -50,11 +54,10 @@ def read_mtx(path) -> tuple[int, int, np.ndarray, np.ndarray, np.ndarray]:
         vals = data[:, 2].astype(np.float64)   # complex: the real part
     if rows.size and (rows.min() < 0 or rows.max() >= m or cols.min() < 0 or cols.max() >= n):
         raise ValueError(f"{path}: index out of range")
-    if sym in ("symmetric", "skew-symmetric", "hermitian"):
+    if sym in ("symmetric", "hermitian"):   # mmio_highlevel.h:175-178 (mm_is_symmetric || mm_is_hermitian)
         off = rows != cols
-        sign = -1.0 if sym == "skew-symmetric" else 1.0
         rows, cols, vals = (np.concatenate([rows, cols[off]]), np.concatenate([cols, rows[off]]),
-                            np.concatenate([vals, sign * vals[off]]))
+                            np.concatenate([vals, vals[off]]))
     import scipy.sparse as sp
     a = sp.coo_matrix((vals, (rows, cols)), shape=(m, n)).tocsr()
     a.sum_duplicates()

@@ -165,6 +165,31 @@ def ref() -> _Impl | None:
     return _CACHE["ref"]
 
 
+def ref_read_mtx(path):
+    """The reference's Matrix Market reader (mmio_highlevel.h:8-134 mmio_info and
+    :137-296 mmio_data, compiled in place): (m, n, row_ptr, col_idx, val) of the CSR
+    it builds (rows in file order, symmetric and hermitian storage expanded,
+    duplicates kept), or None where the reference build is absent."""
+    imp = ref()
+    if imp is None:
+        return None
+    lib = imp.lib
+    fn = str(path).encode()
+    m, n, nnz, sym = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    lib.ref_mmio_info_f64.restype = ctypes.c_int
+    lib.ref_mmio_data_f64.restype = ctypes.c_int
+    rc = lib.ref_mmio_info_f64(ctypes.byref(m), ctypes.byref(n), ctypes.byref(nnz), ctypes.byref(sym), fn)
+    if rc != 0:
+        raise ValueError(f"{path}: reference reader status {rc}")
+    row_ptr = np.zeros(m.value + 1, dtype=np.int32)
+    col_idx = np.zeros(max(nnz.value, 1), dtype=np.int32)
+    val = np.zeros(max(nnz.value, 1), dtype=np.float64)
+    rc = lib.ref_mmio_data_f64(_p(row_ptr), _p(col_idx), _p(val), fn)
+    if rc != 0:
+        raise ValueError(f"{path}: reference reader status {rc}")
+    return m.value, n.value, row_ptr, col_idx[:nnz.value], val[:nnz.value]
+
+
 def csc_spmv(col_ptr, row_idx, val, n, x):
     """b = L x in the order of main.cu:347-358 (via the port)."""
     lib = port().lib

@@ -12,6 +12,8 @@
  *   sptrsv_syncfree_executor  sptrsv_syncfree_serialref.h:25-108
  *   matrix_transposition      tranpose.h:6-43
  *   findlevel / findlevel_csc findlevel.h:6-69, 71-147
+ *   mmio_info / mmio_data     mmio_highlevel.h:8-134, 137-296 (Matrix Market
+ *                             reader, with mmio.h)
  */
 #include <time.h>
 #include <stdio.h>
@@ -37,6 +39,7 @@ void exclusive_scan(T *a, int len)
 #include "sptrsv_syncfree_serialref.h"
 #include "tranpose.h"
 #include "findlevel.h"
+#include "mmio_highlevel.h"
 }
 
 extern "C" {
@@ -67,5 +70,13 @@ int WRAP(ref_findlevel_csc)(const int *col_ptr, const int *row_idx, const VALUE_
                             int *pmax)
 {
     return findlevel_csc(col_ptr, row_idx, val, m, n, nnz, nlevel, pmin, pavg, pmax);
+}
+int WRAP(ref_mmio_info)(int *m, int *n, int *nnz, int *is_symmetric, const char *filename)
+{
+    return mmio_info(m, n, nnz, is_symmetric, const_cast<char *>(filename));
+}
+int WRAP(ref_mmio_data)(int *row_ptr, int *col_idx, VALUE_TYPE *val, const char *filename)
+{
+    return mmio_data(row_ptr, col_idx, val, const_cast<char *>(filename));
 }
 }
