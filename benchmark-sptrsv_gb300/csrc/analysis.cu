@@ -606,12 +606,18 @@ cudaError_t launch_levels(const int* col_ptr, const int* row_idx, const int* in_
 // system / block) * count + system (second, stable pass of the blocked level
 // order; batches interleave their systems block by block).
 __global__ void k_schedule_keys(const int* __restrict__ rows, const int* __restrict__ depth, int n, SysDesc sd,
-                                int block, int mode, unsigned* keys) {
+                                int block, int mode, unsigned* keys, const int* __restrict__ sys_depth,
+                                int max_depth) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
     const int r = rows[i];
     if (mode == 0) {
       keys[i] = static_cast<unsigned>(depth[r]);
+    } else if (mode == 2) {
+      // the level stretched to the batch's depth: floor(level * D / D_s) grows
+      // strictly with the level inside system s (D >= D_s)
+      const long long ds = sys_depth[sd.sys_of[r]];
+      keys[i] = static_cast<unsigned>((long long)depth[r] * max_depth / (ds > 0 ? ds : 1));
     } else {
       long long off, nat;
       nat_of(sd, n, r, &off, &nat);
@@ -621,9 +627,21 @@ __global__ void k_schedule_keys(const int* __restrict__ rows, const int* __restr
   }
 }
 cudaError_t launch_schedule_keys(const int* rows, const int* depth, int n, const SysDesc& sd, int block, int mode,
-                                 unsigned* keys, cudaStream_t s) {
+                                 unsigned* keys, cudaStream_t s, const int* sys_depth, int max_depth) {
   if (n <= 0) return cudaSuccess;
-  k_schedule_keys<<<grid_for(n), kThreads, 0, s>>>(rows, depth, n, sd, block, mode, keys);
+  k_schedule_keys<<<grid_for(n), kThreads, 0, s>>>(rows, depth, n, sd, block, mode, keys, sys_depth, max_depth);
+  return cudaGetLastError();
+}
+
+// sys_depth[s] = 1 + the deepest level of system s (zeroed by the caller)
+__global__ void k_sys_depth(const int* __restrict__ depth, const int* __restrict__ sys_of, int n, int* sys_depth) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n; r += stride)
+    atomicMax(&sys_depth[sys_of[r]], depth[r] + 1);
+}
+cudaError_t launch_sys_depth(const int* depth, const int* sys_of, int n, int* sys_depth, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_sys_depth<<<grid_for(n), kThreads, 0, s>>>(depth, sys_of, n, sys_depth);
   return cudaGetLastError();
 }
 

@@ -50,6 +50,9 @@ struct sptrsv_gb300_handle_s {
   int wsync = 0;
   int split = 32;
   int wsync_batch = 0;   // 0: automatic (2 for short lists, else 1)
+  int opt_option = SPTRSV_OPT_WARP_AUTO;  // push, many rhs: the reference's lane mode
+  int rhs_tile_option = 0;                // many rhs: right-hand sides per lane (0: automatic)
+  int stretch_option = 1;                 // batches in level order: levels stretched to the batch depth
   unsigned long long user_set = 0;  // options the caller set explicitly (bit = option id)
   // executor settings chosen from the analysis for SPTRSV_SCHED_AUTO (one rhs)
   struct AutoPlan {
@@ -83,6 +86,7 @@ struct sptrsv_gb300_handle_s {
   int* level_ptr_nat = nullptr;
   Layout layout;
   int layout_block = -1;
+  int layout_stretched = 0;        // the layout's level order is stretched per system (batches)
   std::vector<int> layout_units;   // blocked layouts: start positions of the units (+ n), else empty
   std::vector<int> dep_cnt_host;   // dependencies per position
   std::vector<int> out_cnt_host;   // dependents per position
@@ -317,6 +321,12 @@ int read_flags(sptrsv_gb300_handle_s* h, cudaStream_t s, int* flags) {
 }
 
 // Builds the position-space layout for the given order block.
+// Batches in level order (not for the level-set executor, which needs whole
+// levels): each system's levels stretched to the batch's depth.
+bool want_stretch(const sptrsv_gb300_handle_s* h, int block) {
+  return h->batch_count > 1 && block >= h->n && h->stretch_option && h->sched_option != SCHED_LEVELSET;
+}
+
 int build_layout(sptrsv_gb300_handle_s* h, int block, cudaStream_t s) {
   free_layout(h->layout);
   free_table(h->tab_fwd);
@@ -349,6 +359,7 @@ int build_layout(sptrsv_gb300_handle_s* h, int block, cudaStream_t s) {
   ST_TRY(dev_alloc(h, &L.diag_src, n));
 
   const bool level_order = block >= n;
+  const bool stretched = want_stretch(h, block);
   h->layout_units.clear();
   if (n > 0) {
     // natural order rows
@@ -372,7 +383,18 @@ int build_layout(sptrsv_gb300_handle_s* h, int block, cudaStream_t s) {
       CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&rows_ls), sizeof(int) * n, s));
       CUDA_TRY(launch_long_keys(rows_nat, h->in_degree, n, kLongDeps, keys, s));
       CUDA_TRY(radix_sort_pairs(keys, rows_nat, keys_sorted, rows_ls, n, 1, temp, s));
-      CUDA_TRY(launch_schedule_keys(rows_ls, h->depth, n, sd, block, 0, keys, s));
+      if (stretched) {
+        // every system's levels spread over the batch's depth, so a deep system's
+        // chain does not queue behind the shallow systems' wide levels
+        int* sys_depth = nullptr;
+        CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&sys_depth), sizeof(int) * h->batch_count, s));
+        CUDA_TRY(cudaMemsetAsync(sys_depth, 0, sizeof(int) * h->batch_count, s));
+        CUDA_TRY(launch_sys_depth(h->depth, h->sys_of, n, sys_depth, s));
+        CUDA_TRY(launch_schedule_keys(rows_ls, h->depth, n, sd, block, 2, keys, s, sys_depth, h->nlevels));
+        CUDA_TRY(cudaFreeAsync(sys_depth, s));
+      } else {
+        CUDA_TRY(launch_schedule_keys(rows_ls, h->depth, n, sd, block, 0, keys, s));
+      }
       CUDA_TRY(radix_sort_pairs(keys, rows_ls, keys_sorted, level_order ? L.perm : rows_lv, n,
                                 bits_for(h->nlevels - 1), temp, s));
       CUDA_TRY(cudaFreeAsync(rows_ls, s));
@@ -429,7 +451,7 @@ int build_layout(sptrsv_gb300_handle_s* h, int block, cudaStream_t s) {
       h->max_out_cnt = std::max(h->max_out_cnt, h->out_cnt_host[p]);
     }
   }
-  if (level_order) {
+  if (level_order && !stretched) {
     L.nlevels = h->nlevels;
     L.level_ptr_host.assign(h->nlevels + 1, 0);
     for (int l = 0; l < h->nlevels; ++l) L.level_ptr_host[l + 1] = L.level_ptr_host[l] + h->level_sizes_host[l];
@@ -439,6 +461,7 @@ int build_layout(sptrsv_gb300_handle_s* h, int block, cudaStream_t s) {
   }
   CUDA_TRY(cudaStreamSynchronize(s));
   h->layout_block = block;
+  h->layout_stretched = stretched ? 1 : 0;
   return SPTRSV_OK;
 }
 
@@ -824,7 +847,8 @@ int make_plan(sptrsv_gb300_handle_s* h, const std::vector<int>& row_ptr, cudaStr
 int ensure_layout(sptrsv_gb300_handle_s* h, cudaStream_t s) {
   const int want = effective_block(h);
   const int have = h->layout_block;
-  const bool same = (want >= h->n && have >= h->n) || want == have;
+  const bool same = ((want >= h->n && have >= h->n) || want == have) &&
+                    (want_stretch(h, want) ? 1 : 0) == h->layout_stretched;
   if (same && h->layout.perm != nullptr) return SPTRSV_OK;
   if (h->n == 0 && have >= 0) return SPTRSV_OK;
   return build_layout(h, want, s);
@@ -893,7 +917,9 @@ ExecConfig pick_config(const sptrsv_gb300_handle_s* h, int rhs) {
   c.block = h->block_option > 0 ? h->block_option : 256;
   // one-rhs: one unknown per consumer thread per chunk; many rhs: one unknown per
   // lane group (the group width the multi-rhs executors pick for this rhs)
-  const int group = rhs <= 4 ? 4 : rhs <= 8 ? 8 : rhs <= 16 ? 16 : 32;
+  c.opt = h->opt_option;
+  c.rhs_tile = h->rhs_tile_option;
+  const int group = multi_group(rhs, c.rhs_tile, nullptr);
   c.chunk = h->chunk_option > 0 ? h->chunk_option : (rhs == 1 ? 224 : std::max(1, c.block / group));
   c.sleep_max = static_cast<unsigned>(h->backoff_ns);
   c.ctas_per_sm = h->ctas_per_sm;
@@ -1210,6 +1236,17 @@ static int set_option_value(sptrsv_handle_t h, int option, long long value) {
     case SPTRSV_OPTION_FUSED_REFINE:
       h->fused_refine = value != 0;
       return SPTRSV_OK;
+    case SPTRSV_OPTION_OPT:
+      if (value < SPTRSV_OPT_WARP_NNZ || value > SPTRSV_OPT_WARP_AUTO) return SPTRSV_ERR_INVALID;
+      h->opt_option = static_cast<int>(value);
+      return SPTRSV_OK;
+    case SPTRSV_OPTION_RHS_TILE:
+      if (!(value == 0 || value == 1 || value == 2 || value == 4)) return SPTRSV_ERR_INVALID;
+      h->rhs_tile_option = static_cast<int>(value);
+      return SPTRSV_OK;
+    case SPTRSV_OPTION_STRETCH:
+      h->stretch_option = value != 0;
+      return SPTRSV_OK;
     default:
       return SPTRSV_ERR_INVALID;
   }
@@ -1240,6 +1277,9 @@ int sptrsv_gb300_get_option(sptrsv_handle_t h, int option, long long* value) {
     case SPTRSV_OPTION_IMPORT: *value = h->import_option; break;
     case SPTRSV_OPTION_UNIT_PIPELINE: *value = h->pipe_option; break;
     case SPTRSV_OPTION_FUSED_REFINE: *value = h->fused_refine; break;
+    case SPTRSV_OPTION_OPT: *value = h->opt_option; break;
+    case SPTRSV_OPTION_RHS_TILE: *value = h->rhs_tile_option; break;
+    case SPTRSV_OPTION_STRETCH: *value = h->stretch_option; break;
     default: return SPTRSV_ERR_INVALID;
   }
   return SPTRSV_OK;
@@ -1880,11 +1920,27 @@ int sptrsv_gb300_tune(sptrsv_handle_t h, const void* d_val, int dtype, int rhs, 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   struct Cand {
     int sched, order_block, chunk, staged, backoff, ctas, lanes, stages, wsync, block, split, batch = 0;
+    int smem = 1, opt = SPTRSV_OPT_WARP_AUTO, tile = 0;
   };
   const int n = h->n;
   const int big = INT_MAX;
   std::vector<Cand> cands;
   const int sp = 32;  // split length of the warp-synchronous candidates
+  // Order blocks from the analysis: blocks of 16, 32 and 64 average level
+  // widths (the automatic plan's locality test uses 32), multiples of 32
+  // unknowns, kept between 1024 and 32768 and below n; plus the plan's own.
+  std::vector<int> blocks;
+  if (n > 0 && h->nlevels > 0) {
+    const long long width = ((long long)n + h->nlevels - 1) / h->nlevels;
+    for (int f : {16, 32, 64}) {
+      long long b = (f * width + 31) / 32 * 32;
+      b = std::min<long long>(32768, std::max<long long>(1024, b));
+      if (b < n && std::find(blocks.begin(), blocks.end(), (int)b) == blocks.end()) blocks.push_back((int)b);
+    }
+    if (h->plan.valid && h->plan.order_block < n &&
+        std::find(blocks.begin(), blocks.end(), h->plan.order_block) == blocks.end())
+      blocks.push_back(h->plan.order_block);
+  }
   if (rhs == 1) {
     // staged warp-specialised executor, level order
     for (int bo : {0, 256}) cands.push_back({SCHED_PULL, big, 224, 1, bo, 0, 1, 2, 0, 256, sp});
@@ -1898,20 +1954,36 @@ int sptrsv_gb300_tune(sptrsv_handle_t h, const void* d_val, int dtype, int rhs, 
       cands.push_back({SCHED_PULL, big, 256, 0, 0, ct, 1, 2, 1, 256, 0});
       cands.push_back({SCHED_PULL, big, 128, 0, 0, ct, 1, 2, 1, 128, sp});
     }
-    for (int ob : {2048, 8192, 22624}) cands.push_back({SCHED_PULL, ob, ob, 0, 0, 0, 1, 2, 1, 128, sp});
-    for (int bt : {1, 2, 4}) cands.push_back({SCHED_PULL, 22624, 22624, 0, 0, 0, 1, 2, 1, 128, sp, bt});
+    // in-chunk dependencies through global memory only (no shared-memory tier)
+    cands.push_back({SCHED_PULL, big, 256, 0, 0, 2, 1, 2, 1, 256, sp, 0, 0});
+    for (int ob : blocks) {
+      cands.push_back({SCHED_PULL, ob, ob, 0, 0, 0, 1, 2, 1, 128, sp});
+      for (int bt : {1, 2, 4}) cands.push_back({SCHED_PULL, ob, ob, 0, 0, 0, 1, 2, 1, 128, sp, bt});
+    }
     // thread-per-unknown executor, level order
     cands.push_back({SCHED_PULL, big, 256, 0, 128, 1, 1, 2, 0, 256, sp});
     cands.push_back({SCHED_LEVELSET, big, 256, 0, 256, 1, 8, 2, 0, 256, sp});
     cands.push_back({SCHED_PUSH, 1024, 1024, 0, 256, 0, 1, 2, 0, 256, sp});
+    cands.push_back({SCHED_PUSH, 1024, 1024, 0, 256, 0, 1, 2, 0, 256, sp, 0, 0});
   } else {
-    // chunk 0 = one unknown per lane group
+    // chunk 0 = one unknown per lane group; right-hand-side tiles (1, 2, 4 per lane)
     for (int bo : {64, 512}) cands.push_back({SCHED_PULL, big, 0, 0, bo, 0, 1, 2, 1, 256, sp});
-    for (int ct : {1, 2, 3}) cands.push_back({SCHED_PULL, big, 0, 0, 0, ct, 1, 2, 1, 256, sp});
-    for (int ob : {1024, 4096, 16384}) cands.push_back({SCHED_PULL, ob, ob, 0, 0, 0, 1, 2, 1, 256, sp});
+    std::vector<int> groups;   // distinct (lanes, right-hand sides per lane) pairs
+    for (int tile : {1, 2, 4}) {
+      int rpl = 1;
+      const int key = multi_group(rhs, tile, &rpl) * 8 + rpl;
+      if (std::find(groups.begin(), groups.end(), key) != groups.end()) continue;
+      groups.push_back(key);
+      for (int ct : {1, 2, 3})
+        cands.push_back({SCHED_PULL, big, 0, 0, 0, ct, 1, 2, 1, 256, sp, 0, 1, SPTRSV_OPT_WARP_AUTO, tile});
+    }
+    cands.push_back({SCHED_PULL, big, 0, 0, 0, 0, 1, 2, 1, 256, sp, 0, 0});   // global-memory tier only
+    for (int ob : blocks) cands.push_back({SCHED_PULL, ob, ob, 0, 0, 0, 1, 2, 1, 256, sp});
     cands.push_back({SCHED_PULL, big, 0, 0, 256, 0, 1, 2, 0, 256, sp});
     cands.push_back({SCHED_LEVELSET, big, 256, 0, 256, 1, 8, 2, 0, 256, sp});
-    cands.push_back({SCHED_PUSH, big, 0, 0, 256, 0, 1, 2, 0, 256, sp});
+    // the reference's scheme with its three lane modes
+    for (int o : {SPTRSV_OPT_WARP_NNZ, SPTRSV_OPT_WARP_RHS, SPTRSV_OPT_WARP_AUTO})
+      cands.push_back({SCHED_PUSH, big, 0, 0, 256, 0, 1, 2, 0, 256, sp, 0, 1, o, 0});
   }
   (void)n;
   const int saved_check = h->sync_check, saved_profile = h->profile;
@@ -1936,6 +2008,9 @@ int sptrsv_gb300_tune(sptrsv_handle_t h, const void* d_val, int dtype, int rhs, 
     h->block_option = c.block;
     h->split = c.split;
     h->wsync_batch = c.batch;
+    h->cfg.smem_tier = c.smem;
+    h->opt_option = c.opt;
+    h->rhs_tile_option = c.tile;
     int st = sptrsv_gb300_solve(h, d_val, dtype, rhs, layout, d_b, d_x, stream);
     if (st == SPTRSV_OK) st = check_device(h, s);
     if (st != SPTRSV_OK) continue;  // a candidate that fails (or times out) is skipped
@@ -1976,6 +2051,9 @@ int sptrsv_gb300_tune(sptrsv_handle_t h, const void* d_val, int dtype, int rhs, 
   h->block_option = c.block;
   h->split = c.split;
   h->wsync_batch = c.batch;
+  h->cfg.smem_tier = c.smem;
+  h->opt_option = c.opt;
+  h->rhs_tile_option = c.tile;
   ST_TRY(ensure_layout(h, s));
   ST_TRY(stage_values(h, d_val, dtype, s, false));
   if (best_ms) *best_ms = best;
@@ -2034,7 +2112,6 @@ int sptrsv_gb300_syncfree_host(const int* cscColPtrTR, const int* cscRowIdxTR, c
                                int nnzTR, int substitution, int rhs, int opt, double* x, const double* b,
                                const double* x_ref, double* gflops, double* solve_ms, double* analysis_ms,
                                double* l1_err) {
-  (void)opt;
   if (m != n) {
     if (g_verbose) printf("This is not a square matrix, return.\n");
     return SPTRSV_ERR_NOT_SQUARE;
@@ -2081,6 +2158,9 @@ int sptrsv_gb300_syncfree_host(const int* cscColPtrTR, const int* cscRowIdxTR, c
     t_an /= g_bench_repeat;
     if (g_verbose) printf("cuda syncfree SpTRSV analysis on L used %4.2f ms\n", t_an);
     if ((st = sptrsv_gb300_create(&h)) != SPTRSV_OK) break;
+    // the reference's lane mode for many right-hand sides (used by the push
+    // schedule, the reference's own scheme; out-of-range values keep AUTO)
+    if (opt >= SPTRSV_OPT_WARP_NNZ && opt <= SPTRSV_OPT_WARP_AUTO) sptrsv_gb300_set_option(h, SPTRSV_OPTION_OPT, opt);
     if ((st = sptrsv_gb300_analyse(h, m, n, nnzTR, d_ptr, d_row, substitution, nullptr)) != SPTRSV_OK) break;
     if ((st = sptrsv_gb300_set_values(h, d_val, SPTRSV_DTYPE_F64, nullptr)) != SPTRSV_OK) break;
     for (int i = 0; i < g_bench_repeat; ++i) {

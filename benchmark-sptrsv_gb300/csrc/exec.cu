@@ -30,6 +30,7 @@ namespace {
 template <typename T>
 struct ExecArgs {
   int n, rhs, chunk, nchunks, smem_tier, ctas_per_sm;
+  int opt;  // push, many rhs: lane mode (1 over entries, 2 over rhs, 3 the reference's rule per column)
   // pull walks: chunk c covers walk indices [c*chunk - walk_pad, (c+1)*chunk - walk_pad);
   // the reverse (adjoint) walk is shifted so its chunks line up with order blocks
   int walk_pad;
@@ -1157,6 +1158,11 @@ __global__ void __launch_bounds__(256) k_push_multi(ExecArgs<T> a) {
       __syncwarp(gmask);
       const T rc = a.rcp[p];
       const int o0 = a.out_ptr[p], o1 = a.out_ptr[p + 1];
+      // Lanes over right-hand sides (the loop below) or over the column's
+      // entries (after it); the automatic mode is the reference's rule
+      // (SpTRSV_cuda/sptrsv_syncfree_cuda.h:258-262), decided per column.
+      const int len = o1 - o0;
+      const bool rhs_lanes = a.opt == 2 || (a.opt != 1 && (len <= rhs || rhs > 16) && len < 2048);
       for (int kt = 0; kt < rhs; kt += G * RPL) {
         T xi[RPL];
 #pragma unroll
@@ -1174,6 +1180,7 @@ __global__ void __launch_bounds__(256) k_push_multi(ExecArgs<T> a) {
             a.x[(long long)col * a.x_si + (long long)k * a.x_sk] = xi[j];
           }
         }
+        if (!rhs_lanes) continue;
         for (int e = o0; e < o1; ++e) {
           const int tp = a.out_pos[e];
           const T v = a.out_val[e];
@@ -1185,6 +1192,21 @@ __global__ void __launch_bounds__(256) k_push_multi(ExecArgs<T> a) {
               if (sizeof(T) == 8) red_add_f64(reinterpret_cast<double*>(dst), (double)(xi[j] * v));
               else red_add_f32(reinterpret_cast<float*>(dst), (float)(xi[j] * v));
             }
+          }
+        }
+      }
+      if (!rhs_lanes) {
+        // lanes over entries: each lane pushes x_p * L(r, p) of its dependents for
+        // every right-hand side, reading x_p back (written by the group above)
+        __syncwarp(gmask);
+        for (int e = o0 + lane; e < o1; e += G) {
+          const int tp = a.out_pos[e];
+          const T v = a.out_val[e];
+          for (int k = 0; k < rhs; ++k) {
+            T* dst = &a.left_sum[(long long)tp * rhs + k];
+            const T xk = a.x[(long long)col * a.x_si + (long long)k * a.x_sk];
+            if (sizeof(T) == 8) red_add_f64(reinterpret_cast<double*>(dst), (double)(xk * v));
+            else red_add_f32(reinterpret_cast<float*>(dst), (float)(xk * v));
           }
         }
       }
@@ -1329,17 +1351,28 @@ cudaError_t launch_pull_impl(ExecArgs<T>& a, int rhs, const ExecConfig& cfg, siz
       default: return run(k_pull_vec<T, 32, false, 1, ADJ>, a, block, smem, num_sms, s);
     }
   }
-  // many right-hand sides: lanes over rhs
+  // many right-hand sides: lanes over rhs, G lanes per unknown covering RPL
+  // right-hand sides each (the right-hand-side tile, multi_group)
   if (cfg.wsync && rhs <= 64 && a.grad == nullptr) {
     if (cfg.exact) {
       if (rhs <= 8) return run(k_pull_wsync_multi<T, true, ADJ, 8, 1>, a, block, smem, num_sms, s);
       return run(k_pull_wsync_multi<T, true, ADJ, 32, 2>, a, block, smem, num_sms, s);
     }
-    if (rhs <= 4) return run(k_pull_wsync_multi<T, false, ADJ, 4, 1>, a, block, smem, num_sms, s);
-    if (rhs <= 8) return run(k_pull_wsync_multi<T, false, ADJ, 8, 1>, a, block, smem, num_sms, s);
-    if (rhs <= 16) return run(k_pull_wsync_multi<T, false, ADJ, 16, 1>, a, block, smem, num_sms, s);
-    if (rhs <= 32) return run(k_pull_wsync_multi<T, false, ADJ, 32, 1>, a, block, smem, num_sms, s);
-    return run(k_pull_wsync_multi<T, false, ADJ, 32, 2>, a, block, smem, num_sms, s);
+    int rpl = 1;
+    const int g = multi_group(rhs, cfg.rhs_tile, &rpl);
+    switch (g * 8 + rpl) {
+      case 4 * 8 + 1: return run(k_pull_wsync_multi<T, false, ADJ, 4, 1>, a, block, smem, num_sms, s);
+      case 8 * 8 + 1: return run(k_pull_wsync_multi<T, false, ADJ, 8, 1>, a, block, smem, num_sms, s);
+      case 16 * 8 + 1: return run(k_pull_wsync_multi<T, false, ADJ, 16, 1>, a, block, smem, num_sms, s);
+      case 32 * 8 + 1: return run(k_pull_wsync_multi<T, false, ADJ, 32, 1>, a, block, smem, num_sms, s);
+      case 4 * 8 + 2: return run(k_pull_wsync_multi<T, false, ADJ, 4, 2>, a, block, smem, num_sms, s);
+      case 8 * 8 + 2: return run(k_pull_wsync_multi<T, false, ADJ, 8, 2>, a, block, smem, num_sms, s);
+      case 16 * 8 + 2: return run(k_pull_wsync_multi<T, false, ADJ, 16, 2>, a, block, smem, num_sms, s);
+      case 32 * 8 + 2: return run(k_pull_wsync_multi<T, false, ADJ, 32, 2>, a, block, smem, num_sms, s);
+      case 4 * 8 + 4: return run(k_pull_wsync_multi<T, false, ADJ, 4, 4>, a, block, smem, num_sms, s);
+      case 8 * 8 + 4: return run(k_pull_wsync_multi<T, false, ADJ, 8, 4>, a, block, smem, num_sms, s);
+      default: return run(k_pull_wsync_multi<T, false, ADJ, 16, 4>, a, block, smem, num_sms, s);
+    }
   }
   if (cfg.exact) {
     if (rhs <= 8) return run(k_pull_multi<T, 8, 1, true, ADJ>, a, block, smem, num_sms, s);
@@ -1456,6 +1489,7 @@ cudaError_t launch_push(const Layout& L, const Values<T>& V, int rhs, const VecV
     }
   }
   a.smem_tier = 0;
+  a.opt = cfg.opt;
   if (rhs <= 4) return run(k_push_multi<T, 4, 1>, a, block, 0, num_sms, s);
   if (rhs <= 8) return run(k_push_multi<T, 8, 1>, a, block, 0, num_sms, s);
   if (rhs <= 16) return run(k_push_multi<T, 16, 1>, a, block, 0, num_sms, s);

@@ -38,7 +38,27 @@ struct ExecConfig {
   int wsync = 0;          // unstaged one-rhs pull: warp-synchronous lanes (k_pull_wsync)
   int split = 0;          // warp-synchronous, fast arithmetic: split lists longer than this (0: never)
   int wsync_batch = 4;    // warp-synchronous one rhs, fast arithmetic: dependencies per lane per iteration
+  int opt = 3;            // push, many rhs: the reference's lane mode (1 entries, 2 rhs, 3 automatic rule)
+  int rhs_tile = 0;       // many rhs: right-hand sides per lane (1, 2, 4; 0: automatic)
 };
+
+// Lane group of the many-rhs executors: G lanes per unknown (a power of two,
+// 4..32), each covering `rpl` right-hand sides, with G * rpl >= rhs when
+// rhs <= 128. rhs_tile = 0 picks one right-hand side per lane up to 32 and two
+// beyond; otherwise rpl = rhs_tile where that keeps G >= 4 (else the next
+// smaller tile).
+inline int multi_group(int rhs, int rhs_tile, int* rpl_out) {
+  int rpl = rhs_tile > 0 ? rhs_tile : (rhs <= 32 ? 1 : 2);
+  if (rpl != 1 && rpl != 2 && rpl != 4) rpl = 1;
+  while (rpl > 1 && (rhs + rpl - 1) / rpl < 4) rpl >>= 1;
+  if (rpl < 2 && rhs > 32) rpl = 2;
+  if (rpl < 4 && rhs > 64) rpl = 4;
+  const int need = (rhs + rpl - 1) / rpl;
+  int g = 4;
+  while (g < need && g < 32) g <<= 1;
+  if (rpl_out) *rpl_out = rpl;
+  return g;
+}
 
 // Work units of the staged executor: chunk k covers walk indices
 // [start[k], start[k+1]) (positions for a forward walk, reversed positions for
@@ -191,8 +211,12 @@ cudaError_t launch_gather_int(const int* src, const int* idx, int* out, int coun
 cudaError_t launch_levels(const int* col_ptr, const int* row_idx, const int* in_degree, int n,
                           int* cnt_scratch, int* front_a, int* front_b, int* depth, int* level_sizes,
                           DeviceCtl* ctl, unsigned long long timeout_ns, cudaStream_t s);
+// mode 0: level; 1: (natural block, system) of blocked orders; 2: the level
+// stretched to the batch depth, floor(level * max_depth / sys_depth[system])
 cudaError_t launch_schedule_keys(const int* rows, const int* depth, int n, const SysDesc& sd, int block,
-                                 int mode, unsigned* keys, cudaStream_t s);
+                                 int mode, unsigned* keys, cudaStream_t s, const int* sys_depth = nullptr,
+                                 int max_depth = 0);
+cudaError_t launch_sys_depth(const int* depth, const int* sys_of, int n, int* sys_depth, cudaStream_t s);
 cudaError_t launch_inverse_perm(const int* perm, int n, int* iperm, cudaStream_t s);
 // key = 0 for rows with more than `threshold` dependencies, 1 otherwise
 cudaError_t launch_long_keys(const int* rows, const int* in_degree, int n, int threshold, unsigned* keys,

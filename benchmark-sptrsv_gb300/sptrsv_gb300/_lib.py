@@ -63,6 +63,9 @@ OPTION_WSYNC_BATCH = 18
 OPTION_IMPORT = 19
 OPTION_UNIT_PIPELINE = 20
 OPTION_FUSED_REFINE = 21
+OPTION_OPT = 22
+OPTION_RHS_TILE = 23
+OPTION_STRETCH = 24
 
 NOALLOC_MAX_N = 262144  # SPTRSV_NOALLOC_MAX_N
 

@@ -106,7 +106,8 @@ class SyncFreeSolver:
                  staged: bool | None = None, stage_entries: int | None = None, stages: int | None = None,
                  warp_sync: bool | None = None, split: int | None = None, wsync_batch: int | None = None,
                  import_deps: bool | None = None, unit_pipeline: int | None = None, fused_grad: bool | None = None,
-                 fused_refine: bool | None = None, stream=None):
+                 fused_refine: bool | None = None, opt: int | None = None, rhs_tile: int | None = None,
+                 stretch: bool | None = None, stream=None):
         torch = _torch()
         self._lib = load()
         self.device = torch.device("cuda", torch.cuda.current_device())
@@ -150,7 +151,9 @@ class SyncFreeSolver:
                        (_lib.OPTION_WARP_SYNC, warp_sync), (_lib.OPTION_SPLIT, split),
                        (_lib.OPTION_WSYNC_BATCH, wsync_batch), (_lib.OPTION_IMPORT, import_deps),
                        (_lib.OPTION_UNIT_PIPELINE, unit_pipeline),
-                       (_lib.OPTION_FUSED_GRAD, fused_grad), (_lib.OPTION_FUSED_REFINE, fused_refine)):
+                       (_lib.OPTION_FUSED_GRAD, fused_grad), (_lib.OPTION_FUSED_REFINE, fused_refine),
+                       (_lib.OPTION_OPT, opt), (_lib.OPTION_RHS_TILE, rhs_tile),
+                       (_lib.OPTION_STRETCH, stretch)):
             if v is not None:
                 self.set_option(opt, int(v))
         self._stream = stream
@@ -316,7 +319,7 @@ class SyncFreeSolver:
         return dval
 
     TUNED_OPTIONS = ("SCHEDULE", "ORDER_BLOCK", "CHUNK", "STAGED", "BACKOFF_NS", "CTAS_PER_SM", "LANES", "STAGES",
-                     "WARP_SYNC", "BLOCK", "SPLIT", "WSYNC_BATCH")
+                     "WARP_SYNC", "BLOCK", "SPLIT", "WSYNC_BATCH", "SMEM_TIER", "OPT", "RHS_TILE")
 
     def tune(self, b, values=None, reps: int = 3) -> dict:
         """Autotune the executor on this right-hand side; returns the chosen options and time."""

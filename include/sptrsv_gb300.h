@@ -116,11 +116,29 @@ typedef enum sptrsv_option {
                                      SPTRSV_OPTION_STAGES buffers, default 3) and an importer warp, with
                                      a ring of up to 8192 value slots per unit; a power of two from 128
                                      to 8192 = that ring size cap; 0 (default) = off */
-  SPTRSV_OPTION_FUSED_REFINE = 21 /* sptrsv_gb300_solve_refine: 1 (default) = the FP32 solve, the FP64
+  SPTRSV_OPTION_FUSED_REFINE = 21, /* sptrsv_gb300_solve_refine: 1 (default) = the FP32 solve, the FP64
                                      residual and the FP32 correction of the first refinement step run
                                      as one pass over the dependency DAG (pull schedules, rhs <= 64,
                                      and for one rhs only where no dependency list is split over
                                      lanes); 0 = separate passes */
+  SPTRSV_OPTION_OPT = 22,         /* the reference's opt argument (sptrsv_syncfree_cuda.h:234-286) for
+                                     solves with several right-hand sides on the push schedule (the
+                                     reference's scheme): SPTRSV_OPT_WARP_NNZ = the lanes of a column's
+                                     group take its entries, each looping over the right-hand sides;
+                                     SPTRSV_OPT_WARP_RHS = the lanes take right-hand sides, looping over
+                                     the entries; SPTRSV_OPT_WARP_AUTO (default) = the reference's rule
+                                     per column: right-hand-side lanes when (entries <= rhs or rhs > 16)
+                                     and entries < 2048. The pull executors always put lanes over
+                                     right-hand sides (tile: SPTRSV_OPTION_RHS_TILE) */
+  SPTRSV_OPTION_RHS_TILE = 23,    /* pull executors with several right-hand sides: right-hand sides each
+                                     lane covers, 1, 2 or 4 (so 4-32 lanes per unknown); 0 (default) =
+                                     one per lane up to 32 right-hand sides, two beyond */
+  SPTRSV_OPTION_STRETCH = 24      /* batches in level order (not the level-set schedule): 1 (default) =
+                                     the schedule key of an unknown is its level stretched to the
+                                     batch's depth, floor(level * depth(batch) / depth(system)), so every
+                                     system's chain spreads over the whole launch instead of a deep
+                                     system waiting behind the shallow systems' wide levels; 0 = global
+                                     level order */
 } sptrsv_option;
 
 typedef struct sptrsv_info {
@@ -299,10 +317,17 @@ int sptrsv_gb300_graph_create(sptrsv_handle_t handle, int kind, int dtype, int r
 int sptrsv_gb300_graph_launch(void *graph, void *stream);
 int sptrsv_gb300_graph_destroy(void *graph);
 
-/* Autotuner: times candidate executor configurations (executor family, order
- * block, chunk size, staging, poll backoff, residency, lanes) on this
- * request, `reps` timed solves each, skips candidates that fail, and leaves
- * the fastest configuration set on the handle (values re-staged from d_val).
+/* Autotuner: times candidate executor configurations on this request,
+ * `reps` timed solves each, skips candidates that fail, and leaves the
+ * fastest configuration set on the handle (values re-staged from d_val).
+ * Axes: executor family (pull warp-synchronous / staged / thread per unknown,
+ * level sets, push), order block (candidates derived from the analysed level
+ * widths: blocks of 16, 32 and 64 average level widths, besides global level
+ * order), chunk size, threads per CTA, residency, poll back-off, lockstep
+ * batch, split lists, shared- vs global-memory tier for in-chunk dependencies
+ * (SPTRSV_OPTION_SMEM_TIER) and, with several right-hand sides, the
+ * right-hand-side tile (SPTRSV_OPTION_RHS_TILE) and the reference's lane
+ * modes (SPTRSV_OPTION_OPT) on the push schedule.
  * *best_ms (may be NULL) receives its median solve time. Read the chosen
  * options back with sptrsv_gb300_get_option. */
 int sptrsv_gb300_tune(sptrsv_handle_t handle, const void *d_val, int dtype, int rhs, int layout, const void *d_b,
