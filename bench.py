@@ -299,6 +299,14 @@ def reference_scheme_ms(cases, dev, reps: int = 3) -> dict:
     return out
 
 
+# Hardware hop latencies measured on GB300 by a stand-alone probe (figures in
+# profiles/machine_probe_gb300.md): one-way flag hop SM -> SM with a relaxed
+# store and a relaxed poll, 303 ns (627 cycles; 464 ns on another box), and a
+# warp -> warp hop through shared memory inside one CTA, 196 cycles.
+HW_HOP_GLOBAL_NS = (303.0, 464.0)
+HW_HOP_SMEM_CYCLES = 196.0
+
+
 def hop_latency(dev, n: int = 8192, reps: int = 9) -> dict:
     """Per-hop latency of this library's executor, measured on a chain (unknown j
     feeds j+1 only, n levels): one unknown per chunk puts every hop through global
@@ -483,6 +491,12 @@ def run_gpu(args, world, rank, local):
         details[c["name"]]["latency_floor_ms"] = round(floor_ms, 4)
         details[c["name"]]["floor_path"] = "shared memory (blocked order)" if blocked else "global memory (level order)"
         details[c["name"]]["exec_over_floor"] = round(ems / floor_ms, 2) if floor_ms > 0 else None
+        # the same floor from the hardware hop alone (no executor loop around it)
+        sm_mhz = clock_info.get("sm_mhz") or 2070.0
+        hw_ns = ((HW_HOP_SMEM_CYCLES / sm_mhz * 1e3,) * 2) if blocked else HW_HOP_GLOBAL_NS
+        hw_ms = [info[c["name"]]["nlevels"] * h * 1e-6 for h in hw_ns]
+        details[c["name"]]["hw_hop_floor_ms"] = [round(v, 4) for v in hw_ms]
+        details[c["name"]]["exec_over_hw_hop_floor"] = [round(ems / v, 2) for v in hw_ms[::-1]]
         if c["name"] in ref_scheme:
             details[c["name"]]["reference_scheme_ms"] = round(ref_scheme[c["name"]], 4)
             details[c["name"]]["speedup_vs_reference_scheme"] = round(ref_scheme[c["name"]] / ms, 2)
@@ -508,7 +522,13 @@ def run_gpu(args, world, rank, local):
                           "floor_ms_per_step": round(sum(d["latency_floor_ms"] for d in details.values()), 4),
                           "how": "chain of 8,192 unknowns: one unknown per chunk (every hop through global "
                                  "memory) and one chunk for the chain (every hop through shared memory); "
-                                 "floor = nlevels x t_hop of the path the case's schedule uses"},
+                                 "floor = nlevels x t_hop of the path the case's schedule uses",
+                          "hw_hop_global_ns": list(HW_HOP_GLOBAL_NS), "hw_hop_smem_cycles": HW_HOP_SMEM_CYCLES,
+                          "hw_floor_ms_per_step": [round(sum(d["hw_hop_floor_ms"][0] for d in details.values()), 4),
+                                                   round(sum(d["hw_hop_floor_ms"][1] for d in details.values()), 4)],
+                          "hw_how": "nlevels x the hardware hop alone (stand-alone probe: relaxed flag hop SM to SM "
+                                    "303-464 ns by box; shared-memory hop 196 cycles at the sampled SM clock); "
+                                    "per case exec_over_hw_hop_floor gives the range"},
         "cpu_baseline": cpu,
         "e2e": {"value": round(e2e_val, 3), "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": round(e2e_step, 4)},
@@ -533,6 +553,7 @@ def run_gpu(args, world, rank, local):
         torch.cuda.empty_cache()
         ex_args = argparse.Namespace(**vars(args))
         ex_args.steps = min(args.steps, 10)
+        ex_args.rhs_list = [1, 16, 64]
         m1 = matgen.system_1m(seed=2)
         t0 = time.perf_counter()
         line["system_10k"] = measure_system_10k(ex_args, dev)
@@ -623,13 +644,13 @@ def measure_multi_rhs(args, dev, m=None, world=1, rank=0, dist=None) -> dict:
     from oracle import oracle
     from sptrsv_gb300 import SyncFreeSolver, matgen, shard
     if m is None:
-        m = matgen.system_1m(seed=2)
+        m = matgen.system_1m(seed=2, n=int(round(1_000_000 * args.scale)))
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
     out = {}
     clocks = ClockSampler(dev.index)
     clocks.start()
     time.sleep(0.2)
-    for rhs in (1, 16, 64):
+    for rhs in args.rhs_list:
         rng = np.random.default_rng(rhs)
         B = rng.standard_normal((m.n, rhs))
         # the right-hand sides shard over ranks as contiguous column slices;
@@ -671,7 +692,8 @@ def measure_multi_rhs(args, dev, m=None, world=1, rank=0, dist=None) -> dict:
                             "mixed_problem_gbs": round(bp / tmix / 1e6, 2),
                             "fp64_solves_per_s": round(1e3 / t64, 1)}
     clk = clocks.stop()
-    return {"workload": "n=1M Poisson(9) band 20k, rhs 1/16/64, column-major B ~ N(0,1)", "n": m.n, "nnz": m.nnz,
+    return {"workload": f"n={m.n:,} Poisson(9) band 20k, rhs {'/'.join(map(str, args.rhs_list))}, "
+                        "column-major B ~ N(0,1)", "n": m.n, "nnz": m.nnz,
             "cases": out, "l2": "flushed before every solve", "clocks": clk,
             "parallelism": f"rhs columns sharded over {world} rank(s)" if world > 1 else "one GPU"}
 
@@ -891,6 +913,8 @@ def main(argv=None) -> int:
                     help="default workload only: skip the 10k, multi-rhs, batch and adjoint measurements "
                          "attached to its line")
     ap.add_argument("--batch-count", type=int, default=512)
+    ap.add_argument("--rhs-list", default="1,16,64",
+                    help="multi_rhs workload: right-hand-side counts (comma-separated; profiling runs)")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="size factor of the deep/wide systems (1.0 = the benchmark sizes; smaller for profiling)")
     ap.add_argument("--cases", default=None,
@@ -905,6 +929,7 @@ def main(argv=None) -> int:
             ap.error(f"unknown case(s) {bad}")
     if args.warmup < 3:
         args.warmup = 3
+    args.rhs_list = [int(v) for v in args.rhs_list.split(",") if v.strip()]
     kw = {}
     for k in ("schedule", "lanes", "chunk", "order_block"):
         v = getattr(args, k)

@@ -97,7 +97,8 @@ struct sptrsv_gb300_handle_s {
   int import_option = 1;   // importer warp on blocked layouts (SPTRSV_OPTION_IMPORT)
   ImportTable pipe;        // unit pipeline tables (ring slots, stages)
   int pipe_option = 0;     // SPTRSV_OPTION_UNIT_PIPELINE: 0 off, 1 on, else the ring cap
-  int fused_refine = 1;    // SPTRSV_OPTION_FUSED_REFINE: first refinement step fused into the FP32 pass
+  int fused_refine = 2;    // SPTRSV_OPTION_FUSED_REFINE: first refinement step fused into the FP32 pass
+                           // (2: residual in double-float on the FP32 pipe, 1: in FP64, 0: separate passes)
   // staged values
   Values<double> v64;
   Values<float> v32;
@@ -106,6 +107,8 @@ struct sptrsv_gb300_handle_s {
   DevBuf xw, left_sum, counters, r32, d32, stats;
   DevBuf tb, tx;  // row-major staging of column-major blocks of many right-hand sides
   DevBuf c0;      // unit pipeline: first term b/d of every position
+  DevBuf wsplit;  // fused refinement in double-float: (hi, lo) float pairs of the FP64 weights
+  bool wsplit_ok = false;
   DeviceCtl* ctl = nullptr;
   int* flags = nullptr;
   int* host_pinned = nullptr;  // 4 ints
@@ -247,6 +250,7 @@ void free_analysis(sptrsv_gb300_handle_s* h) {
   free_values(h->v64);
   free_values(h->v32);
   h->staged64 = h->staged32 = false;
+  h->wsplit_ok = false;
   h->analysed = false;
   h->layout_block = -1;
 }
@@ -338,6 +342,7 @@ int build_layout(sptrsv_gb300_handle_s* h, int block, cudaStream_t s) {
   free_values(h->v64);
   free_values(h->v32);
   h->staged64 = h->staged32 = false;
+  h->wsplit_ok = false;
   Layout& L = h->layout;
   const int n = h->n;
   const int ndep = h->nnz - n;
@@ -880,6 +885,7 @@ int stage_values(sptrsv_gb300_handle_s* h, const void* d_val, int dtype, cudaStr
     ST_TRY(stage<double, double>(h, h->v64, static_cast<const double*>(d_val), s, check));
     ST_TRY(stage<double, float>(h, h->v32, static_cast<const double*>(d_val), s, false));
     h->staged64 = h->staged32 = true;
+    h->wsplit_ok = false;
   } else if (dtype == SPTRSV_DTYPE_F32) {
     ST_TRY(stage<float, float>(h, h->v32, static_cast<const float*>(d_val), s, check));
     h->staged32 = true;
@@ -1135,6 +1141,7 @@ int sptrsv_gb300_destroy(sptrsv_handle_t h) {
   free_buf(h->tb);
   free_buf(h->tx);
   free_buf(h->c0);
+  free_buf(h->wsplit);
   if (h->ctl) cudaFree(h->ctl);
   if (h->flags) cudaFree(h->flags);
   if (h->host_pinned) cudaFreeHost(h->host_pinned);
@@ -1234,7 +1241,8 @@ static int set_option_value(sptrsv_handle_t h, int option, long long value) {
       h->pipe_option = static_cast<int>(value);
       return SPTRSV_OK;
     case SPTRSV_OPTION_FUSED_REFINE:
-      h->fused_refine = value != 0;
+      if (value < 0 || value > 2) return SPTRSV_ERR_INVALID;
+      h->fused_refine = static_cast<int>(value);
       return SPTRSV_OK;
     case SPTRSV_OPTION_OPT:
       if (value < SPTRSV_OPT_WARP_NNZ || value > SPTRSV_OPT_WARP_AUTO) return SPTRSV_ERR_INVALID;
@@ -1704,9 +1712,20 @@ int sptrsv_gb300_solve_refine(sptrsv_handle_t h, const double* d_val, int rhs, i
       }
       CUDA_TRY(cudaEventRecord(h->ev_exec[0], s));
     }
+    const float2* wsplit = nullptr;
+    if (h->fused_refine == 2) {
+      // the residual in double-float: (hi, lo) pairs of the FP64 weights, once per staging
+      const long long ndep = h->layout.ndep;
+      if (!h->wsplit_ok) {
+        ST_TRY(ensure_buf(h, h->wsplit, sizeof(float2) * (size_t)(ndep + 16), 0, s));
+        CUDA_TRY(launch_split_weights(h->v64.dep_w, ndep, static_cast<float2*>(h->wsplit.p), s));
+        h->wsplit_ok = true;
+      }
+      wsplit = static_cast<const float2*>(h->wsplit.p);
+    }
     CUDA_TRY(launch_refine_fused(h->layout, h->v32, h->v64, rhs, d_b, d_x, si, sk,
                                  static_cast<unsigned long long*>(h->xw.p), stats, h->ctl, fc, timeout_ns(h),
-                                 h->num_sms, s));
+                                 h->num_sms, s, wsplit));
     if (h->profile) {
       CUDA_TRY(cudaEventRecord(h->ev_exec[1], s));
       h->ev_recorded = true;

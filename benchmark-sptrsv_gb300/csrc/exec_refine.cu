@@ -30,6 +30,24 @@
 // stats (non-negative doubles as ordered bit patterns, max over the pass,
 // taken in FP32): [0] max |d|, [1] max |x|, [2] max |x0| -- the refinement's
 // stopping estimate.
+//
+// DF variant (the residual in double-float on the FP32 pipe). On this GPU an
+// FP64 FMA issues at 1/64 of the FP32 rate and has 64 cycles of latency, so
+// the residual's FP64 FMA per dependency sits both on the FP64 pipe and on
+// every hop's critical path. The DF variant keeps the FP64 weight as two
+// floats, w ~ hi + lo (hi = RN32(w), lo = RN32(w - hi), 48 significant bits),
+// and carries S = b/d - sum_j w_j x0_j as an unevaluated float pair (acc, rl):
+//   p  = RN(hi * x0_j),  pe = hi * x0_j - p (exact, by FMA),
+//   t  = RN(lo * x0_j + pe)                 (the product's low part),
+//   acc' = RN(acc - p),  e = (acc - p) - acc' (exact, TwoSum),
+//   rl' = RN(rl + (e - t)).
+// acc is the FP32 solve's own accumulator, so when the list is done x0 = acc
+// and the scaled residual rho = S - x0 is rl itself: d = rl - sum_j hi_j d_j.
+// The terms dropped are the product's low part rounding (2^-24 of a 2^-24
+// fraction of each term) and the roundings of rl, which stays at the size of
+// the residual: rho is exact to about 2^-44 relative to x, far below what the
+// FP32 correction resolves. FP64 work is left only once per unknown: b/d at
+// the start (product, split into the pair) and x = x0 + d at the end.
 #include "exec_common.cuh"
 #include "internal.h"
 
@@ -47,6 +65,7 @@ struct RefineArgs {
   const int* dep_pos_f;
   const float* w32;
   const double* w64;
+  const float2* wsplit;       // DF: (hi, lo) of every FP64 weight, ready order
   const float* rcp32;
   const double* rcp64;
   const double* b;
@@ -95,7 +114,20 @@ __device__ __forceinline__ void stats_max(unsigned long long* p, float v) {
     atomicMax(p, static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(v))));
 }
 
-template <int G, int RPL, int UD>
+// Exact FP32 error-free steps; the intrinsics keep the compiler from fusing
+// the product into the subtraction, which would break the exactness.
+__device__ __forceinline__ void df_sub_product(float& acc, float& rl, float hi, float lo, float x) {
+  const float p = __fmul_rn(hi, x);
+  const float pe = __fmaf_rn(hi, x, -p);
+  const float t = __fmaf_rn(lo, x, pe);
+  const float s = __fsub_rn(acc, p);
+  const float bb = __fsub_rn(s, acc);
+  const float e = __fadd_rn(__fsub_rn(acc, __fsub_rn(s, bb)), __fsub_rn(-p, bb));
+  acc = s;
+  rl = __fadd_rn(rl, __fsub_rn(e, t));
+}
+
+template <int G, int RPL, int UD, bool DF = false>
 __global__ void __launch_bounds__(256) k_pull_refine1(RefineArgs a) {
   using Bits = unsigned long long;
   constexpr int P = 32 / G;
@@ -123,12 +155,14 @@ __global__ void __launch_bounds__(256) k_pull_refine1(RefineArgs a) {
       const int p = base + j;
       int row = 0, e = 0, e1 = 0;
       float acc0[RPL], accd[RPL];
-      double res[RPL];
+      double res[RPL];   // FP64 residual accumulator (not DF)
+      float rlo[RPL];    // DF: low part of S = b/d - sum w x0
 #pragma unroll
       for (int r = 0; r < RPL; ++r) {
         acc0[r] = 0.f;
         accd[r] = 0.f;
         res[r] = 0.0;
+        rlo[r] = 0.f;
       }
       if (!done) {
         row = a.perm[p];
@@ -141,13 +175,21 @@ __global__ void __launch_bounds__(256) k_pull_refine1(RefineArgs a) {
           const int k = gl + r * G;
           if (k < rhs) {
             const double bv = a.b[(long long)row * a.b_si + (long long)k * a.b_sk];
-            acc0[r] = static_cast<float>(bv) * s32;
-            res[r] = bv * s64;
+            if (DF) {
+              // b/d as a float pair: hi = RN32(b*s), lo = RN32(b*s - hi)
+              const double bs = bv * s64;
+              const float hi = __double2float_rn(bs);
+              acc0[r] = hi;
+              rlo[r] = __double2float_rn(__fma_rn(bv, s64, -widen(hi)));
+            } else {
+              acc0[r] = static_cast<float>(bv) * s32;
+              res[r] = bv * s64;
+            }
           }
         }
       }
       int q[UD], sl[UD];
-      float w32[UD];
+      float w32[UD], wlo[UD];
       double w64[UD];
       Bits bits[UD][RPL];
       unsigned todo = 0u;
@@ -157,8 +199,14 @@ __global__ void __launch_bounds__(256) k_pull_refine1(RefineArgs a) {
         for (int u = 0; u < UD; ++u) {
           const bool in = e + u < e1;
           q[u] = in ? a.dep_pos_f[e + u] : -1;
-          w32[u] = in ? a.w32[e + u] : 0.f;
-          w64[u] = in ? a.w64[e + u] : 0.0;
+          if (DF) {
+            const float2 ws = in ? a.wsplit[e + u] : make_float2(0.f, 0.f);
+            w32[u] = ws.x;
+            wlo[u] = ws.y;
+          } else {
+            w32[u] = in ? a.w32[e + u] : 0.f;
+            w64[u] = in ? a.w64[e + u] : 0.0;
+          }
           sl[u] = (q[u] >= 0 && a.smem_tier && q[u] >= base) ? q[u] - base : -1;
 #pragma unroll
           for (int r = 0; r < RPL; ++r) {
@@ -186,8 +234,12 @@ __global__ void __launch_bounds__(256) k_pull_refine1(RefineArgs a) {
               if (!(todo & bit)) continue;
               if (bits[u][r] != kPairEmpty) {
                 const float xj = pair_x0(bits[u][r]);
-                acc0[r] = fmaf(-w32[u], xj, acc0[r]);
-                res[r] = fma(-w64[u], widen(xj), res[r]);
+                if (DF) {
+                  df_sub_product(acc0[r], rlo[r], w32[u], wlo[u], xj);
+                } else {
+                  acc0[r] = fmaf(-w32[u], xj, acc0[r]);
+                  res[r] = fma(-w64[u], widen(xj), res[r]);
+                }
                 accd[r] = fmaf(-w32[u], pair_d(bits[u][r]), accd[r]);
                 todo &= ~bit;
                 progress = true;
@@ -210,7 +262,8 @@ __global__ void __launch_bounds__(256) k_pull_refine1(RefineArgs a) {
                 if (k < rhs) {
                   const float x0 = acc0[r];
                   const double x0w = widen(x0);
-                  const float d = static_cast<float>(res[r] - x0w) + accd[r];
+                  // DF: rho = S - x0 = the pair's low part
+                  const float d = DF ? __fadd_rn(rlo[r], accd[r]) : static_cast<float>(res[r] - x0w) + accd[r];
                   const Bits v = pack_pair(x0, d);
                   if (a.smem_tier) st_shared_u64(&s_x[(long long)j * rhs + k], v);
                   st_relaxed_u64(&a.xw[(long long)p * rhs + k], v);
@@ -264,9 +317,9 @@ __global__ void __launch_bounds__(256) k_pull_refine1(RefineArgs a) {
   leave(a.ctl);
 }
 
-template <int G, int RPL, int UD>
+template <int G, int RPL, int UD, bool DF>
 cudaError_t run_refine1(const RefineArgs& a, int block, size_t smem, int num_sms, cudaStream_t s) {
-  auto kernel = k_pull_refine1<G, RPL, UD>;
+  auto kernel = k_pull_refine1<G, RPL, UD, DF>;
   if (smem > 48 * 1024) {
     const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -287,7 +340,7 @@ cudaError_t run_refine1(const RefineArgs& a, int block, size_t smem, int num_sms
 cudaError_t launch_refine_fused(const Layout& L, const Values<float>& v32, const Values<double>& v64, int rhs,
                                 const double* b, double* x, long long si, long long sk, unsigned long long* xw,
                                 unsigned long long* stats, DeviceCtl* ctl, const ExecConfig& cfg,
-                                unsigned long long timeout_ns, int num_sms, cudaStream_t s) {
+                                unsigned long long timeout_ns, int num_sms, cudaStream_t s, const float2* wsplit) {
   if (L.n == 0) return cudaSuccess;
   if (rhs < 1 || rhs > 64) return cudaErrorInvalidValue;
   RefineArgs a{};
@@ -321,13 +374,41 @@ cudaError_t launch_refine_fused(const Layout& L, const Values<float>& v32, const
   }
   const int block = cfg.block;
   const int ud = cfg.wsync_batch == 1 ? 1 : 2;
-  if (rhs == 1) return ud == 1 ? run_refine1<1, 1, 1>(a, block, smem, num_sms, s)
-                               : run_refine1<1, 1, 2>(a, block, smem, num_sms, s);
-  if (rhs <= 4) return run_refine1<4, 1, 2>(a, block, smem, num_sms, s);
-  if (rhs <= 8) return run_refine1<8, 1, 2>(a, block, smem, num_sms, s);
-  if (rhs <= 16) return run_refine1<16, 1, 2>(a, block, smem, num_sms, s);
-  if (rhs <= 32) return run_refine1<32, 1, 2>(a, block, smem, num_sms, s);
-  return run_refine1<32, 2, 2>(a, block, smem, num_sms, s);
+  a.wsplit = wsplit;
+  if (wsplit) {
+    if (rhs == 1) return ud == 1 ? run_refine1<1, 1, 1, true>(a, block, smem, num_sms, s)
+                                 : run_refine1<1, 1, 2, true>(a, block, smem, num_sms, s);
+    if (rhs <= 4) return run_refine1<4, 1, 2, true>(a, block, smem, num_sms, s);
+    if (rhs <= 8) return run_refine1<8, 1, 2, true>(a, block, smem, num_sms, s);
+    if (rhs <= 16) return run_refine1<16, 1, 2, true>(a, block, smem, num_sms, s);
+    if (rhs <= 32) return run_refine1<32, 1, 2, true>(a, block, smem, num_sms, s);
+    return run_refine1<32, 2, 2, true>(a, block, smem, num_sms, s);
+  }
+  if (rhs == 1) return ud == 1 ? run_refine1<1, 1, 1, false>(a, block, smem, num_sms, s)
+                               : run_refine1<1, 1, 2, false>(a, block, smem, num_sms, s);
+  if (rhs <= 4) return run_refine1<4, 1, 2, false>(a, block, smem, num_sms, s);
+  if (rhs <= 8) return run_refine1<8, 1, 2, false>(a, block, smem, num_sms, s);
+  if (rhs <= 16) return run_refine1<16, 1, 2, false>(a, block, smem, num_sms, s);
+  if (rhs <= 32) return run_refine1<32, 1, 2, false>(a, block, smem, num_sms, s);
+  return run_refine1<32, 2, 2, false>(a, block, smem, num_sms, s);
+}
+
+// (hi, lo) float pairs of the FP64 weights for the DF fused pass:
+// hi = RN32(w), lo = RN32(w - hi).
+__global__ void k_split_weights(const double* __restrict__ w, long long count, float2* out) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += stride) {
+    const double v = w[i];
+    const float hi = __double2float_rn(v);
+    out[i] = make_float2(hi, __double2float_rn(v - static_cast<double>(hi)));
+  }
+}
+cudaError_t launch_split_weights(const double* w, long long count, float2* out, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  long long grid = (count + 255) / 256;
+  if (grid > (1 << 20)) grid = 1 << 20;
+  k_split_weights<<<static_cast<int>(grid), 256, 0, s>>>(w, count, out);
+  return cudaGetLastError();
 }
 
 }  // namespace sptrsv

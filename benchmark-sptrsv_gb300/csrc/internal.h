@@ -293,10 +293,14 @@ cudaError_t launch_transpose(const T* in, T* out, int rows, int cols, cudaStream
 // solution x0, the FP64 residual and the FP32 correction d together; writes
 // x = x0 + d (FP64, strides si/sk) and stats[0..2] = max |d|, max |x|, max |x0|
 // (ordered bits; zero them first). xw: n*rhs 64-bit words set to all ones.
+// wsplit (optional): (hi, lo) float pairs of v64.dep_w; given, the residual runs
+// in double-float on the FP32 pipe instead of FP64 (launch_split_weights fills it)
 cudaError_t launch_refine_fused(const Layout& L, const Values<float>& v32, const Values<double>& v64, int rhs,
                                 const double* b, double* x, long long si, long long sk, unsigned long long* xw,
                                 unsigned long long* stats, DeviceCtl* ctl, const ExecConfig& cfg,
-                                unsigned long long timeout_ns, int num_sms, cudaStream_t s);
+                                unsigned long long timeout_ns, int num_sms, cudaStream_t s,
+                                const float2* wsplit = nullptr);
+cudaError_t launch_split_weights(const double* w, long long count, float2* out, cudaStream_t s);
 cudaError_t launch_cast_d2f(const double* in, float* out, long long count, cudaStream_t s);
 cudaError_t launch_residual(const Layout& L, const Values<double>& V, int rhs, const double* b, const double* x,
                             long long si, long long sk, float* r, cudaStream_t s);

@@ -106,7 +106,7 @@ class SyncFreeSolver:
                  staged: bool | None = None, stage_entries: int | None = None, stages: int | None = None,
                  warp_sync: bool | None = None, split: int | None = None, wsync_batch: int | None = None,
                  import_deps: bool | None = None, unit_pipeline: int | None = None, fused_grad: bool | None = None,
-                 fused_refine: bool | None = None, opt: int | None = None, rhs_tile: int | None = None,
+                 fused_refine: int | None = None, opt: int | None = None, rhs_tile: int | None = None,
                  stretch: bool | None = None, stream=None):
         torch = _torch()
         self._lib = load()

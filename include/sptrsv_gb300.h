@@ -116,11 +116,14 @@ typedef enum sptrsv_option {
                                      SPTRSV_OPTION_STAGES buffers, default 3) and an importer warp, with
                                      a ring of up to 8192 value slots per unit; a power of two from 128
                                      to 8192 = that ring size cap; 0 (default) = off */
-  SPTRSV_OPTION_FUSED_REFINE = 21, /* sptrsv_gb300_solve_refine: 1 (default) = the FP32 solve, the FP64
-                                     residual and the FP32 correction of the first refinement step run
-                                     as one pass over the dependency DAG (pull schedules, rhs <= 64,
-                                     and for one rhs only where no dependency list is split over
-                                     lanes); 0 = separate passes */
+  SPTRSV_OPTION_FUSED_REFINE = 21, /* sptrsv_gb300_solve_refine: the FP32 solve, the residual and the FP32
+                                     correction of the first refinement step run as one pass over the
+                                     dependency DAG (pull schedules, rhs <= 64, and for one rhs only
+                                     where no dependency list is split over lanes). 2 (default) = the
+                                     residual of that pass in double-float on the FP32 pipe (each FP64
+                                     weight as two floats, exact products and sums, ~2^-44 relative to
+                                     x; FP64 only once per unknown); 1 = the residual in FP64
+                                     arithmetic; 0 = separate passes (FP64 residual) */
   SPTRSV_OPTION_OPT = 22,         /* the reference's opt argument (sptrsv_syncfree_cuda.h:234-286) for
                                      solves with several right-hand sides on the push schedule (the
                                      reference's scheme): SPTRSV_OPT_WARP_NNZ = the lanes of a column's
@@ -279,8 +282,10 @@ int sptrsv_gb300_solve(sptrsv_handle_t handle, const void *d_val, int dtype, int
  * NULL for the staged FP64 values). With SPTRSV_OPTION_FUSED_REFINE (default)
  * the first solve and the first correction share one sync-free pass: each
  * unknown publishes its FP32 value and its FP32 correction together, so the
- * step costs one walk of the dependency chain instead of two; further steps
- * run as separate residual, solve and update passes. Stops when the estimated relative forward
+ * step costs one walk of the dependency chain instead of two, and by default
+ * that pass forms the residual in double-float on the FP32 pipe (this GPU's
+ * FP64 FMA issues at 1/64 of the FP32 rate with 64 cycles of latency);
+ * further steps run as separate residual (FP64), solve and update passes. Stops when the estimated relative forward
  * error ||D_k||^2 / (||D_{k-1}|| ||X||) (max norms; D_0 = X_0) is at most
  * `tol`, after at least one refinement step and at most `max_iter`; tol <= 0
  * runs exactly max_iter steps without reading anything back (asynchronous,

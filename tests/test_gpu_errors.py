@@ -145,7 +145,8 @@ def test_wait_budget_expires_cleanly_then_recovers(cuda, cfg):
     assert float((x - 1).abs().max()) < 1e-12
 
 
-def test_fused_refine_wait_budget_expires_cleanly_then_recovers(cuda):
+@pytest.mark.parametrize("fused", [1, 2])
+def test_fused_refine_wait_budget_expires_cleanly_then_recovers(cuda, fused):
     """The fused refinement pass bounds its waits too: on a 200,000-long chain the
     CTAs that hold late chunks wait for every earlier chunk, far longer than a 1 ms
     budget, so the call reports SPTRSV_ERR_TIMEOUT; the handle then refines
@@ -154,7 +155,7 @@ def test_fused_refine_wait_budget_expires_cleanly_then_recovers(cuda):
     m = matgen.chain(200_000)
     b = cuda.from_numpy(m.matvec(np.ones(m.n))).cuda()
     s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, values=m.val, schedule=2, order_block=1,
-                       chunk=64, timeout_ms=1, fused_refine=True)
+                       chunk=64, timeout_ms=1, fused_refine=fused)
     with pytest.raises(SptrsvError) as ei:
         s.solve_refine(b)
     assert ei.value.status == _lib.ERR_TIMEOUT

@@ -1,5 +1,7 @@
 """FP32 storage/solve + FP64-residual iterative refinement: forward error against
-the FP64 oracle must be at most 1e-10 (relative, max norm)."""
+the FP64 oracle must be at most 1e-10 (relative, max norm). The fused first step
+runs with the residual in FP64 (fused_refine=1) or in double-float on the FP32
+pipe (fused_refine=2); both are held to the same tolerance."""
 from __future__ import annotations
 
 import numpy as np
@@ -19,7 +21,7 @@ def relerr(x, ref):
 
 
 @pytest.mark.parametrize("name", golden_names())
-@pytest.mark.parametrize("schedule,fused", [(0, True), (0, False), (1, True), (2, True), (2, False), (3, True)])
+@pytest.mark.parametrize("schedule,fused", [(0, 1), (0, 2), (0, 0), (1, 1), (2, 1), (2, 2), (2, 0), (3, 1)])
 def test_refined_forward_error(cuda, name, schedule, fused):
     from sptrsv_gb300 import SyncFreeSolver
     g = load_golden(name)
@@ -85,7 +87,7 @@ def test_fused_first_step_against_oracle(cuda, oracle_port, case, rhs):
     B = np.random.default_rng(rhs).standard_normal((m.n, rhs))
     ref = oracle_port.solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, B)
     results = {}
-    for fused in (True, False):
+    for fused in (1, 2, 0):
         s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, values=m.val, fused_refine=fused)
         for layout in ("row", "col"):
             b = cuda.from_numpy(B).cuda()
@@ -100,9 +102,11 @@ def test_fused_first_step_against_oracle(cuda, oracle_port, case, rhs):
             assert relerr(x2.cpu().numpy(), ref) <= TOL_FWD
             results[(fused, layout)] = (x.cpu().numpy(), iters)
         s.close()
-    assert results[(True, "row")][1] == 1
-    # the fused step and the separate passes agree to well below the tolerance
-    assert relerr(results[(True, "row")][0], results[(False, "row")][0]) <= TOL_FWD
+    assert results[(1, "row")][1] == 1 and results[(2, "row")][1] == 1
+    # the fused steps (FP64 or double-float residual) and the separate passes agree
+    # to well below the tolerance
+    assert relerr(results[(1, "row")][0], results[(0, "row")][0]) <= TOL_FWD
+    assert relerr(results[(2, "row")][0], results[(0, "row")][0]) <= TOL_FWD
 
 
 def test_fused_refine_more_steps_and_option(cuda, oracle_port):
@@ -113,16 +117,24 @@ def test_fused_refine_more_steps_and_option(cuda, oracle_port):
     B = np.random.default_rng(3).standard_normal((m.n, 2))
     ref = oracle_port.solve(m.col_ptr, m.row_idx, m.val, m.n, 0, B)
     s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, 0, values=m.val)
-    assert s.get_option(_lib.OPTION_FUSED_REFINE) == 1
+    assert s.get_option(_lib.OPTION_FUSED_REFINE) == 2
     b = cuda.from_numpy(B).cuda()
     for steps in (1, 2, 3):
         x, it, _ = s.solve_refine(b, tol=0.0, max_iter=steps)
         assert it == steps
         assert relerr(x.cpu().numpy(), ref) <= TOL_FWD
-    s.set_option(_lib.OPTION_FUSED_REFINE, 0)
-    assert s.get_option(_lib.OPTION_FUSED_REFINE) == 0
-    x, it, _ = s.solve_refine(b)
-    assert relerr(x.cpu().numpy(), ref) <= TOL_FWD
+    for mode in (0, 1):
+        s.set_option(_lib.OPTION_FUSED_REFINE, mode)
+        assert s.get_option(_lib.OPTION_FUSED_REFINE) == mode
+        for steps in (1, 2):
+            x, it, _ = s.solve_refine(b, tol=0.0, max_iter=steps)
+            assert relerr(x.cpu().numpy(), ref) <= TOL_FWD
+        x, it, _ = s.solve_refine(b)
+        assert relerr(x.cpu().numpy(), ref) <= TOL_FWD
+    # re-staged values reach the double-float weights too
+    s.set_values(cuda.from_numpy(2.0 * m.val).cuda())
+    x, it, _ = s.solve_refine(b, tol=0.0, max_iter=1)
+    assert relerr(x.cpu().numpy(), ref / 2.0) <= TOL_FWD
 
 
 @pytest.mark.parametrize("case", ["one", "diagonal", "chain", "dense64", "star"])
@@ -137,7 +149,8 @@ def test_fused_refine_edge_structures(cuda, oracle_port, case):
     for rhs in (1, 5):
         B = np.random.default_rng(rhs).standard_normal((m.n, rhs))
         ref = oracle_port.solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, B)
-        s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, values=m.val, fused_refine=True)
-        x, iters, est = s.solve_refine(cuda.from_numpy(B).cuda())
-        assert relerr(x.cpu().numpy(), ref) <= TOL_FWD, (case, rhs)
-        s.close()
+        for fused in (1, 2):
+            s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, values=m.val, fused_refine=fused)
+            x, iters, est = s.solve_refine(cuda.from_numpy(B).cuda())
+            assert relerr(x.cpu().numpy(), ref) <= TOL_FWD, (case, rhs, fused)
+            s.close()
