@@ -1695,11 +1695,14 @@ int sptrsv_gb300_solve_refine(sptrsv_handle_t h, const double* d_val, int rhs, i
     // X_0, the FP64 residual and the first FP32 correction in one pass: X = X_0 + D_1
     if (rhs == 1 && fc.wsync_batch == 0) fc.wsync_batch = (long long)(h->nnz - h->n) > 3LL * (long long)h->n ? 1 : 2;
     // level order: one CTA of 256 threads per SM up to 4 right-hand sides (two
-    // for batches), three beyond (measured on the 1M-row band and power-law
-    // systems and the 512-system batch; the pass reads more per dependency than
-    // a plain solve, and fewer polling warps paid)
+    // for batches); beyond, three with the FP64 residual and every CTA that fits
+    // (four) with the double-float one, which holds fewer registers (measured
+    // on the 1M-row band and power-law systems and the 512-system batch: the
+    // pass reads more per dependency than a plain solve, and fewer polling
+    // warps paid up to 4 right-hand sides; at 16 / 64 the double-float pass
+    // took 1.34 / 2.78 ms with three and 1.23 / 2.43 ms with four)
     if (h->sched_option == SCHED_AUTO && planned(h, SPTRSV_OPTION_CTAS_PER_SM) && h->layout_block >= h->n)
-      fc.ctas_per_sm = rhs <= 4 ? (h->batch_count > 1 ? 2 : 1) : 3;
+      fc.ctas_per_sm = rhs <= 4 ? (h->batch_count > 1 ? 2 : 1) : (h->fused_refine == 2 ? 0 : 3);
     ST_TRY(ensure_buf(h, h->xw, sizeof(unsigned long long) * count, 0, s));
     CUDA_TRY(cudaMemsetAsync(h->xw.p, 0xFF, sizeof(unsigned long long) * count, s));
     CUDA_TRY(cudaMemsetAsync(stats, 0, 3 * sizeof(unsigned long long), s));
