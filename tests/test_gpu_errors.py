@@ -164,3 +164,48 @@ def test_fused_refine_wait_budget_expires_cleanly_then_recovers(cuda, fused):
     s.set_values(m.val)
     x, it, est = s.solve_refine(b)
     assert float((x - 1).abs().max()) < 1e-10
+
+
+def test_new_options_validate_and_round_trip(cuda):
+    """SPTRSV_OPTION_OPT (1..3), SPTRSV_OPTION_RHS_TILE (0, 1, 2, 4),
+    SPTRSV_OPTION_FUSED_REFINE (0..2) and SPTRSV_OPTION_STRETCH (boolean): valid
+    values round-trip, others return SPTRSV_ERR_INVALID and leave the option as it was."""
+    from sptrsv_gb300 import SptrsvError, SyncFreeSolver, _lib, matgen
+    m = matgen.poisson_band(500, 4.0, 50, seed=1)
+    s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, values=m.val)
+    cases = {_lib.OPTION_OPT: ([1, 2, 3], [0, 4, -1]), _lib.OPTION_RHS_TILE: ([0, 1, 2, 4], [3, 8, -1]),
+             _lib.OPTION_FUSED_REFINE: ([0, 1, 2], [3, -1])}
+    for opt, (good, bad) in cases.items():
+        for v in good:
+            s.set_option(opt, v)
+            assert s.get_option(opt) == v
+        for v in bad:
+            with pytest.raises(SptrsvError) as ei:
+                s.set_option(opt, v)
+            assert ei.value.status == _lib.ERR_INVALID
+            assert s.get_option(opt) == good[-1]
+    for v in (0, 1):
+        s.set_option(_lib.OPTION_STRETCH, v)
+        assert s.get_option(_lib.OPTION_STRETCH) == v
+    s.close()
+
+
+def test_stretch_option_on_a_batch_changes_only_the_order(cuda, oracle_port):
+    """A batch solved with and without the stretched level order (switching between
+    them on one handle re-lays the schedule out) gives the same answers."""
+    from sptrsv_gb300 import SyncFreeSolver, _lib, matgen
+    systems = matgen.batch_uneven(count=24, seed=8, nmin=200, nmax=20_000)
+    vals = np.concatenate([m.val for m in systems])
+    bs = [np.random.default_rng(k).standard_normal((m.n, 2)) for k, m in enumerate(systems)]
+    refs = [oracle_port.solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, bs[k])
+            for k, m in enumerate(systems)]
+    s = SyncFreeSolver(batch=[(m.col_ptr, m.row_idx, m.n, m.substitution) for m in systems], values=vals)
+    b = cuda.from_numpy(np.concatenate(bs)).cuda()
+    for stretch in (1, 0, 1):
+        s.set_option(_lib.OPTION_STRETCH, stretch)
+        s.set_values(vals)
+        x = s.solve(b).cpu().numpy()
+        for k in range(len(systems)):
+            sl = slice(s.offsets[k], s.offsets[k + 1])
+            assert np.max(np.abs(x[sl] - refs[k])) / np.max(np.abs(refs[k])) <= 1e-12, (stretch, k)
+    s.close()
