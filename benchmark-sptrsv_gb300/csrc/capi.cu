@@ -798,9 +798,19 @@ int effective_block(const sptrsv_gb300_handle_s* h) {
 // blocks of 32 level widths): level order inside such blocks, one CTA per
 // block with in-block hops through shared memory.
 //
-// Lists are split over lanes only where long lists carry a real share of the
-// work (> 5 % of the entries in lists longer than 32): the split executor
-// costs ~25 % more than the one-lane one on systems without them.
+// Lists are split over lanes only where a few lists are far longer than the
+// rest: > 5 % of the entries in lists longer than max(32, 4 x the mean list
+// length). Splitting pays for heavy-tailed lists (power-law backward walks:
+// 2.19 vs 32.5 ms at 4M rows, 63 vs 301 ms at 1M) and costs where most lists
+// are long and alike, since a warp then holds fewer unknowns and pays suffix
+// sums (band systems with 30-100 entries per row, power-law forward walks:
+// 1.5-1.9x slower split, e.g. 243 vs 128 ms on a 2M-row band of width 500).
+//
+// Residency in level order follows the average level width: one CTA of 256
+// threads per SM below 1,536 unknowns per level (fewer lanes polling ahead of
+// the wave: 1M-row band 1.109 vs 1.139 ms, 500k-row band 2.21 vs 2.68 ms),
+// two up to 8,192 (4M-row power-law 1.68 vs 1.76 ms forward, 2.19 vs 2.60
+// backward), three beyond (a 4M-row band with 17,468 per level 0.51 vs 0.60).
 double long_share(const std::vector<int>& ptr, int cut) {
   long long all = 0, lng = 0;
   for (size_t i = 0; i + 1 < ptr.size(); ++i) {
@@ -820,8 +830,13 @@ int make_plan(sptrsv_gb300_handle_s* h, const std::vector<int>& row_ptr, cudaStr
     std::vector<int> col_ptr((size_t)n + 1);
     CUDA_TRY(cudaMemcpyAsync(col_ptr.data(), h->csc_ptr, sizeof(int) * ((size_t)n + 1), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
-    P.split_fwd = long_share(row_ptr, 32) > 0.05 ? 32 : 0;
-    P.split_adj = long_share(col_ptr, 32) > 0.05 ? 8 : 0;  // the reverse walk measured best with short pieces
+    const int cut = std::max<int>(32, static_cast<int>(4.0 * (double)(nnz - n) / (double)n));
+    P.split_fwd = long_share(row_ptr, cut) > 0.05 ? 32 : 0;
+    P.split_adj = long_share(col_ptr, cut) > 0.05 ? 8 : 0;  // the reverse walk measured best with short pieces
+    if (h->batch_count == 1 && nl > 0) {
+      const long long width = ((long long)n + nl - 1) / nl;
+      P.ctas = width < 1536 ? 1 : (width < 8192 ? 2 : 3);
+    }
   }
   if (n > 0 && nl >= 256 && h->batch_count == 1 && nnz > n) {
     const long long width = ((long long)n + nl - 1) / nl;

@@ -67,6 +67,18 @@ def test_long_lists_get_split(cuda, oracle_port):
     assert relerr(s.solve(cuda.from_numpy(b).cuda()).cpu().numpy(), ref) <= TOL64
 
 
+def test_uniformly_long_lists_stay_on_one_lane(cuda, oracle_port):
+    """Lists that are long but alike (a band with ~40 entries per row) are not split:
+    splitting pays only when a few lists are far longer than the rest."""
+    from sptrsv_gb300 import matgen
+    m = matgen.poisson_band(40_000, 40.0, 800, seed=6)
+    s = _solver(m)
+    assert s.info()["split"] == 0
+    b = np.random.default_rng(3).standard_normal(m.n)
+    ref = oracle_port.solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, b)
+    assert relerr(s.solve(cuda.from_numpy(b).cuda()).cpu().numpy(), ref) <= TOL64
+
+
 def test_explicit_options_override_the_plan(cuda, oracle_port):
     from sptrsv_gb300 import _lib, matgen
     m = matgen.laplace2d_lower(200)
