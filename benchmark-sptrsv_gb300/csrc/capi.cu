@@ -1741,9 +1741,23 @@ int sptrsv_gb300_solve_refine(sptrsv_handle_t h, const double* d_val, int rhs, i
       }
       wsplit = static_cast<const float2*>(h->wsplit.p);
     }
-    CUDA_TRY(launch_refine_fused(h->layout, h->v32, h->v64, rhs, d_b, d_x, si, sk,
-                                 static_cast<unsigned long long*>(h->xw.p), stats, h->ctl, fc, timeout_ns(h),
-                                 h->num_sms, s, wsplit));
+    // one right-hand side on a blocked layout: the importer-warp variant (as the
+    // plain solve's k_pull_wsync_imp) keeps the cross-block polls out of the
+    // consumer warps' lockstep iterations
+    const bool imported = wsplit && rhs == 1 && fc.wsync && h->import_option && h->layout_block < h->n &&
+                          fc.chunk == h->layout_block && fc.smem_tier &&
+                          (h->imports.chunk == fc.chunk || build_imports(h, fc.chunk, 8, s) == SPTRSV_OK) &&
+                          h->imports.ptr != nullptr &&
+                          imported_smem_bytes(h->imports.width, h->imports.max_imports, 8) <= 220 * 1024;
+    if (imported) {
+      CUDA_TRY(launch_refine_fused_imported(h->layout, h->v64, wsplit, d_b, d_x,
+                                            static_cast<unsigned long long*>(h->xw.p), stats, h->ctl, fc,
+                                            timeout_ns(h), h->num_sms, s, h->imports));
+    } else {
+      CUDA_TRY(launch_refine_fused(h->layout, h->v32, h->v64, rhs, d_b, d_x, si, sk,
+                                   static_cast<unsigned long long*>(h->xw.p), stats, h->ctl, fc, timeout_ns(h),
+                                   h->num_sms, s, wsplit));
+    }
     if (h->profile) {
       CUDA_TRY(cudaEventRecord(h->ev_exec[1], s));
       h->ev_recorded = true;

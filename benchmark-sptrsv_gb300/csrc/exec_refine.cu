@@ -66,6 +66,13 @@ struct RefineArgs {
   const float* w32;
   const double* w64;
   const float2* wsplit;       // DF: (hi, lo) of every FP64 weight, ready order
+  // imported dependencies of a blocked layout (k_pull_refine1_imp): unit c covers
+  // positions [im_start[c], im_start[c+1]) and imports im_q[im_ptr[c] ..
+  // im_ptr[c+1]); dep_slot[e] is the shared-memory slot of dependency e
+  const int* im_start;
+  const int* im_ptr;
+  const int* im_q;
+  const int* dep_slot;
   const float* rcp32;
   const double* rcp64;
   const double* b;
@@ -261,16 +268,12 @@ __global__ void __launch_bounds__(256) k_pull_refine1(RefineArgs a) {
                 const int k = gl + r * G;
                 if (k < rhs) {
                   const float x0 = acc0[r];
-                  const double x0w = widen(x0);
                   // DF: rho = S - x0 = the pair's low part
-                  const float d = DF ? __fadd_rn(rlo[r], accd[r]) : static_cast<float>(res[r] - x0w) + accd[r];
+                  const float d = DF ? __fadd_rn(rlo[r], accd[r]) : static_cast<float>(res[r] - widen(x0)) + accd[r];
                   const Bits v = pack_pair(x0, d);
                   if (a.smem_tier) st_shared_u64(&s_x[(long long)j * rhs + k], v);
                   st_relaxed_u64(&a.xw[(long long)p * rhs + k], v);
-                  a.x[(long long)row * a.x_si + (long long)k * a.x_sk] = x0w + widen(d);
-                  mx_d = fmaxf(mx_d, fabsf(d));
-                  mx_x = fmaxf(mx_x, fabsf(x0 + d));
-                  mx_x0 = fmaxf(mx_x0, fabsf(x0));
+                  accd[r] = d;  // d from here on; x and the maxima follow the lockstep loop
                 }
               }
               done = true;
@@ -306,6 +309,190 @@ __global__ void __launch_bounds__(256) k_pull_refine1(RefineArgs a) {
             fail = true;
             break;
           }
+        }
+      }
+      // x = x0 + d and the stopping-estimate maxima, once the segment is done:
+      // off the lockstep iterations, on which the in-warp hops wait
+      if (!fail && j < len) {
+#pragma unroll
+        for (int r = 0; r < RPL; ++r) {
+          const int k = gl + r * G;
+          if (k < rhs) {
+            a.x[(long long)row * a.x_si + (long long)k * a.x_sk] = widen(acc0[r]) + widen(accd[r]);
+            mx_d = fmaxf(mx_d, fabsf(accd[r]));
+            mx_x = fmaxf(mx_x, fabsf(acc0[r] + accd[r]));
+            mx_x0 = fmaxf(mx_x0, fabsf(acc0[r]));
+          }
+        }
+      }
+    }
+    if (__syncthreads_or(fail)) break;
+  }
+  stats_max(&a.stats[0], mx_d);
+  stats_max(&a.stats[1], mx_x);
+  stats_max(&a.stats[2], mx_x0);
+  leave(a.ctl);
+}
+
+// ------------------------------------------------------------------ fused step, blocked layouts
+// The fused first refinement step (double-float residual, one right-hand side)
+// on a blocked layout, with the importer warp of k_pull_wsync_imp: one CTA per
+// order block, an extra warp that polls the block's external (x0, d) pairs from
+// global memory and copies each into a shared-memory slot as it lands, and
+// consumer warps that resolve every dependency in shared memory (slot from
+// dep_slot), one lane per unknown in lockstep. Without the importer the
+// consumer warps' lockstep iterations would wait on L2 polls of the few
+// cross-block dependencies.
+template <int U>
+__global__ void __launch_bounds__(288) k_pull_refine1_imp(RefineArgs a) {
+  using Bits = unsigned long long;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Bits* s_x = reinterpret_cast<Bits*>(smem_raw);
+  __shared__ unsigned s_chunk;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int ncw = (blockDim.x >> 5) - 1;  // consumer warps; warp ncw imports
+  float mx_d = 0.f, mx_x = 0.f, mx_x0 = 0.f;
+  for (;;) {
+    const unsigned c = next_chunk(a.ctl, a.nchunks, &s_chunk);
+    if (c >= (unsigned)a.nchunks) break;
+    const int base = a.im_start[c];
+    const int len = a.im_start[c + 1] - base;  // <= a.chunk (the window)
+    const int i0 = a.im_ptr[c], nimp = a.im_ptr[c + 1] - i0;
+    for (int i = threadIdx.x; i < len; i += blockDim.x) s_x[i] = kPairEmpty;
+    for (int i = threadIdx.x; i < nimp; i += blockDim.x) s_x[a.chunk + i] = kPairEmpty;
+    __syncthreads();
+    bool fail = false;
+    if (warp == ncw) {
+      // importer: each lane walks its imports in order, one poll at a time
+      WaitBudget wb(a.timeout_ns);
+      unsigned idle = 0u;
+      int i = lane;
+      Bits v = kPairEmpty;
+      if (i < nimp) v = ld_relaxed_u64(&a.xw[a.im_q[i0 + i]]);
+      for (;;) {
+        bool progress = false;
+        if (i < nimp) {
+          if (v != kPairEmpty) {
+            st_shared_u64(&s_x[a.chunk + i], v);
+            i += 32;
+            v = i < nimp ? ld_relaxed_u64(&a.xw[a.im_q[i0 + i]]) : kPairEmpty;
+            progress = true;
+          } else {
+            v = ld_relaxed_u64(&a.xw[a.im_q[i0 + i]]);
+          }
+        }
+        if (__all_sync(0xffffffffu, i >= nimp)) break;
+        if (!__any_sync(0xffffffffu, progress) && ((++idle & 15u) == 0u)) {
+          if (__any_sync(0xffffffffu, !wb.poll(a.ctl, base))) {
+            fail = true;
+            break;
+          }
+        }
+      }
+    } else {
+      // A warp takes every ncw-th segment; the row and list bounds of its next
+      // segment are loaded while it works on the current one.
+      int n_row = 0, n_e = 0, n_e1 = 0;
+      auto fetch = [&](int sg) {
+        const int jj = sg * 32 + lane;
+        if (jj < len) {
+          n_row = a.perm[base + jj];
+          n_e = a.dep_ptr[base + jj];
+          n_e1 = a.dep_ptr[base + jj + 1];
+        }
+      };
+      if (warp * 32 < len) fetch(warp);
+      for (int seg = warp; seg * 32 < len && !fail; seg += ncw) {
+        const int j = seg * 32 + lane;
+        bool done = j >= len;
+        const int p = base + j;
+        const int row = n_row;
+        int e = n_e;
+        const int e1 = n_e1;
+        if ((seg + ncw) * 32 < len) fetch(seg + ncw);
+        float acc0 = 0.f, rlo = 0.f, accd = 0.f;
+        if (!done) {
+          // b/d as a float pair: hi = RN32(b*s), lo = RN32(b*s - hi)
+          const double bv = a.b[(long long)row * a.b_si];
+          const double s64 = a.rcp64[p];
+          const float hi = __double2float_rn(bv * s64);
+          acc0 = hi;
+          rlo = __double2float_rn(__fma_rn(bv, s64, -widen(hi)));
+        }
+        int ls[U];
+        float wh[U], wl[U];
+        Bits bits[U];
+        unsigned todo = 0u;
+        auto load_batch = [&]() {
+          todo = 0u;
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            const int ee = e + u;
+            ls[u] = ee < e1 ? a.dep_slot[ee] : -1;
+            const float2 ws = ee < e1 ? a.wsplit[ee] : make_float2(0.f, 0.f);
+            wh[u] = ws.x;
+            wl[u] = ws.y;
+          }
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            bits[u] = kPairEmpty;
+            if (ls[u] >= 0) {
+              bits[u] = ld_shared_u64(&s_x[ls[u]]);
+              todo |= 1u << u;
+            }
+          }
+        };
+        if (!done) load_batch();
+        WaitBudget wb(a.timeout_ns);
+        unsigned idle = 0u;
+        for (;;) {
+          bool progress = false;
+          if (!done) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+              if (!(todo & (1u << u))) continue;
+              if (bits[u] != kPairEmpty) {
+                df_sub_product(acc0, rlo, wh[u], wl[u], pair_x0(bits[u]));
+                accd = fmaf(-wh[u], pair_d(bits[u]), accd);
+                todo &= ~(1u << u);
+                progress = true;
+              }
+            }
+            if (!todo) {
+              e += U;
+              if (e < e1) {
+                load_batch();
+              } else {
+                // rho = S - x0 is the pair's low part
+                accd = __fadd_rn(rlo, accd);  // accd holds d from here on
+                const Bits v = pack_pair(acc0, accd);
+                st_shared_u64(&s_x[j], v);
+                st_relaxed_u64(&a.xw[p], v);
+                done = true;
+              }
+              progress = true;
+            } else {
+#pragma unroll
+              for (int u = 0; u < U; ++u)
+                if ((todo & (1u << u)) && bits[u] == kPairEmpty) bits[u] = ld_shared_u64(&s_x[ls[u]]);
+            }
+          }
+          // no lane consumed anything: nothing was published, so the
+          // completion vote is skipped
+          if (__any_sync(0xffffffffu, progress)) {
+            if (__all_sync(0xffffffffu, done)) break;
+          } else if (((++idle & 255u) == 0u) && __any_sync(0xffffffffu, !wb.poll(a.ctl, p))) {
+            fail = true;
+            break;
+          }
+        }
+        // x = x0 + d and the stopping-estimate maxima, once the segment is done:
+        // off the lockstep iterations, on which the in-warp hops wait
+        if (!fail && j < len) {
+          a.x[(long long)row * a.x_si] = widen(acc0) + widen(accd);
+          mx_d = fmaxf(mx_d, fabsf(accd));
+          mx_x = fmaxf(mx_x, fabsf(acc0 + accd));
+          mx_x0 = fmaxf(mx_x0, fabsf(acc0));
         }
       }
     }
@@ -391,6 +578,59 @@ cudaError_t launch_refine_fused(const Layout& L, const Values<float>& v32, const
   if (rhs <= 16) return run_refine1<16, 1, 2, false>(a, block, smem, num_sms, s);
   if (rhs <= 32) return run_refine1<32, 1, 2, false>(a, block, smem, num_sms, s);
   return run_refine1<32, 2, 2, false>(a, block, smem, num_sms, s);
+}
+
+cudaError_t launch_refine_fused_imported(const Layout& L, const Values<double>& v64, const float2* wsplit,
+                                         const double* b, double* x, unsigned long long* xw,
+                                         unsigned long long* stats, DeviceCtl* ctl, const ExecConfig& cfg,
+                                         unsigned long long timeout_ns, int num_sms, cudaStream_t s,
+                                         const ImportTable& im) {
+  if (L.n == 0) return cudaSuccess;
+  RefineArgs a{};
+  a.n = L.n;
+  a.rhs = 1;
+  a.chunk = im.width;  // the window: first import slot
+  a.nchunks = im.nchunks;
+  a.ctas_per_sm = cfg.ctas_per_sm;
+  a.perm = L.perm;
+  a.dep_ptr = L.dep_ptr;
+  a.dep_pos_f = L.dep_pos_f;
+  a.rcp64 = v64.rcp;
+  a.wsplit = wsplit;
+  a.b = b;
+  a.x = x;
+  a.b_si = a.x_si = 1;
+  a.b_sk = a.x_sk = L.n;
+  a.xw = xw;
+  a.stats = stats;
+  a.ctl = ctl;
+  a.timeout_ns = timeout_ns;
+  a.im_start = im.start;
+  a.im_ptr = im.ptr;
+  a.im_q = im.q;
+  a.dep_slot = im.dep_slot;
+  const size_t smem = (size_t)(im.width + im.max_imports) * sizeof(unsigned long long);
+  const int block = cfg.block + 32;
+  auto launch = [&](auto kernel) -> cudaError_t {
+    if (smem > 48 * 1024) {
+      const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
+    if (per_sm < 1) per_sm = 1;
+    if (a.ctas_per_sm > 0 && per_sm > a.ctas_per_sm) per_sm = a.ctas_per_sm;
+    long long grid = (long long)num_sms * per_sm;
+    if (grid > a.nchunks) grid = a.nchunks;
+    if (grid < 1) grid = 1;
+    kernel<<<static_cast<int>(grid), block, smem, s>>>(a);
+    return cudaGetLastError();
+  };
+  switch (cfg.wsync_batch) {
+    case 1: return launch(k_pull_refine1_imp<1>);
+    case 4: return launch(k_pull_refine1_imp<4>);
+    default: return launch(k_pull_refine1_imp<2>);
+  }
 }
 
 // (hi, lo) float pairs of the FP64 weights for the DF fused pass:

@@ -301,6 +301,14 @@ cudaError_t launch_refine_fused(const Layout& L, const Values<float>& v32, const
                                 unsigned long long timeout_ns, int num_sms, cudaStream_t s,
                                 const float2* wsplit = nullptr);
 cudaError_t launch_split_weights(const double* w, long long count, float2* out, cudaStream_t s);
+// The same fused step (double-float residual, one right-hand side, b and x
+// vectors) on a blocked layout, with an importer warp per CTA (the table of
+// launch_pull_imported)
+cudaError_t launch_refine_fused_imported(const Layout& L, const Values<double>& v64, const float2* wsplit,
+                                         const double* b, double* x, unsigned long long* xw,
+                                         unsigned long long* stats, DeviceCtl* ctl, const ExecConfig& cfg,
+                                         unsigned long long timeout_ns, int num_sms, cudaStream_t s,
+                                         const ImportTable& im);
 cudaError_t launch_cast_d2f(const double* in, float* out, long long count, cudaStream_t s);
 cudaError_t launch_residual(const Layout& L, const Values<double>& V, int rhs, const double* b, const double* x,
                             long long si, long long sk, float* r, cudaStream_t s);

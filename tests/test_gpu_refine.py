@@ -154,3 +154,23 @@ def test_fused_refine_edge_structures(cuda, oracle_port, case):
             x, iters, est = s.solve_refine(cuda.from_numpy(B).cuda())
             assert relerr(x.cpu().numpy(), ref) <= TOL_FWD, (case, rhs, fused)
             s.close()
+
+
+@pytest.mark.parametrize("lower", [True, False])
+def test_fused_refine_on_blocked_layout_with_importer(cuda, oracle_port, lower):
+    """On a deep, narrow mesh the automatic plan picks a blocked layout; the fused
+    double-float step then runs with an importer warp per block. Same tolerance as
+    every refined solve, with the importer on and off."""
+    from sptrsv_gb300 import SyncFreeSolver, matgen
+    m = matgen.laplace2d_lower(600, lower=lower)
+    b_h = np.random.default_rng(7).standard_normal(m.n)
+    ref = oracle_port.solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, b_h)
+    b = cuda.from_numpy(b_h).cuda()
+    for imp in (True, False):
+        s = SyncFreeSolver(m.col_ptr, m.row_idx, m.n, m.substitution, values=m.val, import_deps=imp)
+        assert s.info()["order_block"] < m.n
+        for _ in range(2):
+            x, iters, est = s.solve_refine(b, tol=1e-12)
+            assert iters == 1 and est <= 1e-12
+            assert relerr(x.cpu().numpy(), ref) <= TOL_FWD, imp
+        s.close()
