@@ -1550,8 +1550,8 @@ cudaError_t launch_grad_values(const int* csc_row, const int* csc_col, int nnz, 
 // in_degree counts down from the analysed in-degree; a column is ready when
 // its count reaches 1. The caller zeroes left_sum and restores in_degree
 // between solves, as with the reference. A row index outside [0, m) is never
-// written through: the column's warp records DEV_BAD_INPUT and every warp
-// stops at its next ticket. With `gate` set and *gate non-zero (structural
+// written through: the lane that meets it records DEV_BAD_INPUT and skips it,
+// and every warp stops at its next ticket or wait. With `gate` set and *gate non-zero (structural
 // flags raised earlier in the stream) nothing is solved and DEV_BAD_INPUT is
 // recorded.
 __device__ __forceinline__ void raise_bad_input(DeviceCtl* ctl, int where) {
@@ -1592,38 +1592,47 @@ __global__ void __launch_bounds__(128) k_ref_exec(const int* __restrict__ col_pt
     // Lanes over right-hand sides (RHS mode) or over entries (NNZ mode); AUTO
     // follows the reference's rule (sptrsv_syncfree_cuda.h:262).
     const bool rhs_mode = rhs > 1 && (opt == 2 || (opt == 3 && (len <= rhs || rhs > 16) && len < 2048));
-    // rows outside [0, m) would write past the counters and partial sums
-    bool bad_row = false;
-    for (int e = s0 + lane; e < s1; e += 32)
-      bad_row |= static_cast<unsigned>(row_idx[e]) >= static_cast<unsigned>(m);
-    if (__any_sync(0xffffffffu, bad_row)) {
-      if (lane == 0) raise_bad_input(ctl, col);
-      break;
-    }
     for (int k = lane; k < rhs; k += 32) {
       const long long p = (long long)col * rhs + k;
       x[p] = (b[p] - Flag<T>::value(Flag<T>::load(&left_sum[p]))) * coef;
     }
     __syncwarp();
+    // a row outside [0, m) would write past the counters and partial sums: it is
+    // skipped and recorded (the other warps stop at their next ticket or wait)
+    const unsigned mm = static_cast<unsigned>(m);
     if (rhs_mode) {
       for (int e = s0; e < s1; ++e) {
         const int r = row_idx[e];
+        if (static_cast<unsigned>(r) >= mm) {
+          if (lane == 0) raise_bad_input(ctl, col);
+          continue;
+        }
         const T v = val[e];
         for (int k = lane; k < rhs; k += 32) atomicAdd(&left_sum[(long long)r * rhs + k], x[(long long)col * rhs + k] * v);
       }
       __syncwarp();
       if (lane == 0) {
         __threadfence();
-        for (int e = s0; e < s1; ++e) atomicSub(&in_degree[row_idx[e]], 1);
+        for (int e = s0; e < s1; ++e) {
+          const int r = row_idx[e];
+          if (static_cast<unsigned>(r) < mm) atomicSub(&in_degree[r], 1);
+        }
       }
     } else {
       for (int e = s0 + lane; e < s1; e += 32) {
         const int r = row_idx[e];
+        if (static_cast<unsigned>(r) >= mm) {
+          raise_bad_input(ctl, col);
+          continue;
+        }
         const T v = val[e];
         for (int k = 0; k < rhs; ++k) atomicAdd(&left_sum[(long long)r * rhs + k], x[(long long)col * rhs + k] * v);
       }
       __threadfence();
-      for (int e = s0 + lane; e < s1; e += 32) atomicSub(&in_degree[row_idx[e]], 1);
+      for (int e = s0 + lane; e < s1; e += 32) {
+        const int r = row_idx[e];
+        if (static_cast<unsigned>(r) < mm) atomicSub(&in_degree[r], 1);
+      }
     }
   }
   if (lane == 0) {
