@@ -959,10 +959,11 @@ ExecConfig pick_config(const sptrsv_gb300_handle_s* h, int rhs) {
     if (planned(h, SPTRSV_OPTION_WARP_SYNC)) c.wsync = h->plan.wsync;
   } else if (rhs > 1 && h->sched_option == SCHED_AUTO && h->plan.valid) {
     // many rhs: warp-synchronous lane groups (up to 64 rhs), one unknown per group
-    // per chunk; for narrow groups (rhs <= 4) a single CTA per SM measured fastest
-    // on one system, two on the 512-system batch (24.8 vs 30.0 ms)
+    // per chunk; two CTAs per SM up to 8 rhs (the 1M-row band system at 4 / 8 rhs:
+    // 1.025 / 1.027 ms against 1.073 / 1.064 with one or with every CTA that
+    // fits), every CTA that fits beyond (16 rhs: 1.13 ms against 1.45 with two)
     if (planned(h, SPTRSV_OPTION_WARP_SYNC)) c.wsync = rhs <= 64 ? 1 : 0;
-    if (planned(h, SPTRSV_OPTION_CTAS_PER_SM)) c.ctas_per_sm = rhs <= 4 ? (h->batch_count > 1 ? 2 : 1) : 0;
+    if (planned(h, SPTRSV_OPTION_CTAS_PER_SM)) c.ctas_per_sm = rhs <= 8 ? 2 : 0;
     if (planned(h, SPTRSV_OPTION_BACKOFF_NS)) c.sleep_max = 0u;  // spinning measured 1-3 % faster at 16 and 64 rhs
     // a blocked layout: one CTA per order block (small chunks would hand the
     // blocks out one after another); the shared-memory tier does not fit there
@@ -1709,15 +1710,17 @@ int sptrsv_gb300_solve_refine(sptrsv_handle_t h, const double* d_val, int rhs, i
   if (fuse) {
     // X_0, the FP64 residual and the first FP32 correction in one pass: X = X_0 + D_1
     if (rhs == 1 && fc.wsync_batch == 0) fc.wsync_batch = (long long)(h->nnz - h->n) > 3LL * (long long)h->n ? 1 : 2;
-    // level order: one CTA of 256 threads per SM up to 4 right-hand sides (two
-    // for batches); beyond, three with the FP64 residual and every CTA that fits
-    // (four) with the double-float one, which holds fewer registers (measured
-    // on the 1M-row band and power-law systems and the 512-system batch: the
-    // pass reads more per dependency than a plain solve, and fewer polling
-    // warps paid up to 4 right-hand sides; at 16 / 64 the double-float pass
-    // took 1.34 / 2.78 ms with three and 1.23 / 2.43 ms with four)
+    // level order: one CTA of 256 threads per SM for one right-hand side on one
+    // system, two up to 4 right-hand sides (and for batches); beyond, three with
+    // the FP64 residual and every CTA that fits (four) with the double-float
+    // one, which holds fewer registers (measured on the 1M-row band system and
+    // the 512-system batch: the pass reads more per dependency than a plain
+    // solve, and fewer polling warps paid with few right-hand sides — rhs 1:
+    // 1.19 ms with one, 1.21 with two; rhs 4: 1.245 with two, 1.29 with one; at
+    // 16 / 64 the double-float pass took 1.34 / 2.78 ms with three and 1.23 /
+    // 2.43 ms with four)
     if (h->sched_option == SCHED_AUTO && planned(h, SPTRSV_OPTION_CTAS_PER_SM) && h->layout_block >= h->n)
-      fc.ctas_per_sm = rhs <= 4 ? (h->batch_count > 1 ? 2 : 1) : (h->fused_refine == 2 ? 0 : 3);
+      fc.ctas_per_sm = rhs <= 4 ? (rhs == 1 && h->batch_count == 1 ? 1 : 2) : (h->fused_refine == 2 ? 0 : 3);
     ST_TRY(ensure_buf(h, h->xw, sizeof(unsigned long long) * count, 0, s));
     CUDA_TRY(cudaMemsetAsync(h->xw.p, 0xFF, sizeof(unsigned long long) * count, s));
     CUDA_TRY(cudaMemsetAsync(stats, 0, 3 * sizeof(unsigned long long), s));
