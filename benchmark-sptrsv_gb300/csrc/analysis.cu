@@ -614,10 +614,12 @@ __global__ void k_schedule_keys(const int* __restrict__ rows, const int* __restr
     if (mode == 0) {
       keys[i] = static_cast<unsigned>(depth[r]);
     } else if (mode == 2) {
-      // the level stretched to the batch's depth: floor(level * D / D_s) grows
-      // strictly with the level inside system s (D >= D_s)
-      const long long ds = sys_depth[sd.sys_of[r]];
-      keys[i] = static_cast<unsigned>((long long)depth[r] * max_depth / (ds > 0 ? ds : 1));
+      // the level stretched to max(D_s, T) keys, T = max_depth (the stretch
+      // target): floor(level * max(D_s, T) / D_s) grows strictly with the
+      // level inside system s
+      const long long ds = sys_depth[sd.sys_of[r]] > 0 ? sys_depth[sd.sys_of[r]] : 1;
+      const long long span = ds > max_depth ? ds : max_depth;
+      keys[i] = static_cast<unsigned>((long long)depth[r] * span / ds);
     } else {
       long long off, nat;
       nat_of(sd, n, r, &off, &nat);

@@ -212,7 +212,8 @@ cudaError_t launch_levels(const int* col_ptr, const int* row_idx, const int* in_
                           int* cnt_scratch, int* front_a, int* front_b, int* depth, int* level_sizes,
                           DeviceCtl* ctl, unsigned long long timeout_ns, cudaStream_t s);
 // mode 0: level; 1: (natural block, system) of blocked orders; 2: the level
-// stretched to the batch depth, floor(level * max_depth / sys_depth[system])
+// stretched to a target of max_depth keys, floor(level * max(D_s, max_depth) /
+// D_s) with D_s = sys_depth[system]
 cudaError_t launch_schedule_keys(const int* rows, const int* depth, int n, const SysDesc& sd, int block,
                                  int mode, unsigned* keys, cudaStream_t s, const int* sys_depth = nullptr,
                                  int max_depth = 0);

@@ -137,9 +137,10 @@ typedef enum sptrsv_option {
                                      lane covers, 1, 2 or 4 (so 4-32 lanes per unknown); 0 (default) =
                                      one per lane up to 32 right-hand sides, two beyond */
   SPTRSV_OPTION_STRETCH = 24      /* batches in level order (not the level-set schedule): 1 (default) =
-                                     the schedule key of an unknown is its level stretched to the
-                                     batch's depth, floor(level * depth(batch) / depth(system)), so every
-                                     system's chain spreads over the whole launch instead of a deep
+                                     the schedule key of an unknown is its level stretched to T =
+                                     65 % of the batch's depth (or to its system's depth, if deeper),
+                                     floor(level * max(T, depth(system)) / depth(system)), so every
+                                     system's chain spreads over most of the launch instead of a deep
                                      system waiting behind the shallow systems' wide levels; 0 = global
                                      level order */
 } sptrsv_option;
