@@ -799,9 +799,15 @@ int effective_block(const sptrsv_gb300_handle_s* h) {
 // Automatic one-rhs executor plan. Wide level sets (or a batch): global level
 // order, warp-synchronous lanes, one CTA of 256 threads per SM (fewer polling
 // warps, measured faster than full occupancy). Deep, narrow DAGs whose
-// dependencies stay local in the natural order (>= 90 % of the entries inside
+// dependencies stay local in the natural order (>= 96 % of the entries inside
 // blocks of 32 level widths): level order inside such blocks, one CTA per
-// block with in-block hops through shared memory.
+// block with in-block hops through shared memory. Measured on 160k-row band
+// systems with 1-16 entries per column and bands of 100-2000 rows: blocked
+// orders won at 965-976 permille local (band 100: 2.84 vs 4.33 ms with two
+// entries, 13.1 vs 17.5 with twelve), and lost at 925-953 (band 300: 3.83 vs
+// 2.77 ms with four entries, 13.6 vs 9.1 with sixteen; band 2000 with two:
+// 1.93 vs 0.40 ms), where too many hops leave the block and the wider levels
+// are better spread over every SM.
 //
 // Lists are split over lanes only where a few lists are far longer than the
 // rest: > 5 % of the entries in lists longer than max(32, 4 x the mean list
@@ -856,7 +862,7 @@ int make_plan(sptrsv_gb300_handle_s* h, const std::vector<int>& row_ptr, cudaStr
       CUDA_TRY(cudaStreamSynchronize(s));
       CUDA_TRY(cudaFree(d_count));
       P.locality = static_cast<double>(count) / static_cast<double>(nnz - n);
-      if (P.locality >= 0.9) {
+      if (P.locality >= 0.96) {
         P.order_block = blk;
         P.chunk = blk;
         P.block = 128;

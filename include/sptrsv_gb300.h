@@ -67,7 +67,7 @@ typedef enum sptrsv_dtype {
 typedef enum sptrsv_schedule {
   SPTRSV_SCHED_AUTO = 0,      /* pull executor with a plan chosen from the analysis (one rhs: warp-
                                  synchronous lanes; level order, or level order inside blocks of ~32
-                                 level widths when >= 90 % of the dependencies stay inside them);
+                                 level widths when >= 96 % of the dependencies stay inside them);
                                  options the caller sets explicitly override the plan */
   SPTRSV_SCHED_PUSH = 1,      /* in-degree counters + atomic partial sums (the reference scheme) */
   SPTRSV_SCHED_PULL = 2,      /* dependency gather with value-as-flag words (deterministic) */
