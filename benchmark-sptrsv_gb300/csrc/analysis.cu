@@ -522,6 +522,43 @@ cudaError_t launch_block_locality(const int* row, const int* col, int nnz, int n
   return cudaGetLastError();
 }
 
+// Unknowns with two or more dependencies on the level just before their own
+// (count[0]; in a warp-synchronous loop those dependencies land in the same
+// iteration) and unknowns with any dependency (count[1]), over the CSR rows
+// (diagonal included in each row and skipped here).
+__global__ void k_coarrival(const int* __restrict__ row_ptr, const int* __restrict__ col,
+                            const int* __restrict__ depth, int n, unsigned long long* count) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  unsigned co = 0, any = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int prev = depth[i] - 1;
+    int k = 0, deps = 0;
+    for (int e = row_ptr[i]; e < row_ptr[i + 1]; ++e) {
+      const int c = col[e];
+      if (c == i) continue;
+      ++deps;
+      k += depth[c] == prev ? 1 : 0;
+    }
+    co += k >= 2 ? 1u : 0u;
+    any += deps > 0 ? 1u : 0u;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    co += __shfl_xor_sync(0xffffffffu, co, o);
+    any += __shfl_xor_sync(0xffffffffu, any, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (co) atomicAdd(&count[0], (unsigned long long)co);
+    if (any) atomicAdd(&count[1], (unsigned long long)any);
+  }
+}
+
+cudaError_t launch_coarrival(const int* row_ptr, const int* col, const int* depth, int n, unsigned long long* count,
+                             cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_coarrival<<<grid_for(n), kThreads, 0, s>>>(row_ptr, col, depth, n, count);
+  return cudaGetLastError();
+}
+
 // ------------------------------------------------------------ level sets
 // Breadth-first peeling of the in-degree, one grid barrier per level
 // (the level definition of SpTRSV_cuda/findlevel.h:6-69): level 0 holds rows

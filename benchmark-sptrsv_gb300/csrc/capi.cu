@@ -49,7 +49,7 @@ struct sptrsv_gb300_handle_s {
   int fused_grad = 0;
   int wsync = 0;
   int split = 32;
-  int wsync_batch = 0;   // 0: automatic (2 for short lists, else 1)
+  int wsync_batch = 0;   // 0: automatic (auto_wsync_batch)
   int opt_option = SPTRSV_OPT_WARP_AUTO;  // push, many rhs: the reference's lane mode
   int rhs_tile_option = 0;                // many rhs: right-hand sides per lane (0: automatic)
   int stretch_option = 1;                 // batches in level order: levels stretched to the batch depth
@@ -60,6 +60,7 @@ struct sptrsv_gb300_handle_s {
     int order_block = INT_MAX, chunk = 256, block = 256, ctas = 2, backoff = 0, staged = 0, wsync = 1;
     int split_fwd = 0, split_adj = 0;  // split length for the forward / transposed walk (0: none)
     double locality = 0.0;
+    double coarrive = 0.0;  // short lists: share of unknowns with >= 2 dependencies on the preceding level
   } plan;
   // analysis
   bool analysed = false;
@@ -848,6 +849,17 @@ int make_plan(sptrsv_gb300_handle_s* h, const std::vector<int>& row_ptr, cudaStr
       const long long width = ((long long)n + nl - 1) / nl;
       P.ctas = width < 1536 ? 1 : (width < 8192 ? 2 : 3);
     }
+    if (nnz > n && (long long)(nnz - n) <= 3LL * (long long)n) {
+      unsigned long long* d_count = nullptr;
+      CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&d_count), 2 * sizeof(unsigned long long), s));
+      CUDA_TRY(cudaMemsetAsync(d_count, 0, 2 * sizeof(unsigned long long), s));
+      CUDA_TRY(launch_coarrival(h->csr_ptr, h->csr_col, h->depth, n, d_count, s));
+      unsigned long long count[2] = {0, 0};
+      CUDA_TRY(cudaMemcpyAsync(count, d_count, sizeof(count), cudaMemcpyDeviceToHost, s));
+      CUDA_TRY(cudaStreamSynchronize(s));
+      CUDA_TRY(cudaFree(d_count));
+      P.coarrive = count[1] ? static_cast<double>(count[0]) / static_cast<double>(count[1]) : 0.0;
+    }
   }
   if (n > 0 && nl >= 256 && h->batch_count == 1 && nnz > n) {
     const long long width = ((long long)n + nl - 1) / nl;
@@ -939,6 +951,22 @@ bool pipe_ready(sptrsv_gb300_handle_s* h, int chunk, cudaStream_t s) {
   }
   return t.ustage != nullptr &&
          unit_smem_bytes(t.ring, t.max_imports, t.pmax, t.emax, t.smax, t.stages, sizeof(T)) <= 220 * 1024;
+}
+
+// Dependencies a lane loads per lockstep iteration (one rhs) when the caller
+// left it open. Forward walks over lists averaging more than 3 entries: one
+// (the shortest iteration; ready-ordered lists let the earlier entries land
+// long before the last). Shorter lists: two when at least half of the unknowns
+// have two or more dependencies on the level just before their own, which
+// land in the same iteration (the mesh triangle in level order: 16.1 ms with
+// two, 18.6 with one), else one (160k-row bands with 1 / 2 entries per column
+// 0.087 / 1.79 ms with two, 0.072 / 1.42 with one; a 1M-row band with 3
+// entries 6.42 vs 5.37 ms; a 20k-row chain on the importer executor 5.24 vs
+// 4.02 ms). Split lists and the transposed walk: two.
+int auto_wsync_batch(const sptrsv_gb300_handle_s* h, bool adj, bool split) {
+  if (adj || split) return 2;
+  if ((long long)(h->nnz - h->n) > 3LL * (long long)h->n) return 1;
+  return h->plan.coarrive >= 0.5 ? 2 : 1;
 }
 
 // Automatic executor settings for a request.
@@ -1050,7 +1078,7 @@ int solve_typed(sptrsv_gb300_handle_s* h, const Values<T>& V, int rhs, int layou
              imported_smem_bytes(h->imports.width, h->imports.max_imports, sizeof(T)) <= 220 * 1024) {
     // blocked layout: an importer warp per CTA brings the chunk's external dependencies
     // into shared memory
-    if (c.wsync_batch == 0) c.wsync_batch = (long long)(h->nnz - h->n) > 3LL * (long long)h->n ? 1 : 2;
+    if (c.wsync_batch == 0) c.wsync_batch = auto_wsync_batch(h, false, false);
     CUDA_TRY(launch_pull_imported<T>(h->layout, V, v, static_cast<T*>(h->xw.p), h->ctl, c, timeout_ns(h),
                                      h->num_sms, s, h->imports));
   } else {
@@ -1061,15 +1089,7 @@ int solve_typed(sptrsv_gb300_handle_s* h, const Values<T>& V, int rhs, int layou
       ST_TRY(ensure_pieces(h, adj != nullptr, c.split, c.chunk, s));
       pc = adj ? &h->pc_adj : &h->pc_fwd;
     }
-    if (c.wsync_batch == 0) {
-      // dependencies per lane per lockstep iteration (measured): one for forward
-      // walks over lists averaging more than 3 entries with one lane per unknown
-      // (the shortest iteration; the earlier entries of a ready-ordered list land
-      // early), two otherwise (short lists, whose entries land together, the
-      // split executor, and the transposed walk)
-      const bool long_avg = (long long)(h->nnz - h->n) > 3LL * (long long)h->n;
-      c.wsync_batch = (!adj && !pc && long_avg) ? 1 : 2;
-    }
+    if (c.wsync_batch == 0) c.wsync_batch = auto_wsync_batch(h, adj != nullptr, pc != nullptr);
     CUDA_TRY(launch_pull<T>(h->layout, V, rhs, v, static_cast<T*>(h->xw.p), h->ctl, c, timeout_ns(h), h->num_sms,
                             s, adj, pc));
   }
@@ -1574,6 +1594,17 @@ int sptrsv_gb300_get_info(sptrsv_handle_t h, sptrsv_info* info) {
   info->split = planned(h, SPTRSV_OPTION_SPLIT) ? h->plan.split_fwd : c.split;
   info->locality_permille = static_cast<int>(h->plan.locality * 1000.0 + 0.5);
   info->unit_pipeline = h->last_pipe ? 1 : 0;
+  if (c.wsync_batch > 0) {
+    info->wsync_batch = c.wsync_batch;
+  } else {
+    // the forward walk of a plain solve: the importer executor on a blocked
+    // layout, else the level-order executor with or without split lists
+    const bool imported = c.wsync && !c.exact && h->import_option && h->layout_block < h->n &&
+                          c.chunk == h->layout_block && c.smem_tier && !(c.split > 0 && h->max_dep_cnt > c.split);
+    const bool split = !imported && c.wsync && !c.exact && info->split > 0 && h->max_dep_cnt > info->split;
+    info->wsync_batch = auto_wsync_batch(h, false, split);
+  }
+  info->coarrive_permille = static_cast<int>(h->plan.coarrive * 1000.0 + 0.5);
   return h->analysed ? SPTRSV_OK : SPTRSV_ERR_STATE;
 }
 
@@ -1720,7 +1751,11 @@ int sptrsv_gb300_solve_refine(sptrsv_handle_t h, const double* d_val, int rhs, i
   }
   if (fuse) {
     // X_0, the FP64 residual and the first FP32 correction in one pass: X = X_0 + D_1
-    if (rhs == 1 && fc.wsync_batch == 0) fc.wsync_batch = (long long)(h->nnz - h->n) > 3LL * (long long)h->n ? 1 : 2;
+    // the plain solve's rule (160k-row bands with 1 / 2 entries per column and a
+    // 1M-row band with 3: 0.101 / 1.95 / 6.40 ms refined with two dependencies
+    // per iteration, 0.082 / 1.54 / 5.62 with one; the mesh triangle with two:
+    // 0.28 vs 0.61 ms)
+    if (rhs == 1 && fc.wsync_batch == 0) fc.wsync_batch = auto_wsync_batch(h, false, false);
     // level order: one CTA of 256 threads per SM for one right-hand side on one
     // system, two up to 4 right-hand sides (and for batches); beyond, three with
     // the FP64 residual and every CTA that fits (four) with the double-float

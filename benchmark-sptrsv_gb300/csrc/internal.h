@@ -234,6 +234,10 @@ cudaError_t launch_fill_push(const int* perm, const int* iperm, const int* col_p
 // unknowns in the natural execution order.
 cudaError_t launch_block_locality(const int* row, const int* col, int nnz, int n, int block, bool backward,
                                   unsigned long long* count, cudaStream_t s);
+// count[0] += unknowns with two or more dependencies on the level just before
+// their own, count[1] += unknowns with any dependency (CSR rows, depth per row).
+cudaError_t launch_coarrival(const int* row_ptr, const int* col, const int* depth, int n, unsigned long long* count,
+                             cudaStream_t s);
 // Sorts every list [ptr[p], ptr[p+1]) of (pos, src) by pos (descending when asked).
 cudaError_t launch_sort_lists(const int* ptr, const int* pos, const int* src, int n, int count, bool descending,
                               int* pos_out, int* src_out, cudaStream_t s);

@@ -101,6 +101,8 @@ class Info(ctypes.Structure):
         ("split", ctypes.c_int),
         ("locality_permille", ctypes.c_int),
         ("unit_pipeline", ctypes.c_int),
+        ("wsync_batch", ctypes.c_int),
+        ("coarrive_permille", ctypes.c_int),
     ]
 
 

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define SPTRSV_GB300_VERSION 100
+#define SPTRSV_GB300_VERSION 101
 
 /* Substitution and multi-RHS lane modes: same values as common.h:25-30. */
 #define SPTRSV_SUBSTITUTION_FORWARD 0
@@ -104,8 +104,11 @@ typedef enum sptrsv_option {
                                      than this many entries are split over up to 32 lanes (default 32;
                                      0 = one lane per unknown) */
   SPTRSV_OPTION_WSYNC_BATCH = 18, /* warp-synchronous one-rhs pull (not exact): dependencies a lane loads
-                                     per lockstep iteration, 1, 2 or 4 (0 = automatic: 2 when the lists
-                                     average <= 3 entries, else 1) */
+                                     per lockstep iteration, 1, 2 or 4 (0 = automatic: 1 for lists
+                                     averaging more than 3 entries; for shorter ones 2 when at least half
+                                     of the unknowns have two or more dependencies on the level just
+                                     before their own, else 1; 2 for split lists and the transposed walk;
+                                     sptrsv_info.wsync_batch reports the forward walk's value) */
   SPTRSV_OPTION_IMPORT = 19,      /* 1 (default): warp-synchronous one-rhs forward pull on a blocked
                                      layout (chunk = order block) gives each CTA an importer warp that
                                      copies the chunk's external dependencies into shared memory */
@@ -167,6 +170,9 @@ typedef struct sptrsv_info {
   int split;            /* split length of the forward walk (0: one lane per unknown) */
   int locality_permille; /* automatic plan: dependencies inside order blocks, per mille */
   int unit_pipeline;    /* 1: the last one-rhs solve ran the unit pipeline (SPTRSV_OPTION_UNIT_PIPELINE) */
+  int wsync_batch;      /* dependencies per lane per lockstep iteration of the forward one-rhs walk */
+  int coarrive_permille; /* lists of <= 3 entries on average: unknowns with two or more dependencies
+                            on the level just before their own, per mille (0 otherwise) */
 } sptrsv_info;
 
 typedef struct sptrsv_gb300_handle_s *sptrsv_handle_t;

@@ -36,7 +36,7 @@ def test_binding_covers_header():
 
 def test_status_strings_and_version(built_lib):
     from sptrsv_gb300 import _lib
-    assert built_lib.sptrsv_gb300_version() == 100
+    assert built_lib.sptrsv_gb300_version() == 101
     for code in range(-9, 1):
         s = _lib.status_string(code)
         assert s and s != "unknown status"

@@ -64,6 +64,29 @@ def test_blocked_order_follows_the_locality_threshold(cuda, oracle_port, band, b
     assert relerr(s.solve(cuda.from_numpy(b).cuda()).cpu().numpy(), ref) <= TOL64
 
 
+def test_dependencies_per_iteration_follow_co_arrival(cuda, oracle_port):
+    """One dependency per lockstep iteration unless at least half of the unknowns
+    have two or more dependencies on the level just before their own (the mesh
+    triangle: both neighbours sit one level up and land together); lists
+    averaging more than 3 entries take one; an explicit option wins."""
+    from sptrsv_gb300 import matgen
+    cases = [(matgen.laplace2d_lower(200), {}, 2), (matgen.poisson_band(40_000, 2.0, 300, seed=21), {}, 1),
+             (matgen.chain(5000), {}, 1), (matgen.poisson_band(20_000, 9.0, 400, seed=22), {}, 1),
+             (matgen.laplace2d_lower(200), {"wsync_batch": 4}, 4)]
+    for m, kw, want in cases:
+        s = _solver(m, **kw)
+        inf = s.info()
+        assert inf["wsync_batch"] == want, (m.n, kw, inf)
+        if (m.nnz - m.n) > 3 * m.n:
+            assert inf["coarrive_permille"] == 0
+        elif not kw:
+            assert (inf["coarrive_permille"] >= 500) == (want == 2)
+        b = np.random.default_rng(m.n).standard_normal(m.n)
+        ref = oracle_port.solve(m.col_ptr, m.row_idx, m.val, m.n, m.substitution, b)
+        assert relerr(s.solve(cuda.from_numpy(b).cuda()).cpu().numpy(), ref) <= TOL64
+        s.close()
+
+
 def test_wide_dag_stays_in_level_order(cuda, oracle_port):
     from sptrsv_gb300 import matgen
     m = matgen.poisson_band(20_000, 9.0, 4000, seed=5)     # dependencies spread over 4000 rows
