@@ -87,6 +87,31 @@ def test_dependencies_per_iteration_follow_co_arrival(cuda, oracle_port):
         s.close()
 
 
+@pytest.mark.parametrize("which", ["mesh", "band", "random"])
+def test_coarrival_count_matches_the_oracle_levels(cuda, oracle_port, which):
+    """sptrsv_info.coarrive_permille against a count over the oracle's level sets
+    (findlevel.h:6-69): unknowns with two or more dependencies on the level just
+    before their own, per mille of the unknowns with any dependency."""
+    from sptrsv_gb300 import matgen
+    m = {"mesh": lambda: matgen.laplace2d_lower(120, lower=False),
+         "band": lambda: matgen.poisson_band(30_000, 2.0, 300, seed=23),
+         "random": lambda: matgen.random_small(3000, 0.002, seed=3)}[which]()
+    assert m.nnz - m.n <= 3 * m.n
+    nl, level_ptr, level_item = oracle_port.findlevel(m.col_ptr, m.row_idx, m.n)
+    level = np.empty(m.n, dtype=np.int64)
+    for lv in range(nl):
+        level[level_item[level_ptr[lv]:level_ptr[lv + 1]]] = lv
+    col = np.repeat(np.arange(m.n), np.diff(m.col_ptr))
+    off = m.row_idx != col
+    rows, deps = m.row_idx[off], col[off]                  # row depends on column
+    prev = np.bincount(rows, weights=(level[deps] == level[rows] - 1), minlength=m.n)
+    anyd = np.bincount(rows, minlength=m.n) > 0
+    want = int(np.sum(prev >= 2) / np.sum(anyd) * 1000.0 + 0.5)
+    s = _solver(m)
+    assert s.info()["coarrive_permille"] == want
+    s.close()
+
+
 def test_wide_dag_stays_in_level_order(cuda, oracle_port):
     from sptrsv_gb300 import matgen
     m = matgen.poisson_band(20_000, 9.0, 4000, seed=5)     # dependencies spread over 4000 rows
