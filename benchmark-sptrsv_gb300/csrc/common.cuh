@@ -155,8 +155,10 @@ __device__ __forceinline__ bool ctl_failed(const DeviceCtl* ctl) {
 }
 
 // Grid-wide barrier for cooperative launches (all CTAs co-resident). Bounded:
-// returns false if the wait runs out or another CTA already failed.
-__device__ __forceinline__ bool grid_barrier(DeviceCtl* ctl, unsigned long long limit_ns) {
+// returns false if the wait runs out or another CTA already failed. Waiting
+// CTAs back off from smin to smax nanoseconds between polls.
+__device__ __forceinline__ bool grid_barrier(DeviceCtl* ctl, unsigned long long limit_ns, unsigned smin = 32u,
+                                             unsigned smax = 256u) {
   __syncthreads();
   __shared__ int s_ok;
   if (threadIdx.x == 0) {
@@ -170,7 +172,7 @@ __device__ __forceinline__ bool grid_barrier(DeviceCtl* ctl, unsigned long long 
       __threadfence();
       red_release_add_u32(&ctl->barrier_gen, 1u);
     } else {
-      WaitBudget w(limit_ns, 32, 256);
+      WaitBudget w(limit_ns, smin, smax);
       while (ld_acquire_u32(&ctl->barrier_gen) == gen) {
         if (!w.poll(ctl, -1)) { ok = 0; break; }
       }
