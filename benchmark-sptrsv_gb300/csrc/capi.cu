@@ -1079,6 +1079,7 @@ int solve_typed(sptrsv_gb300_handle_s* h, const Values<T>& V, int rhs, int layou
     // blocked layout: an importer warp per CTA brings the chunk's external dependencies
     // into shared memory
     if (c.wsync_batch == 0) c.wsync_batch = auto_wsync_batch(h, false, false);
+    c.one_batch = h->max_dep_cnt <= c.wsync_batch ? 1 : 0;
     CUDA_TRY(launch_pull_imported<T>(h->layout, V, v, static_cast<T*>(h->xw.p), h->ctl, c, timeout_ns(h),
                                      h->num_sms, s, h->imports));
   } else {
@@ -1799,6 +1800,7 @@ int sptrsv_gb300_solve_refine(sptrsv_handle_t h, const double* d_val, int rhs, i
                           h->imports.ptr != nullptr &&
                           imported_smem_bytes(h->imports.width, h->imports.max_imports, 8) <= 220 * 1024;
     if (imported) {
+      fc.one_batch = h->max_dep_cnt <= fc.wsync_batch ? 1 : 0;
       CUDA_TRY(launch_refine_fused_imported(h->layout, h->v64, wsplit, d_b, d_x,
                                             static_cast<unsigned long long*>(h->xw.p), stats, h->ctl, fc,
                                             timeout_ns(h), h->num_sms, s, h->imports));

@@ -321,10 +321,11 @@ __global__ void __launch_bounds__(256) k_pull_wsync(ExecArgs<T> a) {
               progress = true;
             }
           } else {
+            // every entry still pending is unpublished (arrived ones were consumed
+            // above; in exact order a reload of an arrived one reads the same word)
 #pragma unroll
             for (int u = 0; u < U; ++u)
-              if ((todo & (1u << u)) && bits[u] == F::EMPTY)
-                bits[u] = ls[u] >= 0 ? F::load_shared(&s_x[ls[u]]) : F::load(&a.xw[q[u]]);
+              if (todo & (1u << u)) bits[u] = ls[u] >= 0 ? F::load_shared(&s_x[ls[u]]) : F::load(&a.xw[q[u]]);
           }
         }
         // no lane consumed anything: nothing was published, so the completion
@@ -361,8 +362,9 @@ __global__ void __launch_bounds__(256) k_pull_wsync(ExecArgs<T> a) {
 // in the order they are published) from global memory and copies each value
 // into a shared-memory slot as it lands. The consumer warps then resolve every
 // dependency in shared memory (slot from dep_slot), so their iterations stay
-// short. Fast arithmetic, one rhs, forward walks.
-template <typename T, int U>
+// short. Fast arithmetic, one rhs, forward walks. ONE: every list holds at most
+// U entries, so a lane publishes once its first batch is consumed.
+template <typename T, int U, bool ONE>
 __global__ void __launch_bounds__(288) k_pull_wsync_imp(ExecArgs<T> a) {
   using F = Flag<T>;
   using Bits = typename F::Bits;
@@ -502,8 +504,8 @@ __global__ void __launch_bounds__(288) k_pull_wsync_imp(ExecArgs<T> a) {
               }
             }
             if (!todo) {
-              e += U;
-              if (e < e1) {
+              if (!ONE) e += U;
+              if (!ONE && e < e1) {
                 load_batch();
               } else {
                 F::store_shared(&s_x[j], acc);
@@ -514,8 +516,8 @@ __global__ void __launch_bounds__(288) k_pull_wsync_imp(ExecArgs<T> a) {
               progress = true;
             } else {
 #pragma unroll
-              for (int u = 0; u < U; ++u)
-                if ((todo & (1u << u)) && bits[u] == F::EMPTY) bits[u] = F::load_shared(&s_x[ls[u]]);
+              for (int u = 0; u < U; ++u)  // pending entries are unpublished: arrived ones were consumed
+                if (todo & (1u << u)) bits[u] = F::load_shared(&s_x[ls[u]]);
             }
           }
           // no lane consumed anything: nothing was published, so the
@@ -644,6 +646,8 @@ __device__ __forceinline__ bool wsync_segment(const ExecArgs<T>& a, T* s_x, int 
         }
         progress = true;
       } else {
+        // (the re-poll keeps its empty check here: without it, the same loads
+        // measured 12 % slower on the power-law backward walk)
 #pragma unroll
         for (int u = 0; u < U; ++u)
           if ((todo & (1u << u)) && bits[u] == F::EMPTY)
@@ -1402,10 +1406,17 @@ cudaError_t launch_pull_imported(const Layout& L, const Values<T>& V, const VecV
   a.nchunks = im.nchunks;
   const size_t smem = (size_t)(im.width + im.max_imports) * sizeof(T);
   const int block = cfg.block + 32;
+  const bool one = cfg.one_batch != 0;
   switch (cfg.wsync_batch) {
-    case 1: return run(k_pull_wsync_imp<T, 1>, a, block, smem, num_sms, s);
-    case 4: return run(k_pull_wsync_imp<T, 4>, a, block, smem, num_sms, s);
-    default: return run(k_pull_wsync_imp<T, 2>, a, block, smem, num_sms, s);
+    case 1:
+      return one ? run(k_pull_wsync_imp<T, 1, true>, a, block, smem, num_sms, s)
+                 : run(k_pull_wsync_imp<T, 1, false>, a, block, smem, num_sms, s);
+    case 4:
+      return one ? run(k_pull_wsync_imp<T, 4, true>, a, block, smem, num_sms, s)
+                 : run(k_pull_wsync_imp<T, 4, false>, a, block, smem, num_sms, s);
+    default:
+      return one ? run(k_pull_wsync_imp<T, 2, true>, a, block, smem, num_sms, s)
+                 : run(k_pull_wsync_imp<T, 2, false>, a, block, smem, num_sms, s);
   }
 }
 

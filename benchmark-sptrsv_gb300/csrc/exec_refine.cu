@@ -342,8 +342,9 @@ __global__ void __launch_bounds__(256) k_pull_refine1(RefineArgs a) {
 // consumer warps that resolve every dependency in shared memory (slot from
 // dep_slot), one lane per unknown in lockstep. Without the importer the
 // consumer warps' lockstep iterations would wait on L2 polls of the few
-// cross-block dependencies.
-template <int U>
+// cross-block dependencies. ONE: every list holds at most U entries, so a lane
+// publishes once its first batch is consumed.
+template <int U, bool ONE>
 __global__ void __launch_bounds__(288) k_pull_refine1_imp(RefineArgs a) {
   using Bits = unsigned long long;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -459,8 +460,8 @@ __global__ void __launch_bounds__(288) k_pull_refine1_imp(RefineArgs a) {
               }
             }
             if (!todo) {
-              e += U;
-              if (e < e1) {
+              if (!ONE) e += U;
+              if (!ONE && e < e1) {
                 load_batch();
               } else {
                 // rho = S - x0 is the pair's low part
@@ -473,8 +474,8 @@ __global__ void __launch_bounds__(288) k_pull_refine1_imp(RefineArgs a) {
               progress = true;
             } else {
 #pragma unroll
-              for (int u = 0; u < U; ++u)
-                if ((todo & (1u << u)) && bits[u] == kPairEmpty) bits[u] = ld_shared_u64(&s_x[ls[u]]);
+              for (int u = 0; u < U; ++u)  // pending entries are unpublished: arrived ones were consumed
+                if (todo & (1u << u)) bits[u] = ld_shared_u64(&s_x[ls[u]]);
             }
           }
           // no lane consumed anything: nothing was published, so the
@@ -626,10 +627,11 @@ cudaError_t launch_refine_fused_imported(const Layout& L, const Values<double>& 
     kernel<<<static_cast<int>(grid), block, smem, s>>>(a);
     return cudaGetLastError();
   };
+  const bool one = cfg.one_batch != 0;
   switch (cfg.wsync_batch) {
-    case 1: return launch(k_pull_refine1_imp<1>);
-    case 4: return launch(k_pull_refine1_imp<4>);
-    default: return launch(k_pull_refine1_imp<2>);
+    case 1: return one ? launch(k_pull_refine1_imp<1, true>) : launch(k_pull_refine1_imp<1, false>);
+    case 4: return one ? launch(k_pull_refine1_imp<4, true>) : launch(k_pull_refine1_imp<4, false>);
+    default: return one ? launch(k_pull_refine1_imp<2, true>) : launch(k_pull_refine1_imp<2, false>);
   }
 }
 

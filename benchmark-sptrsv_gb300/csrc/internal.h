@@ -40,6 +40,7 @@ struct ExecConfig {
   int wsync_batch = 4;    // warp-synchronous one rhs, fast arithmetic: dependencies per lane per iteration
   int opt = 3;            // push, many rhs: the reference's lane mode (1 entries, 2 rhs, 3 automatic rule)
   int rhs_tile = 0;       // many rhs: right-hand sides per lane (1, 2, 4; 0: automatic)
+  int one_batch = 0;      // importer executor: every list fits one lockstep batch (no batch reloads)
 };
 
 // Lane group of the many-rhs executors: G lanes per unknown (a power of two,
