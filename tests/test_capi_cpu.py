@@ -69,3 +69,29 @@ def test_option_constants_match_header():
     for name, value in opts.items():
         assert getattr(_lib, f"OPTION_{name}") == value, name
     assert sorted(opts.values()) == list(range(len(opts)))
+
+
+def test_info_struct_layout_matches_header(tmp_path):
+    """The ctypes mirror of sptrsv_info has the C struct's size and every field at the
+    C offset (a plain C program compiled against the header prints them)."""
+    import shutil
+    import subprocess
+    from sptrsv_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        import pytest
+        pytest.skip("no C compiler")
+    fields = [name for name, _ in _lib.Info._fields_]
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "sptrsv_gb300.h"', "int main(void) {",
+             '  printf("size %zu\\n", sizeof(sptrsv_info));']
+    lines += [f'  printf("{f} %zu\\n", offsetof(sptrsv_info, {f}));' for f in fields]
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "info_layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "info_layout"
+    subprocess.run([cc, "-std=c99", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    out = dict(line.split() for line in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                        text=True).stdout.splitlines())
+    assert int(out.pop("size")) == ctypes.sizeof(_lib.Info)
+    for f in fields:
+        assert int(out[f]) == getattr(_lib.Info, f).offset, f
