@@ -95,3 +95,19 @@ def test_info_struct_layout_matches_header(tmp_path):
     assert int(out.pop("size")) == ctypes.sizeof(_lib.Info)
     for f in fields:
         assert int(out[f]) == getattr(_lib.Info, f).offset, f
+
+
+def test_enum_and_define_constants_match_header():
+    """Every SPTRSV_* enumerator and numeric #define in the header (statuses, layouts,
+    element types, schedules, substitution and lane-mode constants, the no-alloc size)
+    has the same value in the binding, named without the SPTRSV_ prefix."""
+    import re
+    from sptrsv_gb300 import _lib
+    text = re.sub(r"/\*.*?\*/", "", (ROOT / "include" / "sptrsv_gb300.h").read_text(), flags=re.S)
+    consts = {m.group(1): int(m.group(2)) for m in re.finditer(r"\bSPTRSV_([A-Z0-9_]+)\s*=\s*(-?\d+)", text)}
+    consts.update({m.group(1): int(m.group(2))
+                   for m in re.finditer(r"#define\s+SPTRSV_([A-Z0-9_]+)\s+\(?(-?\d+)\)?\s*$", text, flags=re.M)})
+    consts.pop("GB300_VERSION", None)
+    assert {"OK", "ERR_UNSUPPORTED", "LAYOUT_COL_MAJOR", "DTYPE_F32", "SCHED_LEVELSET", "OPT_WARP_AUTO"} <= set(consts)
+    for name, value in consts.items():
+        assert getattr(_lib, name) == value, name
