@@ -51,7 +51,7 @@ typedef enum sptrsv_status {
   SPTRSV_ERR_OOM = -6,            /* device allocation failed */
   SPTRSV_ERR_STATE = -7,          /* call out of order (e.g. solve before analyse) */
   SPTRSV_ERR_NOT_CONVERGED = -8,  /* iterative refinement missed its tolerance */
-  SPTRSV_ERR_UNSUPPORTED = -9     /* valid request this build does not serve */
+  SPTRSV_ERR_UNSUPPORTED = -9     /* valid request the library does not serve */
 } sptrsv_status;
 
 typedef enum sptrsv_layout {

@@ -1,6 +1,6 @@
 """Python access to the CPU oracle.
 
-TEST INFRASTRUCTURE ONLY: the checker for the CUDA library. Only the test
+TEST INFRASTRUCTURE ONLY: what the CUDA library's results are compared with. Only the test
 suite, the smoke check and the benchmark's CPU-baseline leg use this module;
 the library never calls it and there is no CPU fallback.
 

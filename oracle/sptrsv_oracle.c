@@ -1,9 +1,10 @@
 /*
  * CPU oracle for the sync-free sparse triangular solve.
  *
- * TEST INFRASTRUCTURE ONLY. This file is the checker: only the test suite,
- * the smoke check and the benchmark's CPU-baseline leg load it. The library
- * (the CUDA path) never links or calls it, and there is no CPU fallback.
+ * TEST INFRASTRUCTURE ONLY: the CUDA library's results are compared with
+ * it. Only the test suite, the smoke check and the benchmark's CPU-baseline
+ * leg load it. The library (the CUDA path) never links or calls it, and there
+ * is no CPU fallback.
  *
  * It restates, in plain C, the reference's serial algorithm for this path
  * (harunsasmaz/Benchmark-SpTRSV, directory SpTRSV_cuda/):
